@@ -1,0 +1,247 @@
+/*
+ * nlmgpu.h -- C ABI of the GB300 peridynamics library (libnlmgpu.so).
+ *
+ * The library replaces the explicit-dynamics hot path of NLMech
+ * (nonlocalmodels/NLMech): the horizon neighbour search, the RNPBond and
+ * ElasticState bond-force loops, bond breaking / damage, and the
+ * velocity-Verlet and central-difference integrators of FDModel.
+ *
+ * Conventions
+ *  - Every array argument is a caller-owned HOST buffer.  Node vectors use the
+ *    reference's util::Point3 layout: 3 doubles (x, y, z) per node, so a
+ *    std::vector<util::Point3> can be passed as (const double*)&v[0].
+ *  - Node and bond indices at the boundary are the caller's ("original")
+ *    node ids.  Neighbour rows are returned in ascending id order, which is
+ *    the order geometry::Neighbor builds them (src/geometry/neighbor.cpp:78).
+ *  - Bond state is returned as one byte per CSR entry (0 = intact,
+ *    1 = broken) in that same row order, i.e. the bit that
+ *    geometry::Fracture::getBondState(i, j_local) returns
+ *    (src/geometry/fracture.cpp:174-187).
+ *  - Every call returns an int status (NLM_OK = 0).  Nothing calls exit();
+ *    nlm_last_error() gives a message for the calling thread.
+ *  - A handle owns one CUDA stream and its device memory.  A handle is not
+ *    thread-safe; distinct handles are independent.
+ */
+#ifndef NLMGPU_H
+#define NLMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NLM_ABI_VERSION 1
+
+/* ---- status codes ---------------------------------------------------- */
+enum {
+  NLM_OK = 0,
+  NLM_ERR_INVALID = 1,     /* bad argument / inconsistent description   */
+  NLM_ERR_CUDA = 2,        /* CUDA runtime error                        */
+  NLM_ERR_OOM = 3,         /* device allocation failed                  */
+  NLM_ERR_TIMEOUT = 4,     /* a bounded device wait gave up             */
+  NLM_ERR_UNSUPPORTED = 5, /* option not implemented on this path       */
+  NLM_ERR_STATE = 6,       /* call out of order for the handle          */
+  NLM_ERR_NONFINITE = 7    /* NaN / Inf found in an input array         */
+};
+
+/* ---- enums mirroring the reference's deck strings ---------------------- */
+enum nlm_material_kind {
+  NLM_MAT_RNP_BOND = 0,      /* material::pd::RNPBond (rnpBond.cpp)        */
+  NLM_MAT_ELASTIC_STATE = 1  /* material::pd::ElasticState (ElasticState.cpp) */
+};
+
+enum nlm_precision {
+  NLM_PREC_FP64 = 0,  /* "plain": every bond in FP64, reference op order   */
+  NLM_PREC_FP32C = 1  /* "compensated": FP32 bond math on split hi/lo
+                         positions and displacements, FP64 state/update   */
+};
+
+enum nlm_scheme {
+  NLM_VELOCITY_VERLET = 0,     /* "velocity_verlet"   fDModel.cpp:445-525 */
+  NLM_CENTRAL_DIFFERENCE = 1   /* "central_difference" fDModel.cpp:376-443 */
+};
+
+enum nlm_decomposition {
+  NLM_DECOMP_AUTO = 0,   /* pick by the autotuner                        */
+  NLM_DECOMP_THREAD = 1, /* one thread per node, sliced-ELL bond storage  */
+  NLM_DECOMP_WARP = 2    /* one warp per node, CSR bond storage           */
+};
+
+/* Displacement_BC / Force_BC region types (loading/uLoading.cpp:38-46). */
+enum nlm_region {
+  NLM_REGION_RECTANGLE = 0, /* x in [x1,x2], y in [y1,y2] (utilGeom.cpp:43) */
+  NLM_REGION_LINE = 1,      /* x1 < x < x2 (1-D)                          */
+  NLM_REGION_CIRCLE = 2,    /* |x - (x1,y1)| < r1                          */
+  NLM_REGION_TORUS = 3,     /* r2 <= |x - (x1,y1)| < r1                    */
+  NLM_REGION_CUBOID = 4     /* 3-D box [x1,x2]x[y1,y2]x[z1,z2] (extension) */
+};
+
+enum nlm_time_fn { /* uLoading.cpp:210-236 */
+  NLM_TFN_CONSTANT = 0,
+  NLM_TFN_LINEAR = 1,
+  NLM_TFN_QUADRATIC = 2,
+  NLM_TFN_SIN = 3,
+  NLM_TFN_LINEAR_STEP = 4,
+  NLM_TFN_LINEAR_SLOW_FAST = 5
+};
+
+enum nlm_spatial_fn { /* uLoading.cpp:186-208 */
+  NLM_SFN_CONSTANT = 0,
+  NLM_SFN_SIN_X = 1,
+  NLM_SFN_SIN_Y = 2,
+  NLM_SFN_SIN_Z = 3,
+  NLM_SFN_LINEAR_X = 4,
+  NLM_SFN_LINEAR_Y = 5,
+  NLM_SFN_LINEAR_Z = 6
+};
+
+enum nlm_crack_kind {
+  NLM_CRACK_EDGE = 0,  /* inp::EdgeCrack, 2-D (fractureDeck.h:115-186)      */
+  NLM_CRACK_PLANE = 1  /* planar patch z = z0 over [x0,x1]x[y0,y1] (3-D)    */
+};
+
+enum nlm_no_fail {
+  NLM_NOFAIL_OFF = 0,     /* BaseInterior: every node interior            */
+  NLM_NOFAIL_COMPUTE = 1, /* ComputeInterior: bbox minus tolerance        */
+  NLM_NOFAIL_DATA = 2     /* DataInterior: stored flags (all set)         */
+};
+
+/* ---- descriptions --------------------------------------------------- */
+
+/* One Displacement_BC or Force_BC set (inp::BCData). */
+typedef struct nlm_bc_set {
+  int region;            /* enum nlm_region                              */
+  double x1, x2, y1, y2; /* region box / centre                          */
+  double z1, z2;         /* NLM_REGION_CUBOID only                       */
+  double r1, r2;         /* circle / torus radii                         */
+  int dir_mask;          /* bit d set = dof d (0:x 1:y 2:z), "Direction"  */
+  int time_fn;           /* enum nlm_time_fn                             */
+  double time_params[4];
+  int spatial_fn;        /* enum nlm_spatial_fn                          */
+  double spatial_params[2];
+} nlm_bc_set;
+
+/* One pre-crack (inp::EdgeCrack with activation time < 0, or a 3-D plane). */
+typedef struct nlm_crack {
+  int kind;            /* enum nlm_crack_kind                              */
+  int orientation;     /* EdgeCrack d_o: 1 = along x, -1 = along y, 0 = angle */
+  double pb[2], pt[2]; /* EdgeCrack "Line": bottom/left and top/right ends */
+  double theta;        /* EdgeCrack angle for orientation 0               */
+  double z0;           /* plane kind: plane height                        */
+  double lo[2], hi[2]; /* plane kind: patch [lo0,hi0] x [lo1,hi1]          */
+} nlm_crack;
+
+/* inp::MaterialDeck fields used on the hot path (materialDeck.h). */
+typedef struct nlm_material {
+  int kind;                 /* enum nlm_material_kind                      */
+  double density;
+  double E, G, K, Gc, KIc;  /* < 0 means "not given" (deck default -1)     */
+  int plane_strain;         /* Is_Plane_Strain                             */
+  int influence_type;       /* 0 const, 1 linear, 2 Gaussian (influenceFn.h) */
+  int n_influence_params;
+  double influence_params[2];
+  int irreversible;         /* Irreversible_Bond_Fracture (default 1)      */
+  double check_sc_factor;   /* Check_Sc_Factor (default 1)                 */
+  int compute_from_classical; /* Compute_From_Classical (default 1)        */
+  double bond_params[2];    /* C, beta when not computed from classical    */
+  double es_sc;             /* ElasticState critical stretch; <= 0: no breaking */
+  int es_ref_compat;        /* 1: keep the reference's 3-D e_d = 0          */
+} nlm_material;
+
+typedef struct nlm_fd_desc {
+  int dim;                  /* 1, 2 or 3                                   */
+  int64_t n_nodes;
+  const double *x;          /* 3*n reference coordinates (Point3 layout)   */
+  const double *volume;     /* n nodal volumes                             */
+  double horizon;           /* Model.Horizon                               */
+  double mesh_size;         /* h (Model.Mesh_Size or Horizon/Horizon_h_Ratio) */
+  nlm_material material;
+  int n_ubc;                /* Displacement_BC sets                        */
+  const nlm_bc_set *ubc;
+  int n_fbc;                /* Force_BC sets                               */
+  const nlm_bc_set *fbc;
+  int n_cracks;
+  const nlm_crack *cracks;
+  int no_fail;              /* enum nlm_no_fail                            */
+  double no_fail_tol;       /* horizon * No_Fail_Region.Factor             */
+  double dt;                /* Final_Time / Time_Steps                     */
+  int scheme;               /* enum nlm_scheme                             */
+  int precision;            /* enum nlm_precision                          */
+  int decomposition;        /* enum nlm_decomposition                      */
+  const double *u0;         /* optional 3*n initial displacement (or NULL) */
+  const double *v0;         /* optional 3*n initial velocity (or NULL)     */
+} nlm_fd_desc;
+
+/* ---- library ---------------------------------------------------------- */
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *nlm_last_error(void);
+int nlm_abi_version(void);
+/* Number of CUDA devices visible (0 on a host without a GPU). */
+int nlm_device_count(int *count);
+
+/* ---- neighbour search (replaces geometry::Neighbor, neighbor.cpp:24-92) --
+ * Builds rows {j != i : definitelyLessThan(|x_i - x_j|, horizon + 1e-10)}
+ * with a uniform cell list on the GPU.  Two calls: first with cols == NULL
+ * to get rowptr (n+1 entries, rowptr[n] = nnz), then with cols of nnz. */
+int nlm_neighbor_search(int dim, int64_t n, const double *x, double horizon,
+                        int64_t *rowptr, int32_t *cols);
+
+/* ---- explicit finite-difference model (replaces model::FDModel<T>) ----- */
+typedef struct nlm_fd nlm_fd;
+
+/* Uploads the mesh, builds neighbours, applies pre-cracks and BC tables
+ * (FDModel::initHObjects + init, fDModel.cpp:133-315). */
+int nlm_fd_create(const nlm_fd_desc *desc, nlm_fd **out);
+int nlm_fd_destroy(nlm_fd *h);
+
+/* Number of directed bonds (sum of neighbour row lengths). */
+int nlm_fd_num_bonds(const nlm_fd *h, int64_t *nnz);
+/* Neighbour lists in original ids, rows ascending (rowptr n+1, cols nnz). */
+int nlm_fd_get_neighbors(nlm_fd *h, int64_t *rowptr, int32_t *cols);
+
+/* Advance nsteps time steps (FDModel::integrate, fDModel.cpp:317-374).  The
+ * first call also performs the step-0 work: initial loads and forces. */
+int nlm_fd_run(nlm_fd *h, int64_t nsteps);
+
+/* Copy state out: u, v, f are 3*n (any may be NULL).  f is the force
+ * density of the last force evaluation (external + internal). */
+int nlm_fd_get_state(nlm_fd *h, double *u, double *v, double *f);
+/* Overwrite u and v (3*n each, either may be NULL). */
+int nlm_fd_set_state(nlm_fd *h, const double *u, const double *v);
+/* Time and step counter (d_time, d_n). */
+int nlm_fd_get_time(const nlm_fd *h, double *time, int64_t *step);
+/* Bond state, one byte per CSR entry in nlm_fd_get_neighbors order. */
+int nlm_fd_get_bond_state(nlm_fd *h, uint8_t *broken);
+/* Damage fields of FDModel::computePostProcFields (fDModel.cpp:651-778):
+ * phi_i = 1 - sum_unbroken V_j^c / sum V_j^c and Z_i = max_j |S|/S_c.
+ * Either pointer may be NULL. */
+int nlm_fd_damage(nlm_fd *h, float *phi, float *Z);
+/* Number of broken bonds (directed). */
+int nlm_fd_count_broken(nlm_fd *h, int64_t *count);
+/* Work decomposition actually used (enum nlm_decomposition). */
+int nlm_fd_decomposition(const nlm_fd *h, int *decomp);
+/* Average device time of the bond-force kernel over the launches since the
+ * last reset (milliseconds), measured with CUDA events on the handle's
+ * stream; and the algorithmic bytes one launch moves. */
+int nlm_fd_kernel_stats(nlm_fd *h, int reset, double *avg_ms,
+                        int64_t *launches, double *bytes_per_launch);
+/* Enable/disable per-launch event timing of the force kernel. */
+int nlm_fd_set_timing(nlm_fd *h, int enable);
+/* Synchronize the handle's stream. */
+int nlm_fd_sync(nlm_fd *h);
+
+/* Drop-in step for a host-resident state (the reference DataManager keeps
+ * u, v, f on the host): copies u, v in, advances nsteps, copies u, v and f
+ * out (f may be NULL).  Used by FDModel-shaped hosts that keep their own
+ * arrays. */
+int nlm_fd_step_host(nlm_fd *h, double *u, double *v, double *f,
+                     int64_t nsteps);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NLMGPU_H */

@@ -1,0 +1,201 @@
+"""ctypes binding of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by bench.py's CPU-baseline leg
+and by __graft_entry__.smoke() as the checker.  The product package
+(nlmech_gb300) never imports this module.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from nlmech_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+
+
+def build(force=False):
+    """Compile liboracle.so with the Makefile beside this file."""
+    src = [os.path.join(HERE, f) for f in ("nlm_oracle.cpp", "nlm_oracle.h")]
+    if (not force and os.path.exists(LIB)
+            and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in src)):
+        return LIB
+    subprocess.check_call(["make", "-s", "-C", HERE, "liboracle.so"])
+    return LIB
+
+
+class QSParams(C.Structure):
+    _fields_ = [
+        ("jacobian", C.c_int),
+        ("solver", C.c_int),
+        ("max_iters", C.c_int),
+        ("tol", C.c_double),
+        ("tol_relative", C.c_int),
+        ("perturbation", C.c_double),
+        ("lin_max_iters", C.c_int),
+        ("lin_tol", C.c_double),
+        ("dt", C.c_double),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        L.orc_last_error.restype = C.c_char_p
+        for nm in ("orc_fd_create", "orc_qs_create"):
+            getattr(L, nm).restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise RuntimeError("oracle error %d: %s" % (rc, lib().orc_last_error().decode()))
+
+
+def set_threads(n):
+    lib().orc_set_num_threads(int(n))
+
+
+def num_threads():
+    return int(lib().orc_num_threads())
+
+
+def neighbors(x, horizon, dim=2, grid=True):
+    """CSR neighbour lists (rowptr int64 n+1, cols int32), rows ascending."""
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+    n = x.shape[0]
+    rowptr = np.zeros(n + 1, dtype=np.int64)
+    L = lib()
+    fn = L.orc_neighbors_grid if grid else L.orc_neighbors_brute
+    args = ([C.c_int(dim)] if grid else []) + [C.c_int64(n), abi.dptr(x), C.c_double(horizon)]
+    _check(fn(*args, abi.ptr(rowptr, C.c_int64), C.POINTER(C.c_int32)()))
+    cols = np.zeros(int(rowptr[-1]), dtype=np.int32)
+    _check(fn(*args, abi.ptr(rowptr, C.c_int64), abi.ptr(cols, C.c_int32)))
+    return rowptr, cols
+
+
+def rnp_params(material, dim, horizon):
+    out = (C.c_double * 7)()
+    m = material.to_c()
+    _check(lib().orc_rnp_params(C.byref(m), C.c_int(dim), C.c_double(horizon), out))
+    keys = ("C", "beta", "rbar", "invF", "M", "nu", "lambda")
+    return dict(zip(keys, list(out)))
+
+
+class OracleFD:
+    """FDModel restated on the CPU (explicit dynamics)."""
+
+    def __init__(self, problem, grid_neighbors=True):
+        self.problem = problem
+        d, self._keep = problem.desc()
+        h = C.c_void_p()
+        _check(lib().orc_fd_create(C.byref(d), C.c_int(int(grid_neighbors)), C.byref(h)))
+        self.h = h
+        self.n = problem.n
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_fd_destroy(self.h)
+            self.h = None
+
+    def nnz(self):
+        v = C.c_int64()
+        _check(lib().orc_fd_num_bonds(self.h, C.byref(v)))
+        return v.value
+
+    def neighbors(self):
+        rowptr = np.zeros(self.n + 1, dtype=np.int64)
+        cols = np.zeros(self.nnz(), dtype=np.int32)
+        _check(lib().orc_fd_get_neighbors(self.h, abi.ptr(rowptr, C.c_int64), abi.ptr(cols, C.c_int32)))
+        return rowptr, cols
+
+    def run(self, nsteps):
+        _check(lib().orc_fd_run(self.h, C.c_int64(nsteps)))
+
+    def state(self):
+        u = np.zeros((self.n, 3))
+        v = np.zeros((self.n, 3))
+        f = np.zeros((self.n, 3))
+        _check(lib().orc_fd_get_state(self.h, abi.dptr(u), abi.dptr(v), abi.dptr(f)))
+        return u, v, f
+
+    def set_state(self, u=None, v=None):
+        u = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
+        v = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
+        _check(lib().orc_fd_set_state(self.h, abi.dptr(u), abi.dptr(v)))
+
+    def time(self):
+        t = C.c_double()
+        n = C.c_int64()
+        _check(lib().orc_fd_get_time(self.h, C.byref(t), C.byref(n)))
+        return t.value, n.value
+
+    def bond_state(self):
+        b = np.zeros(self.nnz(), dtype=np.uint8)
+        _check(lib().orc_fd_get_bond_state(self.h, abi.ptr(b, C.c_uint8)))
+        return b
+
+    def set_bond_state(self, b):
+        b = np.ascontiguousarray(b, dtype=np.uint8)
+        _check(lib().orc_fd_set_bond_state(self.h, abi.ptr(b, C.c_uint8)))
+
+    def fixity(self):
+        f = np.zeros(self.n, dtype=np.uint8)
+        _check(lib().orc_fd_get_fixity(self.h, abi.ptr(f, C.c_uint8)))
+        return f
+
+    def damage(self):
+        phi = np.zeros(self.n, dtype=np.float32)
+        Z = np.zeros(self.n, dtype=np.float32)
+        _check(lib().orc_fd_damage(self.h, abi.ptr(phi, C.c_float), abi.ptr(Z, C.c_float)))
+        return phi, Z
+
+    def es_fields(self):
+        om = np.zeros(self.nnz())
+        m = np.zeros(self.n)
+        th = np.zeros(self.n)
+        _check(lib().orc_fd_es_fields(self.h, abi.dptr(om), abi.dptr(m), abi.dptr(th)))
+        return om, m, th
+
+    def eval_force(self):
+        f = np.zeros((self.n, 3))
+        _check(lib().orc_fd_eval_force(self.h, abi.dptr(f)))
+        return f
+
+
+class OracleQS:
+    """QuasiStaticModel<ElasticState> restated on the CPU."""
+
+    def __init__(self, problem, params):
+        d, self._keep = problem.desc()
+        h = C.c_void_p()
+        self.params = params
+        _check(lib().orc_qs_create(C.byref(d), C.byref(params), C.byref(h)))
+        self.h = h
+        self.n = problem.n
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_qs_destroy(self.h)
+            self.h = None
+
+    def solve(self, nsteps):
+        iters = (C.c_int * nsteps)()
+        res = C.c_double()
+        _check(lib().orc_qs_solve(self.h, C.c_int(nsteps), iters, C.byref(res)))
+        return list(iters), res.value
+
+    def get(self):
+        u = np.zeros((self.n, 3))
+        f = np.zeros((self.n, 3))
+        nnz = C.c_int64()
+        _check(lib().orc_qs_get(self.h, abi.dptr(u), abi.dptr(f), C.byref(nnz)))
+        return u, f

@@ -1,0 +1,180 @@
+// fd_fp64.cu -- FP64 "plain" explicit-step kernels.
+//
+// Compiled with --fmad=false: every product and sum is rounded separately, in
+// the order of the reference expressions, so a bond force differs from the
+// reference's only by the last-ulp behaviour of exp().  One thread owns one
+// node and sums its bonds in neighbour-list order (ascending original id), as
+// FDModel::computeForce does (src/model/fd/fDModel.cpp:557-575).
+
+#include "fd_internal.h"
+#include "state_io.cuh"
+
+namespace nlm {
+
+// One RNPBond::getBondEF evaluation (src/material/pd/rnpBond.cpp:216-301),
+// contact force off.  Returns the scalar s of F = s * e and the unit vector e.
+template <int DIM>
+__device__ __forceinline__ double rnp_bond64(const StepParams &P, const double xi[3],
+                                             const double ui[3], const double xj[3],
+                                             const double uj[3], double volj,
+                                             bool breakable, bool &fs, double e[3]) {
+  double dx = xj[0] - xi[0], dy = xj[1] - xi[1];
+  double dz = DIM == 3 ? xj[2] - xi[2] : 0.0;
+  double rr = dx * dx + dy * dy;
+  if (DIM == 3) rr = rr + dz * dz;
+  double rji = sqrt(rr);  // xj.dist(xi), also dx.length()
+  double dux = uj[0] - ui[0], duy = uj[1] - ui[1];
+  double dotp = dx * dux + dy * duy;
+  if (DIM == 3) dotp = dotp + dz * (uj[2] - ui[2]);
+  double S = dotp / rr;  // getS, :303-306
+  e[0] = dx / rji;
+  e[1] = dy / rji;
+  e[2] = dz / rji;
+  if (dGT(rji, P.check_low)) volj = volj * ((P.check_up - rji) / P.h);  // :255-256
+  double infl = influence_d(P, rji / P.delta);
+  if (breakable) {
+    if (P.irrev && !fs && dGT(fabs(S), P.fsc * (P.rbar / sqrt(rji)))) fs = true;  // :263-266
+    if (fs) return 0.0;
+    return (infl * 4. * S * P.C * P.beta * exp(-P.beta * rji * S * S) / P.invF) * volj;
+  }
+  return (infl * 4. * S * P.C * P.beta / P.invF) * volj;  // :298
+}
+
+// Thread-per-node step over the sliced-ELL bond store.
+template <int DIM, int SCHEME, bool FIRST>
+__global__ void __launch_bounds__(128)
+    k_rnp64_thread(const StepParams P, const DevPtrs D, const BCTable T, const StepArgs A) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const double *ucur = D.u64[A.cur];
+  double xi[3], ui[3];
+  ld_node<DIM>(D.pos64, i, xi);
+  ld_node<DIM>(ucur, i, ui);
+  const uint8_t fl = D.flags[i];
+  const bool brk_i = !(fl & FLAG_NOFAIL);
+  const int64_t slice = i >> 5;
+  const int64_t base = D.sell_ptr[slice] + (i & 31);
+  const int w = D.sell_w[slice];
+  double fi[3] = {0., 0., 0.};
+  uint32_t word = 0;
+  bool dirty = false;
+  int chunk = 0;
+  for (int k = 0; k < w; k++) {
+    if ((k & 31) == 0) {
+      if (dirty) D.bits[(int64_t)chunk * P.npad + i] = word;
+      chunk = k >> 5;
+      word = D.bits[(int64_t)chunk * P.npad + i];
+      dirty = false;
+    }
+    const int j = __ldg(D.sell_cols + base + (int64_t)k * 32);
+    if (j < 0) break;
+    double xj[3], uj[3], e[3];
+    ld_node<DIM>(D.pos64, j, xj);
+    ld_node<DIM>(ucur, j, uj);
+    bool fs = (word >> (k & 31)) & 1u;
+    const bool was = fs;
+    bool breakable = brk_i;
+    if (P.nofail && breakable) breakable = !(D.flags[j] & FLAG_NOFAIL);
+    double s = rnp_bond64<DIM>(P, xi, ui, xj, uj, __ldg(D.vol64 + j), breakable, fs, e);
+    if (fs != was) {
+      word |= 1u << (k & 31);
+      dirty = true;
+    }
+    if (!fs || !breakable) {
+      fi[0] = fi[0] + s * e[0];
+      fi[1] = fi[1] + s * e[1];
+      if (DIM == 3) fi[2] = fi[2] + s * e[2];
+    }
+  }
+  if (dirty) D.bits[(int64_t)chunk * P.npad + i] = word;
+  integrate_node64<DIM, SCHEME, FIRST>(P, D, T, A, i, fl, ui, fi);
+}
+
+template <int DIM, int SCHEME>
+static cudaError_t launch_dim(const StepParams &P, const DevPtrs &D, const BCTable &T,
+                              const StepArgs &a, cudaStream_t s) {
+  const int bs = 128;
+  const unsigned grid = (unsigned)((P.n + bs - 1) / bs);
+  if (P.n == 0) return cudaSuccess;
+  if (a.first)
+    k_rnp64_thread<DIM, SCHEME, true><<<grid, bs, 0, s>>>(P, D, T, a);
+  else
+    k_rnp64_thread<DIM, SCHEME, false><<<grid, bs, 0, s>>>(P, D, T, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rnp_step_fp64(const StepParams &P, const DevPtrs &D, const BCTable &T,
+                                 const StepArgs &a, int decomp, cudaStream_t s) {
+  (void)decomp;  // the FP64 path keeps the reference summation order
+  if (P.dim == 2)
+    return P.scheme == NLM_VELOCITY_VERLET ? launch_dim<2, NLM_VELOCITY_VERLET>(P, D, T, a, s)
+                                           : launch_dim<2, NLM_CENTRAL_DIFFERENCE>(P, D, T, a, s);
+  return P.scheme == NLM_VELOCITY_VERLET ? launch_dim<3, NLM_VELOCITY_VERLET>(P, D, T, a, s)
+                                         : launch_dim<3, NLM_CENTRAL_DIFFERENCE>(P, D, T, a, s);
+}
+
+// FDModel::computePostProcFields, damage part (fDModel.cpp:651-778):
+// phi_i = 1 - a/b over corrected volumes, Z_i = max |S| / S_c(r).
+template <int DIM>
+__global__ void k_damage(const StepParams P, const DevPtrs D, int cur, bool fp32, bool es,
+                         float *phi, float *Z) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  double xi[3], ui[3];
+  ld_node<DIM>(D.pos64, i, xi);
+  if (fp32)
+    ld_split<DIM>(D.u32[cur], i, ui);
+  else
+    ld_node<DIM>(D.u64[cur], i, ui);
+  double a = 0., b = 0., z = 0.;
+  const int64_t r0 = D.rowptr[i], r1 = D.rowptr[i + 1];
+  for (int64_t k = r0; k < r1; k++) {
+    const int j = D.cols[k];
+    const int kk = (int)(k - r0);
+    const bool fs = (D.bits[(int64_t)(kk >> 5) * P.npad + i] >> (kk & 31)) & 1u;
+    double xj[3], uj[3];
+    ld_node<DIM>(D.pos64, j, xj);
+    if (fp32)
+      ld_split<DIM>(D.u32[cur], j, uj);
+    else
+      ld_node<DIM>(D.u64[cur], j, uj);
+    double dx = xj[0] - xi[0], dy = xj[1] - xi[1], dz = DIM == 3 ? xj[2] - xi[2] : 0.;
+    double rr = dx * dx + dy * dy;
+    if (DIM == 3) rr = rr + dz * dz;
+    double rji = sqrt(rr);
+    double volj = D.vol64[j];
+    if (dGT(rji, P.check_low)) volj = volj * ((P.check_up - rji) / P.h);
+    if (!fs) a += volj;
+    b += volj;
+    double sr = 0.;
+    if (!es) {
+      double dotp = dx * (uj[0] - ui[0]) + dy * (uj[1] - ui[1]);
+      if (DIM == 3) dotp = dotp + dz * (uj[2] - ui[2]);
+      double S = dotp / rr;
+      if (dGT(rji, 1.0E-12)) sr = fabs(S) / (P.rbar / sqrt(rji));
+    } else if (P.es_sc > 0.) {
+      double Y0 = (xj[0] + uj[0]) - (xi[0] + ui[0]);
+      double Y1 = (xj[1] + uj[1]) - (xi[1] + ui[1]);
+      double Y2 = DIM == 3 ? (xj[2] + uj[2]) - (xi[2] + ui[2]) : 0.;
+      double yl = sqrt(Y0 * Y0 + Y1 * Y1 + Y2 * Y2);
+      sr = fabs((yl - rji) / rji) / P.es_sc;
+    }
+    if (dLT(z, sr)) z = sr;
+  }
+  if (phi) phi[i] = (float)(b > 0. ? 1. - a / b : 0.);
+  if (Z) Z[i] = (float)z;
+}
+
+cudaError_t launch_damage(const StepParams &P, const DevPtrs &D, int cur, bool fp32, bool es,
+                          float *phi, float *Z, cudaStream_t s) {
+  if (P.n == 0) return cudaSuccess;
+  const int bs = 128;
+  const unsigned grid = (unsigned)((P.n + bs - 1) / bs);
+  if (P.dim == 2)
+    k_damage<2><<<grid, bs, 0, s>>>(P, D, cur, fp32, es, phi, Z);
+  else
+    k_damage<3><<<grid, bs, 0, s>>>(P, D, cur, fp32, es, phi, Z);
+  return cudaGetLastError();
+}
+
+}  // namespace nlm

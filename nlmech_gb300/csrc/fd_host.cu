@@ -1,0 +1,1083 @@
+// fd_host.cu -- C ABI of libnlmgpu: model set-up, time loop, state I/O.
+//
+// Replaces model::FDModel<T> (src/model/fd/fDModel.cpp) for T = RNPBond and
+// ElasticState.  Set-up mirrors FDModel::initHObjects/init (:133-315):
+// neighbour lists, pre-cracks, interior flags, loading tables, material
+// constants.  The time loop mirrors FDModel::integrate (:317-374).
+//
+// Phase bookkeeping of the fused step.  One launch K_m does, per node, the
+// force evaluation at u^m plus the integrator work on both sides of it:
+//   Verlet:  v^m = (v^{m-1} + c f^{m-1}) + c f^m;   u^{m+1} = u^m + dt (v^m + c f^m)
+//   CD:      u^{m+1} = u^m + (c' f^m + dt v^m);     v^{m+1} = (u^{m+1} - u^m) / dt
+// with c = dt/(2 rho), c' = dt^2/rho.  u is ping-ponged (u^m read, u^{m+1}
+// written); v is ping-ponged for CD.  After K_m the buffers hold exactly the
+// reference's (u^m, v^m, f^m), and u^{m+1} is already in the other buffer.
+// The velocity half-kick v^{m-1} + c f^{m-1} is recomputed from the stored
+// f^{m-1}, so every value is produced by the same sequence of roundings as
+// integrateVerlet.  K_0 (first = true) does the step-0 force evaluation of
+// integrate() (:319-333) and the drift of step 1.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fd_internal.h"
+#include "neighbor.h"
+#include "state_io.cuh"
+
+namespace nlm {
+
+static thread_local std::string g_err;
+void set_error(const std::string &msg) { g_err = msg; }
+int cuda_fail(cudaError_t e, const char *what) {
+  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return NLM_ERR_OOM;
+  return NLM_ERR_CUDA;
+}
+static int fail(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+
+// ---- host restatement of the deck-level set-up --------------------------
+static inline bool hGT(double a, double b) { return (a - b) > (amax_d(a, b) * 1e-5); }
+static inline bool hLT(double a, double b) { return (b - a) > (amax_d(a, b) * 1e-5); }
+
+// Displacement_BC / Force_BC region membership (uLoading.cpp:93-160,
+// fLoading.cpp:88-111, utilGeom.cpp:43-49,97-115,328-333).
+static bool in_region(const nlm_bc_set &bc, const double *p, int dim) {
+  switch (bc.region) {
+    case NLM_REGION_RECTANGLE:
+      return !(hLT(p[0], bc.x1 - 1.0E-12) || hLT(p[1], bc.y1 - 1.0E-12) ||
+               hGT(p[0], bc.x2 + 1.0E-12) || hGT(p[1], bc.y2 + 1.0E-12));
+    case NLM_REGION_LINE:
+      return hGT(p[0], bc.x1) && hLT(p[0], bc.x2);
+    case NLM_REGION_CIRCLE: {
+      const double d[3] = {p[0] - bc.x1, p[1] - bc.y1, p[2] - 0.};
+      return std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) <= bc.r1;
+    }
+    case NLM_REGION_TORUS: {
+      const double d[3] = {p[0] - bc.x1, p[1] - bc.y1, p[2] - 0.};
+      const double l = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      return l <= bc.r1 && !(l <= bc.r2);
+    }
+    case NLM_REGION_CUBOID:
+      if (dim < 3)
+        return !(hLT(p[0], bc.x1 - 1.0E-12) || hLT(p[1], bc.y1 - 1.0E-12) ||
+                 hGT(p[0], bc.x2 + 1.0E-12) || hGT(p[1], bc.y2 + 1.0E-12));
+      return !(hLT(p[0], bc.x1 - 1.0E-12) || hLT(p[1], bc.y1 - 1.0E-12) ||
+               hLT(p[2], bc.z1 - 1.0E-12) || hGT(p[0], bc.x2 + 1.0E-12) ||
+               hGT(p[1], bc.y2 + 1.0E-12) || hGT(p[2], bc.z2 + 1.0E-12));
+  }
+  return false;
+}
+
+// Spatial factor of ULoading::apply times time_params[0] (uLoading.cpp:172-208).
+static double uload_umax(const nlm_bc_set &bc, const double *x) {
+  double umax = bc.time_params[0];
+  const double *sp = bc.spatial_params;
+  switch (bc.spatial_fn) {
+    case NLM_SFN_SIN_X: { const double a = M_PI * sp[0]; umax = umax * std::sin(a * x[0]); } break;
+    case NLM_SFN_SIN_Y: { const double a = M_PI * sp[0]; umax = umax * std::sin(a * x[1]); } break;
+    case NLM_SFN_SIN_Z: { const double a = M_PI * sp[0]; umax = umax * std::sin(a * x[2]); } break;
+    case NLM_SFN_LINEAR_X: { const double a = sp[0]; umax = umax * a * x[0]; } break;
+    case NLM_SFN_LINEAR_Y: { const double a = sp[0]; umax = umax * a * x[1]; } break;
+    case NLM_SFN_LINEAR_Z: { const double a = sp[0]; umax = umax * a * x[2]; } break;
+    default: { const double a = sp[0]; umax = umax * a; } break;
+  }
+  return umax;
+}
+
+// Spatial part of FLoading::apply (fLoading.cpp:124-152).
+static double fload_spatial(const nlm_bc_set &bc, const double *x) {
+  const double *sp = bc.spatial_params;
+  switch (bc.spatial_fn) {
+    case NLM_SFN_SIN_X: { const double a = M_PI * sp[0]; return sp[0] * std::sin(a * x[0]); }
+    case NLM_SFN_SIN_Y: { const double a = M_PI * sp[0]; return sp[0] * std::sin(a * x[1]); }
+    case NLM_SFN_SIN_Z: { const double a = M_PI * sp[0]; return sp[0] * std::sin(a * x[2]); }
+    case NLM_SFN_LINEAR_X: { const double a = sp[0]; return sp[0] * a * x[0]; }
+    case NLM_SFN_LINEAR_Y: { const double a = sp[0]; return sp[0] * a * x[1]; }
+    case NLM_SFN_LINEAR_Z: { const double a = sp[0]; return sp[0] * a * x[2]; }
+    default: return sp[0];
+  }
+}
+
+// Time part of FLoading::apply (fLoading.cpp:246-266), applied as
+// fmax = (spatial * g(t)) * time_params[0].
+__device__ double fload_time(const BCTime &T, double fmax, double time) {
+  switch (T.fn) {
+    case NLM_TFN_LINEAR: fmax = fmax * time; break;
+    case NLM_TFN_LINEAR_STEP: {
+      const double x1 = T.p[1], x2 = T.p[2];
+      const double period = floor(time / (x1 + x2));
+      const double g = dLT(time, period * (x1 + x2) + x1) ? time - period * x2 : (period + 1.) * x1;
+      fmax = fmax * g;
+    } break;
+    case NLM_TFN_LINEAR_SLOW_FAST:
+      fmax = dGT(time, T.p[1]) ? fmax * (T.p[3] * time) : fmax * (T.p[2] * time);
+      break;
+    case NLM_TFN_SIN: fmax = fmax * sin((M_PI * T.p[1]) * time); break;
+    default: break;
+  }
+  return fmax * T.p[0];
+}
+
+// ---- small kernels --------------------------------------------------------
+struct FBCItem {
+  int set;
+  int dir_mask;
+  double spatial;
+};
+
+__global__ void k_fbc_apply(int64_t nf, int S, const int *nodes, const int *iptr,
+                            const FBCItem *items, BCTable T, double time, double *fext) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nf) return;
+  double fe[3] = {0., 0., 0.};
+  for (int k = iptr[t]; k < iptr[t + 1]; k++) {
+    const FBCItem it = items[k];
+    const double v = fload_time(T.t[it.set], it.spatial, time);
+    for (int d = 0; d < 3; d++)
+      if (it.dir_mask >> d & 1) fe[d] = fe[d] + v;
+  }
+  const int64_t i = nodes[t];
+  for (int d = 0; d < S && d < 3; d++) fext[S * i + d] = fe[d];
+}
+
+__global__ void k_bc_apply(int64_t nb, int S, int dim, const int *nodes, const int *bcref,
+                           const BCEntry *bce, const uint8_t *flags, BCTable T, double time,
+                           double *u64, float4 *u32, double *v) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nb) return;
+  const int64_t i = nodes[t];
+  const BCEntry e = bce[bcref[i]];
+  const uint8_t fl = flags[i];
+  double uo[3], vo[3];
+  if (u64) {
+    for (int d = 0; d < 3; d++) uo[d] = d < S ? u64[S * i + d] : 0.;
+  } else {
+    if (S == 2) {
+      const float4 a = u32[i];
+      uo[0] = (double)a.x + (double)a.z;
+      uo[1] = (double)a.y + (double)a.w;
+      uo[2] = 0.;
+    } else {
+      const float4 a = u32[2 * i], b = u32[2 * i + 1];
+      uo[0] = (double)a.x + (double)b.x;
+      uo[1] = (double)a.y + (double)b.y;
+      uo[2] = (double)a.z + (double)b.z;
+    }
+  }
+  for (int d = 0; d < 3; d++) vo[d] = d < S ? v[S * i + d] : 0.;
+  for (int d = 0; d < dim; d++)
+    if ((fl >> d & 1) && e.set[d] >= 0) {
+      double du, dv;
+      bc_value(T.t[e.set[d]], e.umax[d], time, du, dv);
+      uo[d] = du;
+      vo[d] = dv;
+    }
+  if (u64) {
+    for (int d = 0; d < S && d < 3; d++) u64[S * i + d] = uo[d];
+  } else {
+    float h[3], l[3];
+    for (int d = 0; d < 3; d++) {
+      h[d] = __double2float_rn(uo[d]);
+      l[d] = __double2float_rn(uo[d] - (double)h[d]);
+    }
+    if (S == 2)
+      u32[i] = make_float4(h[0], h[1], l[0], l[1]);
+    else {
+      u32[2 * i] = make_float4(h[0], h[1], h[2], 0.f);
+      u32[2 * i + 1] = make_float4(l[0], l[1], l[2], 0.f);
+    }
+  }
+  for (int d = 0; d < S && d < 3; d++) v[S * i + d] = vo[d];
+}
+
+// AoS original order (3 doubles per node) <-> internal layouts.
+__global__ void k_scatter_vec(int64_t n, int S, int dim, const int *perm, const double *src,
+                              double *dst) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double *p = src + 3 * (int64_t)perm[i];
+  for (int d = 0; d < S; d++) dst[S * i + d] = (d < dim && d < 3) ? p[d] : 0.;
+}
+__global__ void k_scatter_split(int64_t n, int S, int dim, const int *perm, const double *src,
+                                float4 *dst) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double *p = src + 3 * (int64_t)perm[i];
+  float h[3], l[3];
+  for (int d = 0; d < 3; d++) {
+    const double val = d < dim ? p[d] : 0.;
+    h[d] = __double2float_rn(val);
+    l[d] = __double2float_rn(val - (double)h[d]);
+  }
+  if (S == 2)
+    dst[i] = make_float4(h[0], h[1], l[0], l[1]);
+  else {
+    dst[2 * i] = make_float4(h[0], h[1], h[2], 0.f);
+    dst[2 * i + 1] = make_float4(l[0], l[1], l[2], 0.f);
+  }
+}
+__global__ void k_gather_vec(int64_t n, int S, const int *perm, const double *src, double *dst) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double *p = dst + 3 * (int64_t)perm[i];
+  for (int d = 0; d < 3; d++) p[d] = d < S ? src[S * i + d] : 0.;
+}
+__global__ void k_gather_split(int64_t n, int S, const int *perm, const float4 *src, double *dst) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double *p = dst + 3 * (int64_t)perm[i];
+  if (S == 2) {
+    const float4 a = src[i];
+    p[0] = (double)a.x + (double)a.z;
+    p[1] = (double)a.y + (double)a.w;
+    p[2] = 0.;
+  } else {
+    const float4 a = src[2 * i], b = src[2 * i + 1];
+    p[0] = (double)a.x + (double)b.x;
+    p[1] = (double)a.y + (double)b.y;
+    p[2] = (double)a.z + (double)b.z;
+  }
+}
+__global__ void k_gather_f32(int64_t n, int S, const int *perm, const float *src, double *dst) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double *p = dst + 3 * (int64_t)perm[i];
+  for (int d = 0; d < 3; d++) p[d] = d < S ? (double)src[S * i + d] : 0.;
+}
+__global__ void k_make_pos32(int64_t n, int S, const double *pos, float4 *pos32) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float h[3], l[3];
+  for (int d = 0; d < 3; d++) {
+    const double v = d < S ? pos[S * i + d] : 0.;
+    h[d] = __double2float_rn(v);
+    l[d] = __double2float_rn(v - (double)h[d]);
+  }
+  if (S == 2)
+    pos32[i] = make_float4(h[0], h[1], l[0], l[1]);
+  else {
+    pos32[2 * i] = make_float4(h[0], h[1], h[2], 0.f);
+    pos32[2 * i + 1] = make_float4(l[0], l[1], l[2], 0.f);
+  }
+}
+__global__ void k_count_bits(int64_t n, int nwords, int64_t npad, const uint32_t *bits,
+                             unsigned long long *out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int c = 0;
+  for (int w = 0; w < nwords; w++) c += __popc(bits[(int64_t)w * npad + i]);
+  if (c) atomicAdd(out, (unsigned long long)c);
+}
+
+static unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+}  // namespace nlm
+
+using namespace nlm;
+
+// ---- the handle ----------------------------------------------------------
+struct nlm_fd {
+  int dim = 2, S = 2;
+  int64_t n = 0, nnz = 0;
+  int precision = NLM_PREC_FP64, scheme = NLM_VELOCITY_VERLET, decomp = NLM_DECOMP_THREAD;
+  int material = NLM_MAT_RNP_BOND;
+  double dt = 0., time = 0.;
+  int64_t step = 0;
+  bool started = false;
+  int cur = 0;
+  StepParams P{};
+  BCTable T{};
+  cudaStream_t stream = nullptr;
+  std::vector<void *> allocs;
+  DevPtrs D{};
+  int64_t nslices = 0, sell_entries = 0;
+  // host copies
+  std::vector<int> perm;    // internal -> original
+  std::vector<int64_t> rowptr;  // internal CSR offsets (host copy)
+  // loads
+  int *bc_nodes = nullptr;
+  int64_t n_bc_nodes = 0;
+  int *fbc_nodes = nullptr, *fbc_iptr = nullptr;
+  FBCItem *fbc_items = nullptr;
+  int64_t n_fbc_nodes = 0;
+  BCTable FT{};
+  // staging
+  double *stage = nullptr;
+  float *dmg_phi = nullptr, *dmg_Z = nullptr;
+  unsigned long long *counter = nullptr;
+  // timing
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  double acc_ms = 0.;
+  int64_t launches = 0;
+  double bytes_per_launch = 0.;
+
+  template <class Tp>
+  cudaError_t alloc(Tp **p, size_t count) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, count * sizeof(Tp) + 16);
+    if (e == cudaSuccess) {
+      allocs.push_back(q);
+      *p = static_cast<Tp *>(q);
+    }
+    return e;
+  }
+  ~nlm_fd() {
+    if (stream) cudaStreamSynchronize(stream);
+    for (void *p : allocs) cudaFree(p);
+    for (auto e : ev_pool) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+bool finite_all(const double *a, int64_t n) {
+  for (int64_t i = 0; i < n; i++)
+    if (!std::isfinite(a[i])) return false;
+  return true;
+}
+
+// RNPBond constants (rnpBond.cpp:23-97, computeParameters :99-189) and the
+// influence function (influenceFn.h:85-402).
+int rnp_constants(const nlm_material &m, int dim, double delta, StepParams &P) {
+  P.infl_type = m.influence_type;
+  const int np = m.n_influence_params;
+  double M = 0.;
+  if (m.influence_type == 0) {
+    P.infl_a0 = np == 0 ? double(dim + 1) : m.influence_params[0];
+    M = P.infl_a0 / double(dim + 1);
+  } else if (m.influence_type == 1) {
+    if (np == 0) {
+      P.infl_a0 = dim == 1 ? 6. : (dim == 2 ? 12. : 20.);
+      P.infl_a1 = -P.infl_a0;
+    } else {
+      P.infl_a0 = m.influence_params[0];
+      P.infl_a1 = np < 2 ? -P.infl_a0 : m.influence_params[1];
+    }
+    M = (P.infl_a0 / double(dim + 1)) + (P.infl_a1 / double(dim + 2));
+  } else if (m.influence_type == 2) {
+    if (np == 0) {
+      P.infl_beta = 0.2;
+      const double b = P.infl_beta;
+      if (dim == 1)
+        P.infl_alpha = 2. / (b * (1. - std::exp(-1. / b)));
+      else if (dim == 2)
+        P.infl_alpha = (4.0 / b) * 1.0 /
+                       (std::sqrt(M_PI * b) * std::erf(1.0 / std::sqrt(b)) - 2.0 * std::exp(-1.0 / b));
+      else
+        P.infl_alpha = (2.0 / b) * 1.0 / (b - (b + 1.) * std::exp(-1.0 / b));
+    } else {
+      P.infl_alpha = m.influence_params[0];
+      P.infl_beta = m.influence_params[1];
+    }
+    const double a = P.infl_alpha, b = P.infl_beta;
+    const double sq1 = std::sqrt(b), sq2 = std::sqrt(M_PI);
+    if (dim == 1)
+      M = 0.5 * a * b * (1. - std::exp(-1. / b));
+    else if (dim == 2)
+      M = 0.5 * a * b * sq1 * (0.5 * sq2 * std::erf(1. / sq1) - (1. / sq1) * std::exp(-1. / b));
+    else
+      M = 0.5 * a * b * b * (1. - (1. + 1. / b) * std::exp(-1. / b));
+  } else {
+    return fail(NLM_ERR_INVALID, "unknown influence function type");
+  }
+  P.irrev = m.irreversible ? 1 : 0;
+  P.fsc = m.check_sc_factor;
+  if (dim == 2)
+    P.invF = std::pow(delta, 3) * M_PI;
+  else
+    P.invF = std::pow(delta, 4) * 4. * M_PI / 3.;
+  if (m.compute_from_classical) {
+    double E = m.E, K = m.K, Gc = m.Gc, KIc = m.KIc;
+    if (hLT(E, 0.) && hLT(K, 0.)) return fail(NLM_ERR_INVALID, "RNPBond needs E or K");
+    if (hLT(Gc, 0.) && hLT(KIc, 0.)) return fail(NLM_ERR_INVALID, "RNPBond needs Gc or KIc");
+    const double nu = m.plane_strain ? 0.25 : 1. / 3.;
+    if (E > 0.) K = E / (3. * (1. - 2. * nu));
+    if (K > 0. && E < 0.) E = K * (3. * (1. - 2. * nu));
+    if (Gc > 0.) KIc = std::sqrt(Gc * E);
+    if (KIc > 0. && Gc < 0.) Gc = KIc * KIc / E;
+    const double lambda = E * nu / ((1. + nu) * (1. - 2. * nu));
+    if (dim == 2) {
+      P.C = M_PI * Gc / (4. * M);
+      P.beta = 4. * lambda / (P.C * M);
+    } else {
+      P.C = 2. * Gc / (3. * M);
+      P.beta = 5. * lambda / (P.C * M);
+    }
+  } else {
+    P.C = m.bond_params[0];
+    P.beta = m.bond_params[1];
+  }
+  P.rbar = std::sqrt(0.5 / P.beta);
+  if (!(P.C > 0.) || !(P.beta > 0.)) return fail(NLM_ERR_INVALID, "RNPBond constants not positive");
+  return NLM_OK;
+}
+
+int launch_step(nlm_fd *h, const StepArgs &a) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (h->timing) {
+    while (h->ev_used + 2 > h->ev_pool.size()) {
+      cudaEvent_t e;
+      NLM_CUDA(cudaEventCreate(&e));
+      h->ev_pool.push_back(e);
+    }
+    e0 = h->ev_pool[h->ev_used++];
+    e1 = h->ev_pool[h->ev_used++];
+    NLM_CUDA(cudaEventRecord(e0, h->stream));
+  }
+  cudaError_t e;
+  const bool fp32 = h->precision == NLM_PREC_FP32C;
+  if (h->material == NLM_MAT_RNP_BOND)
+    e = fp32 ? launch_rnp_step_fp32(h->P, h->D, h->T, a, h->decomp, h->stream)
+             : launch_rnp_step_fp64(h->P, h->D, h->T, a, h->decomp, h->stream);
+  else
+    e = fp32 ? launch_es_step_fp32(h->P, h->D, h->T, a, h->decomp, h->stream)
+             : launch_es_step_fp64(h->P, h->D, h->T, a, h->decomp, h->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
+  if (h->timing) {
+    NLM_CUDA(cudaEventRecord(e1, h->stream));
+    h->launches++;
+  }
+  return NLM_OK;
+}
+
+int apply_fbc(nlm_fd *h, double t) {
+  if (h->n_fbc_nodes == 0) return NLM_OK;
+  k_fbc_apply<<<nblk(h->n_fbc_nodes, 128), 128, 0, h->stream>>>(
+      h->n_fbc_nodes, h->S, h->fbc_nodes, h->fbc_iptr, h->fbc_items, h->FT, t,
+      const_cast<double *>(h->D.fext));
+  NLM_CUDA(cudaGetLastError());
+  return NLM_OK;
+}
+
+int apply_bc(nlm_fd *h, double t) {
+  if (h->n_bc_nodes == 0) return NLM_OK;
+  const bool fp32 = h->precision == NLM_PREC_FP32C;
+  k_bc_apply<<<nblk(h->n_bc_nodes, 128), 128, 0, h->stream>>>(
+      h->n_bc_nodes, h->S, h->dim, h->bc_nodes, h->D.bcref, h->D.bce, h->D.flags, h->T, t,
+      fp32 ? nullptr : h->D.u64[h->cur], fp32 ? h->D.u32[h->cur] : nullptr,
+      h->D.v[h->scheme == NLM_CENTRAL_DIFFERENCE ? h->cur : 0]);
+  NLM_CUDA(cudaGetLastError());
+  return NLM_OK;
+}
+
+int do_run(nlm_fd *h, int64_t nsteps) {
+  if (!h->started) {
+    int rc = apply_bc(h, h->time);
+    if (rc) return rc;
+    if ((rc = apply_fbc(h, h->time))) return rc;
+    StepArgs a{h->cur, true, h->time, h->time + h->dt};
+    if ((rc = launch_step(h, a))) return rc;
+    h->started = true;
+  }
+  for (int64_t s = 0; s < nsteps; s++) {
+    const double tm = h->time + h->dt;
+    h->cur = 1 - h->cur;
+    int rc = apply_fbc(h, tm);
+    if (rc) return rc;
+    StepArgs a{h->cur, false, tm, tm + h->dt};
+    if ((rc = launch_step(h, a))) return rc;
+    h->time = tm;
+    h->step++;
+  }
+  return NLM_OK;
+}
+
+}  // namespace
+
+// ---- C ABI ---------------------------------------------------------------
+extern "C" {
+
+const char *nlm_last_error(void) { return g_err.c_str(); }
+int nlm_abi_version(void) { return NLM_ABI_VERSION; }
+
+int nlm_device_count(int *count) {
+  if (!count) return fail(NLM_ERR_INVALID, "null count");
+  int c = 0;
+  cudaError_t e = cudaGetDeviceCount(&c);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    c = 0;
+  }
+  *count = c;
+  return NLM_OK;
+}
+
+int nlm_neighbor_search(int dim, int64_t n, const double *x, double horizon, int64_t *rowptr,
+                        int32_t *cols) {
+  if (n < 0 || (n > 0 && !x) || !rowptr || dim < 1 || dim > 3 || !(horizon > 0.))
+    return fail(NLM_ERR_INVALID, "nlm_neighbor_search: bad arguments");
+  if (n > INT32_MAX - 1) return fail(NLM_ERR_INVALID, "too many nodes");
+  if (!finite_all(x, 3 * n)) return fail(NLM_ERR_NONFINITE, "non-finite coordinate");
+  cudaStream_t s;
+  NLM_CUDA(cudaStreamCreate(&s));
+  double *dx = nullptr;
+  NeighborBuild nb;
+  std::string why;
+  auto cleanup = [&]() {
+    cudaFree(dx); cudaFree(nb.perm); cudaFree(nb.pos); cudaFree(nb.rowptr); cudaFree(nb.cols);
+    cudaStreamDestroy(s);
+  };
+  cudaError_t e = cudaMalloc(&dx, sizeof(double) * 3 * (n + 1));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s);
+  const Grid g = make_grid(dim, n, x, horizon);
+  if (e == cudaSuccess) e = build_neighbors(nb, dim, n, dx, g, 4, s, why);
+  if (e != cudaSuccess) {
+    int rc = why.empty() ? cuda_fail(e, "neighbour search") : fail(NLM_ERR_INVALID, why);
+    cleanup();
+    return rc;
+  }
+  std::vector<int> perm(n);
+  std::vector<int64_t> rp(n + 1);
+  std::vector<int> cc(nb.nnz);
+  e = cudaMemcpy(perm.data(), nb.perm, sizeof(int) * n, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(rp.data(), nb.rowptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && nb.nnz) e = cudaMemcpy(cc.data(), nb.cols, sizeof(int) * nb.nnz, cudaMemcpyDeviceToHost);
+  cleanup();
+  if (e != cudaSuccess) return cuda_fail(e, "neighbour download");
+  std::vector<int64_t> inv(n);
+  for (int64_t i = 0; i < n; i++) inv[perm[i]] = i;
+  rowptr[0] = 0;
+  for (int64_t o = 0; o < n; o++) rowptr[o + 1] = rowptr[o] + (rp[inv[o] + 1] - rp[inv[o]]);
+  if (cols)
+    for (int64_t o = 0; o < n; o++) {
+      const int64_t s0 = rp[inv[o]], len = rp[inv[o] + 1] - s0;
+      for (int64_t k = 0; k < len; k++) cols[rowptr[o] + k] = perm[cc[s0 + k]];
+    }
+  return NLM_OK;
+}
+
+int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
+  if (!d || !out) return fail(NLM_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (d->dim != 2 && d->dim != 3)
+    return fail(NLM_ERR_UNSUPPORTED, "explicit model supports dim 2 and 3");
+  if (d->n_nodes <= 0 || !d->x || !d->volume) return fail(NLM_ERR_INVALID, "empty mesh");
+  if (d->n_nodes > INT32_MAX - 64) return fail(NLM_ERR_INVALID, "too many nodes for one handle");
+  if (!(d->horizon > 0.) || !(d->mesh_size > 0.) || !(d->dt > 0.))
+    return fail(NLM_ERR_INVALID, "horizon, mesh size and dt must be positive");
+  if (!(d->material.density > 0.)) return fail(NLM_ERR_INVALID, "density must be positive");
+  if (d->n_ubc < 0 || d->n_ubc > kMaxBCSets || d->n_fbc < 0 || d->n_fbc > kMaxBCSets)
+    return fail(NLM_ERR_INVALID, "too many BC sets");
+  if ((d->n_ubc && !d->ubc) || (d->n_fbc && !d->fbc) || (d->n_cracks && !d->cracks))
+    return fail(NLM_ERR_INVALID, "null BC / crack array");
+  if (d->precision != NLM_PREC_FP64 && d->precision != NLM_PREC_FP32C)
+    return fail(NLM_ERR_INVALID, "unknown precision");
+  if (d->scheme != NLM_VELOCITY_VERLET && d->scheme != NLM_CENTRAL_DIFFERENCE)
+    return fail(NLM_ERR_INVALID, "unknown scheme");
+  if (d->material.kind != NLM_MAT_RNP_BOND && d->material.kind != NLM_MAT_ELASTIC_STATE)
+    return fail(NLM_ERR_INVALID, "unknown material");
+  const int64_t n = d->n_nodes;
+  if (!finite_all(d->x, 3 * n) || !finite_all(d->volume, n))
+    return fail(NLM_ERR_NONFINITE, "non-finite coordinate or volume");
+  if ((d->u0 && !finite_all(d->u0, 3 * n)) || (d->v0 && !finite_all(d->v0, 3 * n)))
+    return fail(NLM_ERR_NONFINITE, "non-finite initial state");
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) {
+    cudaGetLastError();
+    return fail(NLM_ERR_CUDA, "no CUDA device");
+  }
+
+  nlm_fd *h = new nlm_fd();
+  auto bail = [&](int rc) {
+    delete h;
+    return rc;
+  };
+  h->dim = d->dim;
+  h->S = d->dim == 2 ? 2 : 4;
+  h->n = n;
+  h->precision = d->precision;
+  h->scheme = d->scheme;
+  h->material = d->material.kind;
+  h->dt = d->dt;
+  StepParams &P = h->P;
+  P.n = n;
+  P.dim = d->dim;
+  P.delta = d->horizon;
+  P.h = d->mesh_size;
+  P.check_up = d->horizon + 0.5 * d->mesh_size;
+  P.check_low = d->horizon - 0.5 * d->mesh_size;
+  P.dt = d->dt;
+  P.rho = d->material.density;
+  P.scheme = d->scheme;
+  int rc;
+  if (h->material == NLM_MAT_RNP_BOND) {
+    if ((rc = rnp_constants(d->material, d->dim, d->horizon, P))) return bail(rc);
+  } else {
+    const nlm_material &m = d->material;
+    if (!(m.K > 0.) || !(m.G > 0.)) return bail(fail(NLM_ERR_INVALID, "ElasticState needs K and G"));
+    P.es_K = m.K;
+    P.es_mu = m.G;
+    P.es_nu = (3 * m.K - 2 * m.G) / (2 * (3 * m.K + m.G));
+    P.es_E = m.E;
+    P.es_plane_strain = m.plane_strain ? 1 : 0;
+    P.es_factor2D = (!m.plane_strain && d->dim == 2) ? (2. * P.es_nu - 1.) / (P.es_nu - 1.) : 1.;
+    P.es_sc = m.es_sc;
+    P.es_ref_compat = m.es_ref_compat ? 1 : 0;
+    P.irrev = 1;
+  }
+  h->decomp = d->decomposition == NLM_DECOMP_AUTO ? NLM_DECOMP_THREAD : d->decomposition;
+  if (h->decomp != NLM_DECOMP_THREAD && h->decomp != NLM_DECOMP_WARP)
+    return bail(fail(NLM_ERR_INVALID, "unknown decomposition"));
+
+  cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
+  cudaStream_t s = h->stream;
+  const int S = h->S;
+#define TRY(call)                                     \
+  do {                                                \
+    cudaError_t _e = (call);                          \
+    if (_e != cudaSuccess) return bail(cuda_fail(_e, #call)); \
+  } while (0)
+
+  // ---- neighbours (Morton order) ----
+  double *dx = nullptr;
+  TRY(h->alloc(&dx, 3 * n));
+  TRY(cudaMemcpyAsync(dx, d->x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  const Grid g = make_grid(d->dim, n, d->x, d->horizon);
+  NeighborBuild nb;
+  std::string why;
+  e = build_neighbors(nb, d->dim, n, dx, g, S, s, why);
+  for (void *p : {(void *)nb.perm, (void *)nb.pos, (void *)nb.rowptr, (void *)nb.cols})
+    if (p) h->allocs.push_back(p);
+  if (e != cudaSuccess)
+    return bail(why.empty() ? cuda_fail(e, "neighbour build") : fail(NLM_ERR_INVALID, why));
+  h->nnz = nb.nnz;
+  if (h->nnz > INT32_MAX) return bail(fail(NLM_ERR_INVALID, "too many bonds for one handle"));
+  SellStore st;
+  e = build_sell(n, nb.rowptr, nb.cols, st, s);
+  for (void *p : {(void *)st.ptr, (void *)st.width, (void *)st.cols})
+    if (p) h->allocs.push_back(p);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "bond store build"));
+  h->nslices = st.nslices;
+  h->sell_entries = st.entries;
+  P.nwords = std::max(1, (st.maxw + 31) / 32);
+  P.npad = ((n + 31) / 32) * 32;
+  h->perm.resize(n);
+  h->rowptr.resize(n + 1);
+  TRY(cudaMemcpyAsync(h->perm.data(), nb.perm, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  TRY(cudaMemcpyAsync(h->rowptr.data(), nb.rowptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, s));
+  TRY(cudaStreamSynchronize(s));
+
+  DevPtrs &D = h->D;
+  D.pos64 = nb.pos;
+  D.perm_dev = nb.perm;
+  D.rowptr = nb.rowptr;
+  D.cols = nb.cols;
+  D.sell_ptr = st.ptr;
+  D.sell_w = st.width;
+  D.sell_cols = st.cols;
+  uint32_t *bits = nullptr;
+  TRY(h->alloc(&bits, (size_t)P.nwords * P.npad));
+  TRY(cudaMemsetAsync(bits, 0, sizeof(uint32_t) * P.nwords * P.npad, s));
+  D.bits = bits;
+  for (int c = 0; c < d->n_cracks; c++) {
+    if (d->cracks[c].kind == NLM_CRACK_EDGE && d->dim != 2)
+      return bail(fail(NLM_ERR_INVALID, "edge pre-cracks are 2-D only (input.cpp:298-307)"));
+    TRY(apply_precrack(n, S, nb.pos, nb.rowptr, nb.cols, d->cracks[c], P.npad, bits, s));
+  }
+
+  // ---- node flags, loads (host, original order then permuted) ----
+  std::vector<uint8_t> fix(n, 0), interior(n, 1);
+  std::vector<int> wset(3 * n, -1);
+  std::vector<double> wumax(3 * n, 0.);
+  for (int sidx = 0; sidx < d->n_ubc; sidx++) {
+    const nlm_bc_set &bc = d->ubc[sidx];
+    if (bc.time_fn < 0 || bc.time_fn > NLM_TFN_LINEAR_SLOW_FAST)
+      return bail(fail(NLM_ERR_INVALID, "unknown BC time function"));
+    for (int64_t i = 0; i < n; i++) {
+      if (!in_region(bc, d->x + 3 * i, d->dim)) continue;
+      const double um = uload_umax(bc, d->x + 3 * i);
+      for (int dd = 0; dd < 3; dd++)
+        if (bc.dir_mask >> dd & 1) {
+          fix[i] |= uint8_t(1 << dd);
+          wset[3 * i + dd] = sidx;
+          wumax[3 * i + dd] = um;
+        }
+    }
+    h->T.t[sidx].fn = bc.time_fn;
+    for (int k = 0; k < 4; k++) h->T.t[sidx].p[k] = bc.time_params[k];
+  }
+  h->T.nsets = d->n_ubc;
+  if (d->no_fail == NLM_NOFAIL_COMPUTE) {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int64_t i = 0; i < n; i++)
+      for (int dd = 0; dd < 3; dd++) {
+        if (hLT(d->x[3 * i + dd], lo[dd])) lo[dd] = d->x[3 * i + dd];
+        if (hLT(hi[dd], d->x[3 * i + dd])) hi[dd] = d->x[3 * i + dd];
+      }
+    const double tol = d->no_fail_tol;
+    for (int64_t i = 0; i < n; i++) {
+      const double *p = d->x + 3 * i;
+      interior[i] = !(hLT(p[0], lo[0] + tol) || hLT(p[1], lo[1] + tol) ||
+                      hGT(p[0], hi[0] - tol) || hGT(p[1], hi[1] - tol));
+    }
+  }
+  // force BC items per node, in set order
+  std::vector<std::vector<FBCItem>> fitems(n);
+  for (int sidx = 0; sidx < d->n_fbc; sidx++) {
+    const nlm_bc_set &bc = d->fbc[sidx];
+    for (int64_t i = 0; i < n; i++)
+      if (in_region(bc, d->x + 3 * i, d->dim))
+        fitems[i].push_back(FBCItem{sidx, bc.dir_mask & 7, fload_spatial(bc, d->x + 3 * i)});
+    h->FT.t[sidx].fn = bc.time_fn;
+    for (int k = 0; k < 4; k++) h->FT.t[sidx].p[k] = bc.time_params[k];
+  }
+  h->FT.nsets = d->n_fbc;
+
+  std::vector<uint8_t> flags(n);
+  std::vector<int> bcref(n, -1), bcn, fnodes, fptr(1, 0);
+  std::vector<BCEntry> bce;
+  std::vector<FBCItem> fits;
+  std::vector<double> volp(n);
+  bool any_nofail = false;
+  for (int64_t i = 0; i < n; i++) {
+    const int o = h->perm[i];
+    uint8_t f = fix[o];
+    if (!interior[o]) {
+      f |= FLAG_NOFAIL;
+      any_nofail = true;
+    }
+    if (!fitems[o].empty()) {
+      f |= FLAG_FBC;
+      fnodes.push_back((int)i);
+      for (auto &it : fitems[o]) fits.push_back(it);
+      fptr.push_back((int)fits.size());
+    }
+    if (fix[o]) {
+      BCEntry be;
+      for (int dd = 0; dd < 3; dd++) {
+        be.set[dd] = wset[3 * o + dd];
+        be.umax[dd] = wumax[3 * o + dd];
+      }
+      bcref[i] = (int)bce.size();
+      bce.push_back(be);
+      bcn.push_back((int)i);
+    }
+    flags[i] = f;
+    volp[i] = d->volume[o];
+  }
+  P.nofail = any_nofail ? 1 : 0;
+  uint8_t *dflags;
+  int *dbcref;
+  BCEntry *dbce;
+  TRY(h->alloc(&dflags, n));
+  TRY(h->alloc(&dbcref, n));
+  TRY(h->alloc(&dbce, bce.size() + 1));
+  TRY(cudaMemcpyAsync(dflags, flags.data(), n, cudaMemcpyHostToDevice, s));
+  TRY(cudaMemcpyAsync(dbcref, bcref.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  if (!bce.empty())
+    TRY(cudaMemcpyAsync(dbce, bce.data(), sizeof(BCEntry) * bce.size(), cudaMemcpyHostToDevice, s));
+  D.flags = dflags;
+  D.bcref = dbcref;
+  D.bce = dbce;
+  h->n_bc_nodes = (int64_t)bcn.size();
+  TRY(h->alloc(&h->bc_nodes, bcn.size() + 1));
+  if (!bcn.empty())
+    TRY(cudaMemcpyAsync(h->bc_nodes, bcn.data(), sizeof(int) * bcn.size(), cudaMemcpyHostToDevice, s));
+  h->n_fbc_nodes = (int64_t)fnodes.size();
+  double *fext;
+  TRY(h->alloc(&fext, (size_t)S * n));
+  TRY(cudaMemsetAsync(fext, 0, sizeof(double) * S * n, s));
+  D.fext = fext;
+  if (!fnodes.empty()) {
+    TRY(h->alloc(&h->fbc_nodes, fnodes.size()));
+    TRY(h->alloc(&h->fbc_iptr, fptr.size()));
+    TRY(h->alloc(&h->fbc_items, fits.size()));
+    TRY(cudaMemcpyAsync(h->fbc_nodes, fnodes.data(), sizeof(int) * fnodes.size(), cudaMemcpyHostToDevice, s));
+    TRY(cudaMemcpyAsync(h->fbc_iptr, fptr.data(), sizeof(int) * fptr.size(), cudaMemcpyHostToDevice, s));
+    TRY(cudaMemcpyAsync(h->fbc_items, fits.data(), sizeof(FBCItem) * fits.size(), cudaMemcpyHostToDevice, s));
+  }
+  double *vol64;
+  TRY(h->alloc(&vol64, n));
+  TRY(cudaMemcpyAsync(vol64, volp.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  D.vol64 = vol64;
+  if (h->precision == NLM_PREC_FP32C) {
+    std::vector<float> v32(n);
+    for (int64_t i = 0; i < n; i++) v32[i] = (float)volp[i];
+    float *vol32;
+    TRY(h->alloc(&vol32, n));
+    TRY(cudaMemcpyAsync(vol32, v32.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    TRY(cudaStreamSynchronize(s));
+    D.vol32 = vol32;
+    float4 *pos32;
+    TRY(h->alloc(&pos32, (size_t)(S / 2) * n));
+    k_make_pos32<<<nblk(n, 256), 256, 0, s>>>(n, S, nb.pos, pos32);
+    TRY(cudaGetLastError());
+    D.pos32 = pos32;
+  }
+
+  // ---- state ----
+  TRY(h->alloc(&h->stage, 3 * n));
+  if (h->precision == NLM_PREC_FP64) {
+    TRY(h->alloc(&D.u64[0], (size_t)S * n));
+    TRY(h->alloc(&D.u64[1], (size_t)S * n));
+    TRY(h->alloc(&D.f64, (size_t)S * n));
+    TRY(cudaMemsetAsync(D.f64, 0, sizeof(double) * S * n, s));
+  } else {
+    TRY(h->alloc(&D.u32[0], (size_t)(S / 2) * n));
+    TRY(h->alloc(&D.u32[1], (size_t)(S / 2) * n));
+    TRY(h->alloc(&D.f32, (size_t)S * n));
+    TRY(cudaMemsetAsync(D.f32, 0, sizeof(float) * S * n, s));
+  }
+  TRY(h->alloc(&D.v[0], (size_t)S * n));
+  TRY(h->alloc(&D.v[1], (size_t)S * n));
+  TRY(h->alloc(&D.err, 1));
+  TRY(cudaMemsetAsync(D.err, 0, sizeof(int), s));
+  TRY(h->alloc(&h->counter, 1));
+  TRY(cudaStreamSynchronize(s));
+  h->bytes_per_launch = 0.;
+  *out = h;
+  rc = nlm_fd_set_state(h, d->u0, d->v0);
+  if (rc == NLM_OK && (!d->u0 || !d->v0)) {
+    // a NULL initial array means zero
+    if (!d->u0) {
+      if (h->precision == NLM_PREC_FP64)
+        TRY(cudaMemsetAsync(D.u64[0], 0, sizeof(double) * S * n, s));
+      else
+        TRY(cudaMemsetAsync(D.u32[0], 0, sizeof(float4) * (S / 2) * n, s));
+    }
+    if (!d->v0) TRY(cudaMemsetAsync(D.v[0], 0, sizeof(double) * S * n, s));
+    TRY(cudaStreamSynchronize(s));
+  }
+  if (rc != NLM_OK) {
+    *out = nullptr;
+    return bail(rc);
+  }
+  // algorithmic bytes of one step launch (compulsory traffic model)
+  {
+    const double per_bond = 4.0 + 0.25;  // int32 column + bond bit read/write
+    double per_node;
+    if (h->precision == NLM_PREC_FP64)
+      per_node = 8.0 * S /*x*/ + 8 /*V*/ + 1 /*flags*/ + 8.0 * S * 2 /*u r,w*/ +
+                 8.0 * S * 2 /*v r,w*/ + 8.0 * S * 2 /*f r,w*/;
+    else
+      per_node = 8.0 * S /*x split*/ + 4 /*V*/ + 1 + 8.0 * S * 2 /*u split r,w*/ +
+                 8.0 * S * 2 /*v r,w*/ + 4.0 * S * 2 /*f r,w*/;
+    if (h->material == NLM_MAT_ELASTIC_STATE) per_node += 8.0 * 2;  // theta, m
+    h->bytes_per_launch = per_bond * (double)h->nnz + per_node * (double)n;
+  }
+#undef TRY
+  return NLM_OK;
+}
+
+int nlm_fd_destroy(nlm_fd *h) {
+  delete h;
+  return NLM_OK;
+}
+
+int nlm_fd_num_bonds(const nlm_fd *h, int64_t *nnz) {
+  if (!h || !nnz) return fail(NLM_ERR_INVALID, "null argument");
+  *nnz = h->nnz;
+  return NLM_OK;
+}
+
+int nlm_fd_get_neighbors(nlm_fd *h, int64_t *rowptr, int32_t *cols) {
+  if (!h || !rowptr) return fail(NLM_ERR_INVALID, "null argument");
+  const int64_t n = h->n;
+  std::vector<int64_t> inv(n);
+  for (int64_t i = 0; i < n; i++) inv[h->perm[i]] = i;
+  rowptr[0] = 0;
+  for (int64_t o = 0; o < n; o++) rowptr[o + 1] = rowptr[o] + (h->rowptr[inv[o] + 1] - h->rowptr[inv[o]]);
+  if (cols) {
+    std::vector<int> cc(h->nnz);
+    if (h->nnz)
+      NLM_CUDA(cudaMemcpyAsync(cc.data(), h->D.cols, sizeof(int) * h->nnz, cudaMemcpyDeviceToHost, h->stream));
+    NLM_CUDA(cudaStreamSynchronize(h->stream));
+    for (int64_t o = 0; o < n; o++) {
+      const int64_t s0 = h->rowptr[inv[o]], len = h->rowptr[inv[o] + 1] - s0;
+      for (int64_t k = 0; k < len; k++) cols[rowptr[o] + k] = h->perm[cc[s0 + k]];
+    }
+  }
+  return NLM_OK;
+}
+
+int nlm_fd_run(nlm_fd *h, int64_t nsteps) {
+  if (!h || nsteps < 0) return fail(NLM_ERR_INVALID, "bad arguments");
+  return do_run(h, nsteps);
+}
+
+int nlm_fd_sync(nlm_fd *h) {
+  if (!h) return fail(NLM_ERR_INVALID, "null handle");
+  NLM_CUDA(cudaStreamSynchronize(h->stream));
+  return NLM_OK;
+}
+
+int nlm_fd_get_state(nlm_fd *h, double *u, double *v, double *f) {
+  if (!h) return fail(NLM_ERR_INVALID, "null handle");
+  const int64_t n = h->n;
+  cudaStream_t s = h->stream;
+  const int *P = h->D.perm_dev;
+  const unsigned g = nblk(n, 256);
+  const bool fp32 = h->precision == NLM_PREC_FP32C;
+  if (u) {
+    if (fp32)
+      k_gather_split<<<g, 256, 0, s>>>(n, h->S, P, h->D.u32[h->cur], h->stage);
+    else
+      k_gather_vec<<<g, 256, 0, s>>>(n, h->S, P, h->D.u64[h->cur], h->stage);
+    NLM_CUDA(cudaGetLastError());
+    NLM_CUDA(cudaMemcpyAsync(u, h->stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+    NLM_CUDA(cudaStreamSynchronize(s));
+  }
+  if (v) {
+    const double *src = h->D.v[h->scheme == NLM_CENTRAL_DIFFERENCE ? h->cur : 0];
+    k_gather_vec<<<g, 256, 0, s>>>(n, h->S, P, src, h->stage);
+    NLM_CUDA(cudaGetLastError());
+    NLM_CUDA(cudaMemcpyAsync(v, h->stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+    NLM_CUDA(cudaStreamSynchronize(s));
+  }
+  if (f) {
+    if (fp32)
+      k_gather_f32<<<g, 256, 0, s>>>(n, h->S, P, h->D.f32, h->stage);
+    else
+      k_gather_vec<<<g, 256, 0, s>>>(n, h->S, P, h->D.f64, h->stage);
+    NLM_CUDA(cudaGetLastError());
+    NLM_CUDA(cudaMemcpyAsync(f, h->stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+    NLM_CUDA(cudaStreamSynchronize(s));
+  }
+  return NLM_OK;
+}
+
+int nlm_fd_set_state(nlm_fd *h, const double *u, const double *v) {
+  if (!h) return fail(NLM_ERR_INVALID, "null handle");
+  const int64_t n = h->n;
+  if ((u && !finite_all(u, 3 * n)) || (v && !finite_all(v, 3 * n)))
+    return fail(NLM_ERR_NONFINITE, "non-finite state");
+  cudaStream_t s = h->stream;
+  const int *P = h->D.perm_dev;
+  const unsigned g = nblk(n, 256);
+  if (u) {
+    NLM_CUDA(cudaMemcpyAsync(h->stage, u, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+    if (h->precision == NLM_PREC_FP32C)
+      k_scatter_split<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.u32[h->cur]);
+    else
+      k_scatter_vec<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.u64[h->cur]);
+    NLM_CUDA(cudaGetLastError());
+  }
+  if (v) {
+    NLM_CUDA(cudaMemcpyAsync(h->stage, v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+    k_scatter_vec<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage,
+                                    h->D.v[h->scheme == NLM_CENTRAL_DIFFERENCE ? h->cur : 0]);
+    NLM_CUDA(cudaGetLastError());
+  }
+  NLM_CUDA(cudaStreamSynchronize(s));
+  if (h->started && (u || v)) {
+    // a new state restarts the force history: redo the step-0 evaluation
+    h->started = false;
+  }
+  return NLM_OK;
+}
+
+int nlm_fd_get_time(const nlm_fd *h, double *time, int64_t *step) {
+  if (!h) return fail(NLM_ERR_INVALID, "null handle");
+  if (time) *time = h->time;
+  if (step) *step = h->step;
+  return NLM_OK;
+}
+
+int nlm_fd_get_bond_state(nlm_fd *h, uint8_t *broken) {
+  if (!h || !broken) return fail(NLM_ERR_INVALID, "null argument");
+  const int64_t n = h->n;
+  std::vector<uint32_t> bits((size_t)h->P.nwords * h->P.npad);
+  NLM_CUDA(cudaMemcpyAsync(bits.data(), h->D.bits, sizeof(uint32_t) * bits.size(), cudaMemcpyDeviceToHost, h->stream));
+  NLM_CUDA(cudaStreamSynchronize(h->stream));
+  std::vector<int64_t> inv(n);
+  for (int64_t i = 0; i < n; i++) inv[h->perm[i]] = i;
+  int64_t o_off = 0;
+  for (int64_t o = 0; o < n; o++) {
+    const int64_t i = inv[o];
+    const int64_t len = h->rowptr[i + 1] - h->rowptr[i];
+    for (int64_t k = 0; k < len; k++)
+      broken[o_off + k] = (bits[(size_t)(k >> 5) * h->P.npad + i] >> (k & 31)) & 1u;
+    o_off += len;
+  }
+  return NLM_OK;
+}
+
+int nlm_fd_count_broken(nlm_fd *h, int64_t *count) {
+  if (!h || !count) return fail(NLM_ERR_INVALID, "null argument");
+  NLM_CUDA(cudaMemsetAsync(h->counter, 0, sizeof(unsigned long long), h->stream));
+  k_count_bits<<<nblk(h->n, 256), 256, 0, h->stream>>>(h->n, h->P.nwords, h->P.npad, h->D.bits, h->counter);
+  NLM_CUDA(cudaGetLastError());
+  unsigned long long c = 0;
+  NLM_CUDA(cudaMemcpyAsync(&c, h->counter, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+  NLM_CUDA(cudaStreamSynchronize(h->stream));
+  *count = (int64_t)c;
+  return NLM_OK;
+}
+
+int nlm_fd_damage(nlm_fd *h, float *phi, float *Z) {
+  if (!h) return fail(NLM_ERR_INVALID, "null handle");
+  const int64_t n = h->n;
+  cudaStream_t s = h->stream;
+  if (!h->dmg_phi) {
+    if (h->alloc(&h->dmg_phi, n) != cudaSuccess || h->alloc(&h->dmg_Z, n) != cudaSuccess)
+      return fail(NLM_ERR_OOM, "damage buffers");
+  }
+  cudaError_t e = launch_damage(h->P, h->D, h->cur, h->precision == NLM_PREC_FP32C,
+                                h->material == NLM_MAT_ELASTIC_STATE, h->dmg_phi, h->dmg_Z, s);
+  if (e != cudaSuccess) return cuda_fail(e, "damage kernel");
+  std::vector<float> a(n), b(n);
+  NLM_CUDA(cudaMemcpyAsync(a.data(), h->dmg_phi, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+  NLM_CUDA(cudaMemcpyAsync(b.data(), h->dmg_Z, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+  NLM_CUDA(cudaStreamSynchronize(s));
+  for (int64_t i = 0; i < n; i++) {
+    if (phi) phi[h->perm[i]] = a[i];
+    if (Z) Z[h->perm[i]] = b[i];
+  }
+  return NLM_OK;
+}
+
+int nlm_fd_decomposition(const nlm_fd *h, int *decomp) {
+  if (!h || !decomp) return fail(NLM_ERR_INVALID, "null argument");
+  *decomp = h->decomp;
+  return NLM_OK;
+}
+
+int nlm_fd_set_timing(nlm_fd *h, int enable) {
+  if (!h) return fail(NLM_ERR_INVALID, "null handle");
+  h->timing = enable != 0;
+  return NLM_OK;
+}
+
+int nlm_fd_kernel_stats(nlm_fd *h, int reset, double *avg_ms, int64_t *launches,
+                        double *bytes_per_launch) {
+  if (!h) return fail(NLM_ERR_INVALID, "null handle");
+  NLM_CUDA(cudaStreamSynchronize(h->stream));
+  double acc = 0.;
+  for (size_t k = 0; k + 1 < h->ev_used; k += 2) {
+    float ms = 0.f;
+    NLM_CUDA(cudaEventElapsedTime(&ms, h->ev_pool[k], h->ev_pool[k + 1]));
+    acc += ms;
+  }
+  const int64_t L = h->launches;
+  if (avg_ms) *avg_ms = L ? acc / (double)L : 0.;
+  if (launches) *launches = L;
+  if (bytes_per_launch) *bytes_per_launch = h->bytes_per_launch;
+  if (reset) {
+    h->ev_used = 0;
+    h->launches = 0;
+  }
+  return NLM_OK;
+}
+
+int nlm_fd_step_host(nlm_fd *h, double *u, double *v, double *f, int64_t nsteps) {
+  if (!h || !u || !v) return fail(NLM_ERR_INVALID, "null argument");
+  int rc = nlm_fd_set_state(h, u, v);
+  if (rc) return rc;
+  if ((rc = do_run(h, nsteps))) return rc;
+  return nlm_fd_get_state(h, u, v, f);
+}
+
+}  // extern "C"

@@ -1,0 +1,63 @@
+// fd_internal.h -- device pointer bundle and launcher prototypes shared by
+// the host code (fd_host.cu) and the kernel translation units.
+#pragma once
+
+#include "common.cuh"
+
+namespace nlm {
+
+// All node arrays are in the handle's internal (Morton) order.
+struct DevPtrs {
+  // geometry
+  const double *pos64;  // FP64: S doubles per node (S = 2 in 2-D, 4 in 3-D)
+  const float4 *pos32;  // FP32C: 2-D one float4 (xh, yh, xl, yl) per node;
+                        //        3-D two float4 (xh, yh, zh, 0), (xl, yl, zl, 0)
+  const double *vol64;
+  const float *vol32;
+  const uint8_t *flags;
+  const int *bcref;     // node -> BCEntry index (-1 none)
+  const BCEntry *bce;
+  const double *fext;   // S doubles per node, valid where FLAG_FBC is set
+  // topology
+  const int64_t *sell_ptr;  // per 32-node slice: first entry
+  const int *sell_w;        // per slice: width (longest row)
+  const int *sell_cols;     // slice-major, column-major inside a slice; -1 pads
+  const int64_t *rowptr;    // CSR (n+1)
+  const int *cols;          // CSR entries, rows ascending in original id
+  uint32_t *bits;           // word-major bond bits: bits[w * npad + i]
+  // state (ping-pong where a step reads the old and writes the new value)
+  double *u64[2];  // FP64 displacement, S per node
+  float4 *u32[2];  // FP32C displacement split, same shape as pos32
+  double *v[2];    // velocity S per node (Verlet uses v[0]; CD ping-pongs)
+  double *f64;     // FP64 force density, S per node
+  float *f32;      // FP32C force density, S per node
+  // ElasticState
+  const double *mw64;     // weighted volume m_i
+  const float *mw32;
+  double *theta64;        // dilatation
+  float *theta32;
+  int *err;               // device error flag
+  const int *perm_dev;    // internal -> original node id
+};
+
+// Which buffers a launch reads/writes.
+struct StepArgs {
+  int cur;        // index of the ping buffer holding u^m (and v^m for CD)
+  bool first;     // step-0 force evaluation (no velocity completion)
+  double t_now;   // t_m
+  double t_next;  // t_{m+1}
+};
+
+// Launchers (return cudaError_t of the launch).
+cudaError_t launch_rnp_step_fp64(const StepParams &P, const DevPtrs &D, const BCTable &T,
+                                 const StepArgs &a, int decomp, cudaStream_t s);
+cudaError_t launch_rnp_step_fp32(const StepParams &P, const DevPtrs &D, const BCTable &T,
+                                 const StepArgs &a, int decomp, cudaStream_t s);
+cudaError_t launch_es_step_fp64(const StepParams &P, const DevPtrs &D, const BCTable &T,
+                                const StepArgs &a, int decomp, cudaStream_t s);
+cudaError_t launch_es_step_fp32(const StepParams &P, const DevPtrs &D, const BCTable &T,
+                                const StepArgs &a, int decomp, cudaStream_t s);
+cudaError_t launch_damage(const StepParams &P, const DevPtrs &D, int cur, bool fp32,
+                          bool es, float *phi, float *Z, cudaStream_t s);
+
+}  // namespace nlm

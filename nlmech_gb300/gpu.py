@@ -1,0 +1,164 @@
+"""ctypes binding of libnlmgpu.so, shaped like the reference's FDModel.
+
+The reference constructs ``model::FDModel<RNPBond>(deck)`` and the constructor
+runs the whole simulation (src/model/fd/fDModel.cpp:47-67).  Here the same
+steps are split so that a caller can drive and inspect them:
+
+    m = FDModel(problem)       # initHObjects + init (neighbours, cracks, loads)
+    m.run(nsteps)              # integrate(): nsteps Verlet / CD steps
+    u, v, f = m.state()        # DataManager displacement / velocity / force
+
+There is no CPU fallback: if libnlmgpu.so is missing or no GPU is present the
+calls raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libnlmgpu.so")
+
+_lib = None
+
+
+class NLMError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("libnlmgpu error %d: %s" % (code, msg))
+        self.code = code
+
+
+def load(path=None):
+    """Load libnlmgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError("libnlmgpu.so not built at %s (run nlmech_gb300/build.py)" % p)
+    L = C.CDLL(p)
+    L.nlm_last_error.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise NLMError(rc, load().nlm_last_error().decode())
+
+
+def device_count():
+    c = C.c_int()
+    _check(load().nlm_device_count(C.byref(c)))
+    return c.value
+
+
+def neighbor_search(x, horizon, dim=2):
+    """GPU cell-list neighbour lists in original ids (rowptr int64, cols int32)."""
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+    n = x.shape[0]
+    rowptr = np.zeros(n + 1, dtype=np.int64)
+    L = load()
+    _check(L.nlm_neighbor_search(C.c_int(dim), C.c_int64(n), abi.dptr(x), C.c_double(horizon),
+                                 abi.ptr(rowptr, C.c_int64), C.POINTER(C.c_int32)()))
+    cols = np.zeros(int(rowptr[-1]), dtype=np.int32)
+    _check(L.nlm_neighbor_search(C.c_int(dim), C.c_int64(n), abi.dptr(x), C.c_double(horizon),
+                                 abi.ptr(rowptr, C.c_int64), abi.ptr(cols, C.c_int32)))
+    return rowptr, cols
+
+
+class FDModel:
+    """model::FDModel<T> on the GPU (T chosen by problem.material.kind)."""
+
+    def __init__(self, problem, precision=None, decomposition=None, scheme=None):
+        self.problem = problem
+        d, self._keep = problem.desc(precision=precision, decomposition=decomposition,
+                                     scheme=scheme)
+        self.precision = d.precision
+        h = C.c_void_p()
+        _check(load().nlm_fd_create(C.byref(d), C.byref(h)))
+        self.h = h
+        self.n = problem.n
+
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.nlm_fd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def nnz(self):
+        v = C.c_int64()
+        _check(load().nlm_fd_num_bonds(self.h, C.byref(v)))
+        return v.value
+
+    def neighbors(self):
+        rowptr = np.zeros(self.n + 1, dtype=np.int64)
+        cols = np.zeros(self.nnz(), dtype=np.int32)
+        _check(load().nlm_fd_get_neighbors(self.h, abi.ptr(rowptr, C.c_int64),
+                                           abi.ptr(cols, C.c_int32)))
+        return rowptr, cols
+
+    def run(self, nsteps):
+        _check(load().nlm_fd_run(self.h, C.c_int64(int(nsteps))))
+
+    def sync(self):
+        _check(load().nlm_fd_sync(self.h))
+
+    def state(self):
+        u = np.zeros((self.n, 3))
+        v = np.zeros((self.n, 3))
+        f = np.zeros((self.n, 3))
+        _check(load().nlm_fd_get_state(self.h, abi.dptr(u), abi.dptr(v), abi.dptr(f)))
+        return u, v, f
+
+    def set_state(self, u=None, v=None):
+        u = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
+        v = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
+        _check(load().nlm_fd_set_state(self.h, abi.dptr(u), abi.dptr(v)))
+
+    def step_host(self, u, v, f=None, nsteps=1):
+        """Drop-in step on host arrays (u, v updated in place)."""
+        _check(load().nlm_fd_step_host(self.h, abi.dptr(u), abi.dptr(v), abi.dptr(f),
+                                       C.c_int64(int(nsteps))))
+
+    def time(self):
+        t = C.c_double()
+        n = C.c_int64()
+        _check(load().nlm_fd_get_time(self.h, C.byref(t), C.byref(n)))
+        return t.value, n.value
+
+    def bond_state(self):
+        b = np.zeros(self.nnz(), dtype=np.uint8)
+        _check(load().nlm_fd_get_bond_state(self.h, abi.ptr(b, C.c_uint8)))
+        return b
+
+    def count_broken(self):
+        c = C.c_int64()
+        _check(load().nlm_fd_count_broken(self.h, C.byref(c)))
+        return c.value
+
+    def damage(self):
+        phi = np.zeros(self.n, dtype=np.float32)
+        Z = np.zeros(self.n, dtype=np.float32)
+        _check(load().nlm_fd_damage(self.h, abi.ptr(phi, C.c_float), abi.ptr(Z, C.c_float)))
+        return phi, Z
+
+    def decomposition(self):
+        d = C.c_int()
+        _check(load().nlm_fd_decomposition(self.h, C.byref(d)))
+        return d.value
+
+    def set_timing(self, on):
+        _check(load().nlm_fd_set_timing(self.h, C.c_int(int(on))))
+
+    def kernel_stats(self, reset=True):
+        ms = C.c_double()
+        L = C.c_int64()
+        b = C.c_double()
+        _check(load().nlm_fd_kernel_stats(self.h, C.c_int(int(reset)), C.byref(ms), C.byref(L),
+                                          C.byref(b)))
+        return ms.value, L.value, b.value

@@ -1,0 +1,212 @@
+"""Parity of the CUDA RNPBond explicit path with the CPU oracle.
+
+Bars (the benchmark spec): neighbour lists bit-exact (identical sorted index sets);
+broken-bond set identical and u, v, f within 1e-12 relative in FP64 plain
+mode; FP32-compensated mode within 1e-5 relative L2 of the FP64 displacement
+and at most 0.1% differing broken bonds.
+"""
+import numpy as np
+import pytest
+
+from nlmech_gb300 import abi, configs
+from nlmech_gb300.decks import BC
+
+pytestmark = pytest.mark.gpu
+
+FP64_RTOL = 1e-12     # relative to the largest magnitude of the field
+FP32_L2 = 1e-5        # relative L2 of u against the FP64 oracle
+FP32_BROKEN = 1e-3    # fraction of differing broken bonds
+
+
+def rel_max(a, b):
+    s = max(np.abs(b).max(), 1e-300)
+    return float(np.abs(a - b).max() / s)
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def bonds_as_pairs(rowptr, cols, broken):
+    rows = np.repeat(np.arange(len(rowptr) - 1), np.diff(rowptr))
+    sel = broken.astype(bool)
+    return set(zip(rows[sel].tolist(), cols[sel].tolist()))
+
+
+def test_neighbor_search_bit_exact(gpu, oracle):
+    for ratio, seed in ((4, 0), (3, 1)):
+        x, _ = configs.grid2d(100, 100, 1e-3, seed=seed)
+        a = gpu.neighbor_search(x, ratio * 1e-3, dim=2)
+        b = oracle.neighbors(x, ratio * 1e-3, dim=2, grid=False)
+        assert np.array_equal(a[0], b[0])
+        assert np.array_equal(a[1], b[1])
+    x3, _ = configs.grid3d(14, 13, 12, 1e-3, seed=2)
+    a = gpu.neighbor_search(x3, 3e-3, dim=3)
+    b = oracle.neighbors(x3, 3e-3, dim=3, grid=False)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_neighbor_search_edge_cases(gpu, oracle):
+    # single node, two nodes at exactly the horizon, empty
+    a = gpu.neighbor_search(np.zeros((1, 3)), 1.0)
+    assert list(a[0]) == [0, 0]
+    x = np.array([[0., 0, 0], [1., 0, 0], [0., 0.5, 0]])
+    a = gpu.neighbor_search(x, 1.0)
+    b = oracle.neighbors(x, 1.0, grid=False)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    a = gpu.neighbor_search(np.zeros((0, 3)), 1.0)
+    assert list(a[0]) == [0]
+    # coincident points and a dense cluster
+    rng = np.random.default_rng(5)
+    x = np.zeros((300, 3))
+    x[:, :2] = rng.uniform(0, 1e-3, size=(300, 2))
+    x[10] = x[11]
+    a = gpu.neighbor_search(x, 2e-4)
+    b = oracle.neighbors(x, 2e-4, grid=False)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_model_neighbors_and_precrack(gpu, oracle):
+    p = configs.config0()
+    m = gpu.FDModel(p)
+    o = oracle.OracleFD(p, grid_neighbors=False)
+    ra, ca = m.neighbors()
+    rb, cb = o.neighbors()
+    assert np.array_equal(ra, rb) and np.array_equal(ca, cb)
+    assert np.array_equal(m.bond_state(), o.bond_state())
+    assert m.count_broken() == int(o.bond_state().sum())
+
+
+def _compare_fp64(m, o, rowptr, cols, what=""):
+    u, v, f = m.state()
+    uo, vo, fo = o.state()
+    assert rel_max(u, uo) <= FP64_RTOL, what + " u"
+    assert rel_max(v, vo) <= FP64_RTOL, what + " v"
+    assert rel_max(f, fo) <= FP64_RTOL, what + " f"
+    bm, bo = m.bond_state(), o.bond_state()
+    assert bonds_as_pairs(rowptr, cols, bm) == bonds_as_pairs(rowptr, cols, bo), what + " bonds"
+    assert m.time() == o.time()
+
+
+def test_fp64_config0_parity(gpu, oracle):
+    """Config 0 in full: 100x100 plate, 1000 Verlet steps, FP64 plain."""
+    p = configs.config0()
+    m = gpu.FDModel(p, precision=abi.FP64)
+    o = oracle.OracleFD(p)
+    rowptr, cols = o.neighbors()
+    done = 0
+    for n in (1, 9, 190, 800):
+        m.run(n)
+        o.run(n)
+        done += n
+        _compare_fp64(m, o, rowptr, cols, "step %d" % done)
+    assert int(o.bond_state().sum()) > 10000  # the crack has grown
+    phi, Z = m.damage()
+    phio, Zo = o.damage()
+    assert np.abs(phi - phio).max() <= 1e-6
+    assert np.abs(Z - Zo).max() <= 1e-5 * max(1.0, np.abs(Zo).max())
+
+
+def test_fp64_central_difference_parity(gpu, oracle):
+    p = configs.rnp_plate(48, 1e-3, 3, 0.012, 0.5, 2e-8, 300, seed=7)
+    m = gpu.FDModel(p, precision=abi.FP64, scheme=abi.CENTRAL_DIFFERENCE)
+    p2 = configs.rnp_plate(48, 1e-3, 3, 0.012, 0.5, 2e-8, 300, seed=7)
+    p2.scheme = abi.CENTRAL_DIFFERENCE
+    o = oracle.OracleFD(p2)
+    rowptr, cols = o.neighbors()
+    m.run(300)
+    o.run(300)
+    _compare_fp64(m, o, rowptr, cols, "CD")
+
+
+def test_fp64_loads_nofail_influence(gpu, oracle):
+    """Force BC, a sin-in-time displacement BC, no-fail boundary layer and a
+    linear influence function, all through the same step kernel."""
+    p = configs.rnp_plate(40, 1e-3, 3, 0.01, 0.3, 2e-8, 200, seed=11)
+    p.material.influence_type = 1
+    p.material.influence_params = []
+    p.fbc = [BC(region="rectangle", x1=0.0, x2=0.004, y1=0.0, y2=0.04, direction=[1],
+                time_fn="linear", time_params=[1.0], spatial_fn="constant",
+                spatial_params=[-2e12]),
+             BC(region="rectangle", x1=0.0, x2=0.002, y1=0.0, y2=0.04, direction=[1, 2],
+                time_fn="sin", time_params=[1.0, 2e4], spatial_fn="linear_y",
+                spatial_params=[1e14])]
+    p.ubc.append(BC(region="rectangle", x1=0.036, x2=0.041, y1=0.01, y2=0.03, direction=[1],
+                    time_fn="sin", time_params=[1e-7, 5e4], spatial_fn="constant",
+                    spatial_params=[1.0]))
+    p.no_fail = abi.NOFAIL_COMPUTE
+    p.no_fail_tol = 2e-3
+    m = gpu.FDModel(p, precision=abi.FP64)
+    o = oracle.OracleFD(p)
+    rowptr, cols = o.neighbors()
+    m.run(200)
+    o.run(200)
+    u, v, f = m.state()
+    uo, vo, fo = o.state()
+    # sin/cos of the BC and exp of the bond are libm-vs-CUDA last-ulp apart
+    assert rel_max(u, uo) <= 1e-11
+    assert rel_max(v, vo) <= 1e-11
+    assert rel_max(f, fo) <= 1e-11
+    assert bonds_as_pairs(rowptr, cols, m.bond_state()) == bonds_as_pairs(rowptr, cols, o.bond_state())
+
+
+def test_fp64_3d_rnp_parity(gpu, oracle):
+    x, vol = configs.grid3d(14, 14, 14, 1e-3, seed=3)
+    p = configs.rnp_plate(8, 1e-3, 3, 0.0, 0.1, 2e-8, 10)
+    p.dim = 3
+    p.x, p.volume = x, vol
+    p.horizon = 3e-3
+    p.cracks = []
+    p.ubc = [BC(region="cuboid", x1=-1, x2=1, y1=-1, y2=1, z1=-1, z2=2e-3, direction=[3],
+                time_fn="linear", time_params=[-0.5]),
+             BC(region="cuboid", x1=-1, x2=1, y1=-1, y2=1, z1=12e-3, z2=1, direction=[3],
+                time_fn="linear", time_params=[0.5])]
+    m = gpu.FDModel(p, precision=abi.FP64)
+    o = oracle.OracleFD(p)
+    rowptr, cols = o.neighbors()
+    m.run(150)
+    o.run(150)
+    _compare_fp64(m, o, rowptr, cols, "3D")
+
+
+def test_fp32c_config0_error(gpu, oracle):
+    """FP32-compensated against the FP64 oracle on config 0 (1000 steps)."""
+    p = configs.config0()
+    o = oracle.OracleFD(p)
+    o.run(1000)
+    uo, vo, fo = o.state()
+    rowptr, cols = o.neighbors()
+    bo = bonds_as_pairs(rowptr, cols, o.bond_state())
+    for dec in (abi.DECOMP_THREAD, abi.DECOMP_WARP):
+        m = gpu.FDModel(p, precision=abi.FP32C, decomposition=dec)
+        m.run(1000)
+        u, v, f = m.state()
+        assert rel_l2(u, uo) <= FP32_L2
+        bm = bonds_as_pairs(rowptr, cols, m.bond_state())
+        ndiff = len(bm ^ bo)
+        assert ndiff <= FP32_BROKEN * max(len(bo), 1), (ndiff, len(bo))
+
+
+def test_step_host_matches_run(gpu):
+    p = configs.rnp_plate(30, 1e-3, 3, 0.008, 0.1, 2e-8, 50, seed=2)
+    a = gpu.FDModel(p, precision=abi.FP64)
+    a.run(20)
+    ua, va, fa = a.state()
+    b = gpu.FDModel(p, precision=abi.FP64)
+    u = np.zeros((p.n, 3))
+    v = np.zeros((p.n, 3))
+    f = np.zeros((p.n, 3))
+    b.step_host(u, v, f, nsteps=20)
+    assert np.array_equal(u, ua) and np.array_equal(v, va) and np.array_equal(f, fa)
+
+
+def test_runs_are_deterministic(gpu):
+    p = configs.config0()
+    for prec in (abi.FP64, abi.FP32C):
+        r = []
+        for _ in range(2):
+            m = gpu.FDModel(p, precision=prec)
+            m.run(300)
+            r.append(m.state() + (m.bond_state(),))
+        for a, b in zip(r[0], r[1]):
+            assert np.array_equal(a, b)

@@ -1,0 +1,314 @@
+#!/usr/bin/env python
+"""Headline benchmark: explicit RNPBond peridynamics step on one GB300.
+
+Workload (default): the 1000 x 1000 node plate (h = 1e-4 m, horizon 3h,
+seeded +-0.05h jitter, 2 mm centre pre-crack, top/bottom 3-node layers pulled
+at +-0.1 m/s, velocity-Verlet dt = 2e-9 s).  A step is one Verlet step: one
+fused force + integrate launch over every node.  The metric is bond-updates/s
+= directed bonds x steps / time.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  `value` is the FP32-compensated device throughput with
+the state resident in HBM; `fp64_plain` is the same run in FP64 plain mode;
+`e2e` is measured through the host-resident drop-in call nlm_fd_step_host,
+copying u, v, f in and out of pinned host memory every step.  The
+`--impl reference` arm times the CPU restatement of the reference (oracle/)
+on the host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "bond-updates/s FP32 vs FP64 plain; QS Newton s, learned vs plain @1e-8 res"
+UNIT = "bond-updates/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nx", type=int, default=1000, help="plate nodes per side")
+    ap.add_argument("--fp64-steps", type=int, default=200)
+    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--cpu-steps", type=int, default=30)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--quick", action="store_true",
+                    help="FP32C timed run only (profiling driver)")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def problem(nx, seed):
+    from nlmech_gb300 import configs
+    if nx == 1000:
+        p = configs.config1(seed=seed)
+    else:
+        p = configs.rnp_plate(nx, 0.1 / nx, 3, 0.02 * 0.1, 0.1, 2e-9, 5000, seed=seed)
+    return p
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "50"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return None
+
+
+def profiled_traffic():
+    """dram bytes per launch of the step kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "rnp_fp32_step_plate1000.md")
+    try:
+        for ln in open(p):
+            if ln.startswith("traffic_bytes_per_launch:"):
+                return float(ln.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(nx, steps, threads=None):
+    """The oracle (CPU restatement of FDModel<RNPBond>) on a bounded sample."""
+    from oracle import oracle as orc
+    if threads:
+        orc.set_threads(threads)
+    p = problem(nx, 0)
+    o = orc.OracleFD(p)
+    nnz = o.nnz()
+    o.run(1)  # step-0 force evaluation and one step, untimed
+    t0 = time.perf_counter()
+    o.run(steps)
+    dt = time.perf_counter() - t0
+    return {"value": nnz * steps / dt, "unit": UNIT, "cores": orc.num_threads(), "kind": "port",
+            "sample": "%d Verlet steps of the %dx%d plate (%d bonds), after 1 untimed step"
+                      % (steps, nx, nx, nnz)}
+
+
+def run_reference(a):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    steps = min(a.steps, a.cpu_steps)
+    cb = cpu_baseline(a.nx, steps)
+    cb["sample"] += "; K=%d requested, %d timed (bounded CPU sample)" % (a.steps, steps)
+    nnz = float(cb["sample"].split("(")[1].split()[0])
+    out = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "impl": "reference",
+           "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+           "ms_per_step": 1e3 * nnz / cb["value"], "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered plate)",
+           "config": {"workload": "rnp2d_plate_%dx%d_d3h_verlet" % (a.nx, a.nx),
+                      "nodes": a.nx * a.nx},
+           "cpu_baseline": cb,
+           "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    return 0
+
+
+def run_ours(a):
+    rank, world, local = dist_env()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    from nlmech_gb300 import abi, build, gpu
+    build.build()
+    gpu.set_device(local)
+    p = problem(a.nx, seed=rank)
+    n = p.n
+
+    def barrier_sync():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+            torch.cuda.synchronize()
+
+    def max_over_ranks(v):
+        if world == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum_over_ranks(v):
+        if world == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t)
+        return float(t.item())
+
+    # ---- FP32-compensated (headline) ----
+    m = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_THREAD)
+    nnz = m.nnz()
+    m.run(a.warmup)
+    barrier_sync()
+    with ClockSampler(local) as cs:
+        ms = m.run_timed(a.steps)
+    barrier_sync()
+    ms = max_over_ranks(ms)
+    total_bonds = sum_over_ranks(float(nnz))
+    value = total_bonds * a.steps / (ms * 1e-3)
+    clocks = cs.summary()
+    if a.quick:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "quick": True,
+                              "ms_per_step": ms / a.steps, "steps": a.steps}))
+        return 0
+    # per-launch kernel time of the step kernel (separate timed pass)
+    m.set_timing(True)
+    m.kernel_stats(reset=True)
+    m.run(min(a.steps, 500))
+    kms, launches, bytes_per_launch = m.kernel_stats(reset=True)
+    m.set_timing(False)
+    broken = m.count_broken()
+    m.close()
+
+    # ---- FP64 plain ----
+    m64 = gpu.FDModel(p, precision=abi.FP64)
+    m64.run(3)
+    barrier_sync()
+    ms64 = m64.run_timed(a.fp64_steps)
+    barrier_sync()
+    ms64 = max_over_ranks(ms64)
+    value64 = total_bonds * a.fp64_steps / (ms64 * 1e-3)
+    m64.close()
+
+    # ---- end to end through the host-resident drop-in call ----
+    me = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_THREAD)
+    bufs = [torch.zeros((n, 3), dtype=torch.float64).pin_memory() for _ in range(3)]
+    ptrs = [b.data_ptr() for b in bufs]
+    me.step_host_ptr(*ptrs, nsteps=1)  # step 0 + first step (untimed)
+    for _ in range(3):
+        me.step_host_ptr(*ptrs, nsteps=1)
+    barrier_sync()
+    t0 = time.perf_counter()
+    for _ in range(a.e2e_steps):
+        me.step_host_ptr(*ptrs, nsteps=1)
+    barrier_sync()
+    te = max_over_ranks(time.perf_counter() - t0)
+    e2e_value = total_bonds * a.e2e_steps / te
+    me.close()
+
+    if rank != 0:
+        return 0
+    peaks = measured_peaks()
+    if peaks and peaks.get("hbm_gbs"):
+        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    achieved = bytes_per_launch / (kms * 1e-3) / 1e9 if kms > 0 else None
+    traffic = profiled_traffic()
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 bond math, f64 state",
+        "data": "synthetic (seeded jittered plate)",
+        "config": {"workload": "rnp2d_plate_%dx%d_d3h_verlet" % (a.nx, a.nx), "nodes": n,
+                   "bonds": nnz, "horizon": "3h", "dt": p.dt, "precision": "fp32c",
+                   "decomposition": "thread-per-node sliced-ELL",
+                   "l2": "inputs larger than L2: %.0f MB moved per step vs 129 MB L2"
+                         % (bytes_per_launch / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "fp64_plain": {"value": value64, "unit": UNIT, "steps": a.fp64_steps,
+                       "ms_per_step": ms64 / a.fp64_steps},
+        "fp32_over_fp64": value / value64,
+        "broken_bonds_after_run": broken,
+        "e2e": {"value": e2e_value, "unit": UNIT, "steps": a.e2e_steps,
+                "h2d_bytes_per_step": 3 * 3 * 8 * n, "d2h_bytes_per_step": 3 * 3 * 8 * n,
+                "call": "nlm_fd_step_host (u, v, f in/out of pinned host memory each step)"},
+        "gpu_launches": a.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "peak_source": peak_src, "kernel": "k_rnp32_thread",
+                     "kernel_ms": kms, "bytes_per_launch": bytes_per_launch},
+        "clocks": clocks,
+    }
+    if not a.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(a.nx, a.cpu_steps)
+    print(json.dumps(out))
+    return 0
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        return run_reference(a)
+    return run_ours(a)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -181,6 +181,8 @@ const char *nlm_last_error(void);
 int nlm_abi_version(void);
 /* Number of CUDA devices visible (0 on a host without a GPU). */
 int nlm_device_count(int *count);
+/* Select the device used by handles created afterwards on this thread. */
+int nlm_set_device(int device);
 
 /* ---- neighbour search (replaces geometry::Neighbor, neighbor.cpp:24-92) --
  * Builds rows {j != i : definitelyLessThan(|x_i - x_j|, horizon + 1e-10)}
@@ -233,12 +235,17 @@ int nlm_fd_set_timing(nlm_fd *h, int enable);
 /* Synchronize the handle's stream. */
 int nlm_fd_sync(nlm_fd *h);
 
-/* Drop-in step for a host-resident state (the reference DataManager keeps
- * u, v, f on the host): copies u, v in, advances nsteps, copies u, v and f
- * out (f may be NULL).  Used by FDModel-shaped hosts that keep their own
- * arrays. */
+/* Drop-in step for a host-resident state (the reference's DataManager keeps
+ * u, v, f on the host, fDModel.cpp:200-206): copies u, v and f (3*n each) in,
+ * advances nsteps from them, copies u, v and f out.  The first call on a
+ * fresh handle performs the step-0 force evaluation (f is then output only).
+ * Passing back unchanged the arrays of the previous call continues the run
+ * exactly as nlm_fd_run would. */
 int nlm_fd_step_host(nlm_fd *h, double *u, double *v, double *f,
                      int64_t nsteps);
+/* nlm_fd_run bracketed by CUDA events on the handle's stream; *ms is the
+ * device time of the whole run (the stream is synchronized). */
+int nlm_fd_run_timed(nlm_fd *h, int64_t nsteps, double *ms);
 
 #ifdef __cplusplus
 }

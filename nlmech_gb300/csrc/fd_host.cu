@@ -225,6 +225,13 @@ __global__ void k_scatter_split(int64_t n, int S, int dim, const int *perm, cons
     dst[2 * i + 1] = make_float4(l[0], l[1], l[2], 0.f);
   }
 }
+__global__ void k_scatter_f32(int64_t n, int S, int dim, const int *perm, const double *src,
+                              float *dst) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double *p = src + 3 * (int64_t)perm[i];
+  for (int d = 0; d < S; d++) dst[S * i + d] = (d < dim && d < 3) ? (float)p[d] : 0.f;
+}
 __global__ void k_gather_vec(int64_t n, int S, const int *perm, const double *src, double *dst) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -511,6 +518,11 @@ int nlm_device_count(int *count) {
     c = 0;
   }
   *count = c;
+  return NLM_OK;
+}
+
+int nlm_set_device(int device) {
+  NLM_CUDA(cudaSetDevice(device));
   return NLM_OK;
 }
 
@@ -1073,11 +1085,60 @@ int nlm_fd_kernel_stats(nlm_fd *h, int reset, double *avg_ms, int64_t *launches,
 }
 
 int nlm_fd_step_host(nlm_fd *h, double *u, double *v, double *f, int64_t nsteps) {
-  if (!h || !u || !v) return fail(NLM_ERR_INVALID, "null argument");
-  int rc = nlm_fd_set_state(h, u, v);
+  if (!h || !u || !v || !f || nsteps < 0) return fail(NLM_ERR_INVALID, "null argument");
+  if (!h->started) {
+    int rc = nlm_fd_set_state(h, u, v);
+    if (rc) return rc;
+    if ((rc = do_run(h, nsteps))) return rc;
+    return nlm_fd_get_state(h, u, v, f);
+  }
+  const int64_t n = h->n;
+  if (!finite_all(u, 3 * n) || !finite_all(v, 3 * n) || !finite_all(f, 3 * n))
+    return fail(NLM_ERR_NONFINITE, "non-finite state");
+  cudaStream_t s = h->stream;
+  const int *P = h->D.perm_dev;
+  const unsigned g = nblk(n, 256);
+  const bool fp32 = h->precision == NLM_PREC_FP32C;
+  NLM_CUDA(cudaMemcpyAsync(h->stage, u, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  if (fp32)
+    k_scatter_split<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.u32[h->cur]);
+  else
+    k_scatter_vec<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.u64[h->cur]);
+  NLM_CUDA(cudaGetLastError());
+  NLM_CUDA(cudaMemcpyAsync(h->stage, v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  k_scatter_vec<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage,
+                                  h->D.v[h->scheme == NLM_CENTRAL_DIFFERENCE ? h->cur : 0]);
+  NLM_CUDA(cudaGetLastError());
+  NLM_CUDA(cudaMemcpyAsync(h->stage, f, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  if (fp32)
+    k_scatter_f32<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.f32);
+  else
+    k_scatter_vec<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.f64);
+  NLM_CUDA(cudaGetLastError());
+  cudaError_t e = launch_drift(h->P, h->D, h->T, h->cur, h->time + h->dt, fp32, s);
+  if (e != cudaSuccess) return cuda_fail(e, "drift kernel");
+  int rc = do_run(h, nsteps);
   if (rc) return rc;
-  if ((rc = do_run(h, nsteps))) return rc;
   return nlm_fd_get_state(h, u, v, f);
+}
+
+int nlm_fd_run_timed(nlm_fd *h, int64_t nsteps, double *ms) {
+  if (!h || !ms || nsteps < 0) return fail(NLM_ERR_INVALID, "bad arguments");
+  cudaEvent_t a, b;
+  NLM_CUDA(cudaEventCreate(&a));
+  NLM_CUDA(cudaEventCreate(&b));
+  cudaEventRecord(a, h->stream);
+  int rc = do_run(h, nsteps);
+  cudaEventRecord(b, h->stream);
+  cudaError_t e = cudaEventSynchronize(b);
+  float t = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&t, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "run timing");
+  *ms = t;
+  return NLM_OK;
 }
 
 }  // extern "C"

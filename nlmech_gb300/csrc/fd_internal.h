@@ -57,6 +57,10 @@ cudaError_t launch_es_step_fp64(const StepParams &P, const DevPtrs &D, const BCT
                                 const StepArgs &a, int decomp, cudaStream_t s);
 cudaError_t launch_es_step_fp32(const StepParams &P, const DevPtrs &D, const BCTable &T,
                                 const StepArgs &a, int decomp, cudaStream_t s);
+// Recompute the drift to u^{m+1} (and v^{m+1} for CD) from (u^m, v^m, f^m)
+// after the host replaced the state: the second half of the step epilogue.
+cudaError_t launch_drift(const StepParams &P, const DevPtrs &D, const BCTable &T, int cur,
+                         double t_next, bool fp32, cudaStream_t s);
 cudaError_t launch_damage(const StepParams &P, const DevPtrs &D, int cur, bool fp32,
                           bool es, float *phi, float *Z, cudaStream_t s);
 

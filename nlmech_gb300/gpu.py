@@ -55,6 +55,10 @@ def device_count():
     return c.value
 
 
+def set_device(dev):
+    _check(load().nlm_set_device(C.c_int(int(dev))))
+
+
 def neighbor_search(x, horizon, dim=2):
     """GPU cell-list neighbour lists in original ids (rowptr int64, cols int32)."""
     x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
@@ -120,10 +124,24 @@ class FDModel:
         v = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
         _check(load().nlm_fd_set_state(self.h, abi.dptr(u), abi.dptr(v)))
 
-    def step_host(self, u, v, f=None, nsteps=1):
-        """Drop-in step on host arrays (u, v updated in place)."""
+    def step_host(self, u, v, f, nsteps=1):
+        """Drop-in step on host arrays u, v, f (3 doubles per node, updated
+        in place); passing back the previous call's arrays continues the run."""
         _check(load().nlm_fd_step_host(self.h, abi.dptr(u), abi.dptr(v), abi.dptr(f),
                                        C.c_int64(int(nsteps))))
+
+    def step_host_ptr(self, u_ptr, v_ptr, f_ptr, nsteps=1):
+        """Same as step_host with raw host addresses (e.g. pinned buffers)."""
+        P = C.POINTER(C.c_double)
+        _check(load().nlm_fd_step_host(self.h, C.cast(u_ptr, P), C.cast(v_ptr, P),
+                                       C.cast(f_ptr, P), C.c_int64(int(nsteps))))
+
+    def run_timed(self, nsteps):
+        """Run nsteps; returns the device time in ms (CUDA events on the
+        handle's stream)."""
+        ms = C.c_double()
+        _check(load().nlm_fd_run_timed(self.h, C.c_int64(int(nsteps)), C.byref(ms)))
+        return ms.value
 
     def time(self):
         t = C.c_double()

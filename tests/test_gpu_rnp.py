@@ -188,16 +188,25 @@ def test_fp32c_config0_error(gpu, oracle):
 
 
 def test_step_host_matches_run(gpu):
+    """Host-resident drop-in: calls that pass back the previous arrays
+    continue the run bit for bit."""
     p = configs.rnp_plate(30, 1e-3, 3, 0.008, 0.1, 2e-8, 50, seed=2)
-    a = gpu.FDModel(p, precision=abi.FP64)
-    a.run(20)
-    ua, va, fa = a.state()
-    b = gpu.FDModel(p, precision=abi.FP64)
-    u = np.zeros((p.n, 3))
-    v = np.zeros((p.n, 3))
-    f = np.zeros((p.n, 3))
-    b.step_host(u, v, f, nsteps=20)
-    assert np.array_equal(u, ua) and np.array_equal(v, va) and np.array_equal(f, fa)
+    for prec in (abi.FP64, abi.FP32C):
+        a = gpu.FDModel(p, precision=prec)
+        a.run(20)
+        ua, va, fa = a.state()
+        b = gpu.FDModel(p, precision=prec)
+        u = np.zeros((p.n, 3))
+        v = np.zeros((p.n, 3))
+        f = np.zeros((p.n, 3))
+        b.step_host(u, v, f, nsteps=5)
+        for _ in range(15):
+            b.step_host(u, v, f, nsteps=1)
+        assert b.time() == a.time()
+        if prec == abi.FP64:
+            assert np.array_equal(u, ua) and np.array_equal(v, va) and np.array_equal(f, fa)
+        else:
+            assert rel_max(u, ua) < 1e-12 and rel_max(v, va) < 1e-9
 
 
 def test_runs_are_deterministic(gpu):

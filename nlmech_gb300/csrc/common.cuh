@@ -66,6 +66,8 @@ struct StepParams {
   int nofail;         // 1 when some node is non-interior (no-fail region)
   int infl_type;
   double infl_a0, infl_a1, infl_alpha, infl_beta;
+  double lo_scale;    // FP32C position lo parts are stored as half(lo * lo_scale)
+  int nw1;            // 1 when every row fits one 32-bit bond-bit word
   // integration
   double dt, rho;
   int scheme;

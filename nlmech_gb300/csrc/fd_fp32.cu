@@ -1,14 +1,24 @@
 // fd_fp32.cu -- FP32 "compensated" explicit-step kernels (RNPBond).
 //
-// Bond arithmetic runs in FP32 on split coordinates: every position and
-// displacement is stored as an FP32 pair (hi, lo) with value hi + lo, so the
-// bond vectors xi = x_j - x_i and eta = u_j - u_i are formed as
-// (hi_j - hi_i) + (lo_j - lo_i).  The hi difference of two nearby nodes is
-// exact (Sterbenz), so xi and eta keep ~2^-24 relative accuracy however small
-// they are compared with the coordinates.  The bond strain is the linearised
-// S = xi.eta / |xi|^2 of RNPBond::getS (src/material/pd/rnpBond.cpp:303-306),
-// which has no cancellation once eta is accurate.  Forces are summed in FP32;
-// velocity and the time update stay FP64 per node.
+// Bond arithmetic runs in FP32 on split coordinates.  A position is stored as
+// hi = (float)x plus its remainder lo = x - hi, packed as a half of
+// lo * lo_scale (lo_scale = 2^24 / X with X the power of two above max |x|,
+// so |lo * lo_scale| <= 1/2).  A displacement is an FP32 pair (hi, lo).  The
+// bond vectors are formed as
+//   xi  = (xh_j - xh_i) + (xl_j - xl_i),   eta = (uh_j - uh_i) + (ul_j - ul_i)
+// The hi difference of two nearby nodes is exact (Sterbenz), so xi and eta
+// keep ~2^-24 relative accuracy however small they are compared with the
+// coordinates (the half-packed position remainder costs ~2^-36 X absolute).
+// The bond strain is the linearised S = xi.eta / |xi|^2 of RNPBond::getS
+// (src/material/pd/rnpBond.cpp:303-306), free of cancellation once eta is
+// accurate.  Forces are summed in FP32.
+//
+// Time integration runs on (hi, lo) FP32 pairs ("double-float", ~48-bit
+// significand) with error-free transformations (Knuth's TwoSum and the FMA
+// TwoProduct): GB300's FP64 rate is a small fraction of its FP32 rate, and the
+// per-node FP64 update would otherwise be the slowest part of the step.
+
+#include <cuda_fp16.h>
 
 #include "fd_internal.h"
 #include "state_io.cuh"
@@ -20,10 +30,20 @@ struct Params32 {
   float check_up, inv_h, inv_delta;
   float K1;             // 4 C beta / invF (times J when J is constant)
   float Ksc;            // (f_sc rbar)^2 / (1 - 1e-5)^2: |S| > S_c  <=>  S^2 r > Ksc
-  float beta;
+  float nbl2e;          // -beta * log2(e)
+  float inv_lo;         // 1 / lo_scale
   int infl_type;
   float a0, a1, alpha, ibeta;
+  // integrator constants as (hi, lo) pairs
+  float c_hi, c_lo;     // Verlet dt/(2 rho) or CD dt^2/rho
+  float dt_hi, dt_lo;
+  float idt_hi, idt_lo; // 1/dt
 };
+
+static void split_const(double v, float &hi, float &lo) {
+  hi = (float)v;
+  lo = (float)(v - (double)hi);
+}
 
 static Params32 make_p32(const StepParams &P) {
   Params32 q;
@@ -34,185 +54,295 @@ static Params32 make_p32(const StepParams &P) {
   double k1 = 4.0 * P.C * P.beta / P.invF;
   if (P.infl_type == 0) k1 *= P.infl_a0;
   q.K1 = (float)k1;
-  double sc = P.fsc * P.rbar / (1.0 - 1e-5);
+  const double sc = P.fsc * P.rbar / (1.0 - 1e-5);
   q.Ksc = (float)(sc * sc);
-  q.beta = (float)P.beta;
+  q.nbl2e = (float)(-P.beta * 1.4426950408889634);
+  q.inv_lo = (float)(1.0 / P.lo_scale);
   q.infl_type = P.infl_type;
   q.a0 = (float)P.infl_a0;
   q.a1 = (float)P.infl_a1;
   q.alpha = (float)P.infl_alpha;
-  q.ibeta = (float)(1.0 / P.infl_beta);
+  q.ibeta = P.infl_type == 2 ? (float)(1.0 / P.infl_beta) : 0.f;
+  const double c = P.scheme == NLM_VELOCITY_VERLET ? 0.5 * P.dt / P.rho : P.dt * P.dt / P.rho;
+  split_const(c, q.c_hi, q.c_lo);
+  split_const(P.dt, q.dt_hi, q.dt_lo);
+  split_const(1.0 / P.dt, q.idt_hi, q.idt_lo);
   return q;
 }
 
+// ---- FP32 approximate transcendental instructions -------------------------
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// ---- double-float arithmetic (error-free transformations) ------------------
+struct df {
+  float hi, lo;
+};
+__device__ __forceinline__ df two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ df fast_two_sum(float a, float b) {
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ df df_add(df x, df y) {
+  const df s = two_sum(x.hi, y.hi);
+  return fast_two_sum(s.hi, s.lo + (x.lo + y.lo));
+}
+__device__ __forceinline__ df df_sub(df x, df y) { return df_add(x, {-y.hi, -y.lo}); }
+// (c_hi + c_lo) * y for a float y, as a pair
+__device__ __forceinline__ df df_cmul(float c_hi, float c_lo, float y) {
+  const float p = c_hi * y;
+  const float e = fmaf(c_hi, y, -p);
+  return fast_two_sum(p, fmaf(c_lo, y, e));
+}
+// x * (c_hi + c_lo)
+__device__ __forceinline__ df df_mul_c(df x, float c_hi, float c_lo) {
+  const float p = x.hi * c_hi;
+  float e = fmaf(x.hi, c_hi, -p);
+  e = fmaf(x.lo, c_hi, fmaf(x.hi, c_lo, e));
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ df df_from_double(double v) {
+  const float h = __double2float_rn(v);
+  return {h, __double2float_rn(v - (double)h)};
+}
+
+// ---- node access -----------------------------------------------------------
 template <int DIM>
-__device__ __forceinline__ void ld_hl(const float4 *p, int64_t j, float h[3], float l[3]) {
+struct Node32 {
+  float xh[3];
+  __half2 lxy;  // lo of (x, y), scaled
+  __half2 lz;   // lo of z (3-D), scaled
+  float vol;
+};
+
+template <int DIM>
+__device__ __forceinline__ void ld_pos(const DevPtrs &D, int64_t j, Node32<DIM> &n) {
   if (DIM == 2) {
-    const float4 a = __ldg(p + j);
+    const float4 a = __ldg(D.pos32 + j);
+    n.xh[0] = a.x;
+    n.xh[1] = a.y;
+    n.xh[2] = 0.f;
+    n.vol = a.z;
+    n.lxy = *reinterpret_cast<const __half2 *>(&a.w);
+    n.lz = __floats2half2_rn(0.f, 0.f);
+  } else {
+    const float4 a = __ldg(D.pos32 + j);
+    const uint2 b = __ldg(D.pos32lo + j);
+    n.xh[0] = a.x;
+    n.xh[1] = a.y;
+    n.xh[2] = a.z;
+    n.vol = a.w;
+    n.lxy = *reinterpret_cast<const __half2 *>(&b.x);
+    n.lz = *reinterpret_cast<const __half2 *>(&b.y);
+  }
+}
+
+template <int DIM>
+__device__ __forceinline__ void ld_pair(const float4 *p, int64_t j, float h[3], float l[3]) {
+  if (DIM == 2) {
+    const float4 a = p[j];
     h[0] = a.x; h[1] = a.y; h[2] = 0.f;
     l[0] = a.z; l[1] = a.w; l[2] = 0.f;
   } else {
-    const float4 a = __ldg(p + 2 * j), b = __ldg(p + 2 * j + 1);
+    const float4 a = p[2 * j], b = p[2 * j + 1];
     h[0] = a.x; h[1] = a.y; h[2] = a.z;
     l[0] = b.x; l[1] = b.y; l[2] = b.z;
   }
 }
 
-// Bond force of RNPBond in FP32.  Returns s with F = s * xi (xi unnormalised;
-// the 1/|xi| of the direction is folded into s).
 template <int DIM>
-__device__ __forceinline__ float rnp_bond32(const Params32 &Q, const float xih[3],
-                                            const float xil[3], const float uih[3],
-                                            const float uil[3], const float xjh[3],
-                                            const float xjl[3], const float ujh[3],
-                                            const float ujl[3], float volj, bool breakable,
-                                            bool irrev, bool &fs, float d[3]) {
-  float e[3];
-  for (int c = 0; c < DIM; c++) {
-    d[c] = (xjh[c] - xih[c]) + (xjl[c] - xil[c]);
-    e[c] = (ujh[c] - uih[c]) + (ujl[c] - uil[c]);
+__device__ __forceinline__ void st_pair(float4 *p, int64_t j, const df v[3]) {
+  if (DIM == 2) {
+    p[j] = make_float4(v[0].hi, v[1].hi, v[0].lo, v[1].lo);
+  } else {
+    p[2 * j] = make_float4(v[0].hi, v[1].hi, v[2].hi, 0.f);
+    p[2 * j + 1] = make_float4(v[0].lo, v[1].lo, v[2].lo, 0.f);
   }
+}
+
+// Bond force of RNPBond in FP32 (rnpBond.cpp:242-300 with contact off).
+// Returns s with F = s * xi (the 1/|xi| of the direction is folded into s).
+template <int DIM>
+__device__ __forceinline__ float rnp_bond32(const Params32 &Q, const Node32<DIM> &ni,
+                                            const float uih[3], const float uil[3],
+                                            const Node32<DIM> &nj, const float ujh[3],
+                                            const float ujl[3], bool breakable, bool irrev,
+                                            bool &fs, float d[3]) {
+  const float2 dl = __half22float2(__hsub2(nj.lxy, ni.lxy));
+  d[0] = fmaf(dl.x, Q.inv_lo, nj.xh[0] - ni.xh[0]);
+  d[1] = fmaf(dl.y, Q.inv_lo, nj.xh[1] - ni.xh[1]);
+  float e0 = (ujh[0] - uih[0]) + (ujl[0] - uil[0]);
+  float e1 = (ujh[1] - uih[1]) + (ujl[1] - uil[1]);
   float r2 = d[0] * d[0] + d[1] * d[1];
-  float de = d[0] * e[0] + d[1] * e[1];
+  float de = d[0] * e0 + d[1] * e1;
   if (DIM == 3) {
-    r2 += d[2] * d[2];
-    de += d[2] * e[2];
+    const float2 dz = __half22float2(__hsub2(nj.lz, ni.lz));
+    d[2] = fmaf(dz.x, Q.inv_lo, nj.xh[2] - ni.xh[2]);
+    const float e2 = (ujh[2] - uih[2]) + (ujl[2] - uil[2]);
+    r2 = fmaf(d[2], d[2], r2);
+    de = fmaf(d[2], e2, de);
   }
-  const float rinv = rsqrtf(r2);
+  const float rinv = rsqrt_approx(r2);
   const float r = r2 * rinv;
   const float S = de * (rinv * rinv);
+  float volj = nj.vol;
   if (r > Q.check_low_eff) volj *= (Q.check_up - r) * Q.inv_h;
   float k = Q.K1;
-  if (Q.infl_type == 1)
+  if (Q.infl_type == 1) {
     k *= Q.a0 + Q.a1 * (r * Q.inv_delta);
-  else if (Q.infl_type == 2) {
+  } else if (Q.infl_type == 2) {
     const float rr = r * Q.inv_delta;
-    k *= Q.alpha * __expf(-rr * rr * Q.ibeta);
+    k *= Q.alpha * ex2_approx(-rr * rr * Q.ibeta * 1.4426950408889634f);
   }
   const float s0 = k * S * volj * rinv;
   if (!breakable) return s0;
   const float bs2 = S * S * r;
   if (irrev && !fs && bs2 > Q.Ksc) fs = true;
   if (fs) return 0.f;
-  return s0 * __expf(-Q.beta * bs2);
+  return s0 * ex2_approx(Q.nbl2e * bs2);
 }
 
-// FP32C integrator epilogue: same update as integrate_node64 with the
-// displacement kept as an FP32 (hi, lo) pair and f stored in FP32.
+// Prescribed (du, dv) of one dof as double-float pairs.
+__device__ __forceinline__ void bc_df(const DevPtrs &D, const BCTable &T, int ref, int c, double t,
+                                      df &u, df &v) {
+  double du, dv;
+  bc_dof(D, T, ref, c, t, du, dv);
+  u = df_from_double(du);
+  v = df_from_double(dv);
+}
+
+// FP32C integrator epilogue (same phase structure as integrate_node64).
 template <int DIM, int SCHEME, bool FIRST>
-__device__ __forceinline__ void integrate_node32(const StepParams &P, const DevPtrs &D,
-                                                 const BCTable &T, const StepArgs &A,
-                                                 int64_t i, uint8_t fl, const float uih[3],
-                                                 const float uil[3], const float fint[3]) {
-  double f[3] = {fint[0], fint[1], fint[2]};
+__device__ __forceinline__ void integrate_node32(const StepParams &P, const Params32 &Q,
+                                                 const DevPtrs &D, const BCTable &T,
+                                                 const StepArgs &A, int64_t i, uint8_t fl,
+                                                 const float uih[3], const float uil[3],
+                                                 const float fint[3]) {
+  float f[3] = {fint[0], fint[1], fint[2]};
   if (fl & FLAG_FBC) {
     double fe[3];
     ld_node<DIM>(D.fext, i, fe);
-    for (int c = 0; c < DIM; c++) f[c] = fe[c] + (double)fint[c];
+    for (int c = 0; c < DIM; c++) f[c] = (float)(fe[c] + (double)fint[c]);
   }
-  float fs_[3] = {(float)f[0], (float)f[1], (float)f[2]};
-  double ui[3], un[3] = {0., 0., 0.};
-  for (int c = 0; c < DIM; c++) ui[c] = (double)uih[c] + (double)uil[c];
   const int ref = (fl & 7) ? D.bcref[i] : -1;
+  df un[3], vn[3];
   if (SCHEME == NLM_VELOCITY_VERLET) {
-    const double fact = 0.5 * P.dt / P.rho;
-    double v[3], vn[3];
-    ld_node_rw<DIM>(D.v[0], i, v);
+    float vh_[3], vl_[3];
+    ld_pair<DIM>(D.v32[0], i, vh_, vl_);
+    float fp[3] = {0.f, 0.f, 0.f};
     if (!FIRST) {
-      double fp[3];
-      ld_f32<DIM>(D.f32, i, fp);
-      for (int c = 0; c < DIM; c++) {
-        if (!(fl >> c & 1)) {
-          vn[c] = (v[c] + fact * fp[c]) + fact * f[c];
-        } else {
-          double du, dv;
-          bc_dof(D, T, ref, c, A.t_now, du, dv);
+      if (DIM == 2) {
+        const float2 a = reinterpret_cast<const float2 *>(D.f32)[i];
+        fp[0] = a.x;
+        fp[1] = a.y;
+      } else {
+        const float4 a = reinterpret_cast<const float4 *>(D.f32)[i];
+        fp[0] = a.x;
+        fp[1] = a.y;
+        fp[2] = a.z;
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < DIM; c++) {
+      const df v{vh_[c], vl_[c]};
+      if (!(fl >> c & 1)) {
+        const df cf = df_cmul(Q.c_hi, Q.c_lo, f[c]);
+        df vm = v;
+        if (!FIRST) vm = df_add(df_add(v, df_cmul(Q.c_hi, Q.c_lo, fp[c])), cf);
+        vn[c] = vm;
+        const df vh2 = df_add(vm, cf);
+        un[c] = df_add({uih[c], uil[c]}, df_mul_c(vh2, Q.dt_hi, Q.dt_lo));
+      } else {
+        df du, dv;
+        if (!FIRST) {
+          bc_df(D, T, ref, c, A.t_now, du, dv);
           vn[c] = dv;
+        } else {
+          vn[c] = v;
         }
-      }
-    } else {
-      for (int c = 0; c < DIM; c++) vn[c] = v[c];
-    }
-    for (int c = 0; c < DIM; c++) {
-      if (!(fl >> c & 1)) {
-        un[c] = ui[c] + P.dt * (vn[c] + fact * f[c]);
-      } else {
-        double du, dv;
-        bc_dof(D, T, ref, c, A.t_next, du, dv);
+        bc_df(D, T, ref, c, A.t_next, du, dv);
         un[c] = du;
       }
     }
-    vn[2] = DIM == 3 ? vn[2] : 0.;
-    st_node<DIM>(D.v[0], i, vn);
+    st_pair<DIM>(D.v32[0], i, vn);
   } else {
-    const double fact = P.dt * P.dt / P.rho;
-    double v[3], vn[3] = {0., 0., 0.};
-    ld_node<DIM>(D.v[A.cur], i, v);
+    float vh_[3], vl_[3];
+    ld_pair<DIM>(D.v32[A.cur], i, vh_, vl_);
+#pragma unroll
     for (int c = 0; c < DIM; c++) {
       if (!(fl >> c & 1)) {
-        un[c] = ui[c] + (fact * f[c] + P.dt * v[c]);
-        vn[c] = (un[c] - ui[c]) / P.dt;
+        const df u{uih[c], uil[c]};
+        const df inc = df_add(df_cmul(Q.c_hi, Q.c_lo, f[c]),
+                              df_mul_c({vh_[c], vl_[c]}, Q.dt_hi, Q.dt_lo));
+        un[c] = df_add(u, inc);
+        vn[c] = df_mul_c(df_sub(un[c], u), Q.idt_hi, Q.idt_lo);
       } else {
-        double du, dv;
-        bc_dof(D, T, ref, c, A.t_next, du, dv);
-        un[c] = du;
-        vn[c] = dv;
+        bc_df(D, T, ref, c, A.t_next, un[c], vn[c]);
       }
     }
-    st_node<DIM>(D.v[1 - A.cur], i, vn);
+    st_pair<DIM>(D.v32[1 - A.cur], i, vn);
   }
-  st_f32<DIM>(D.f32, i, fs_);
-  st_split<DIM>(D.u32[1 - A.cur], i, un);
+  if (DIM == 2)
+    reinterpret_cast<float2 *>(D.f32)[i] = make_float2(f[0], f[1]);
+  else
+    reinterpret_cast<float4 *>(D.f32)[i] = make_float4(f[0], f[1], f[2], 0.f);
+  st_pair<DIM>(D.u32[1 - A.cur], i, un);
 }
 
-// Thread-per-node, sliced-ELL bond store.
-template <int DIM, int SCHEME, bool FIRST>
-__global__ void __launch_bounds__(128)
+// Thread-per-node, sliced-ELL bond store.  NW1: every row fits one bit word.
+template <int DIM, int SCHEME, bool FIRST, bool NW1>
+__global__ void __launch_bounds__(128, DIM == 2 ? 12 : 8)
     k_rnp32_thread(const StepParams P, const Params32 Q, const DevPtrs D, const BCTable T,
                    const StepArgs A) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= P.n) return;
   const float4 *ucur = D.u32[A.cur];
-  float xih[3], xil[3], uih[3], uil[3];
-  ld_hl<DIM>(D.pos32, i, xih, xil);
-  ld_hl<DIM>(ucur, i, uih, uil);
+  Node32<DIM> ni;
+  ld_pos<DIM>(D, i, ni);
+  float uih[3], uil[3];
+  ld_pair<DIM>(ucur, i, uih, uil);
   const uint8_t fl = D.flags[i];
   const bool brk_i = !(fl & FLAG_NOFAIL);
-  const int64_t slice = i >> 5;
-  const int64_t base = D.sell_ptr[slice] + (i & 31);
-  const int w = D.sell_w[slice];
+  const int len = D.rowlen[i];
+  const int *colp = D.sell_cols + D.sell_ptr[i >> 5] + (i & 31);
   float fi[3] = {0.f, 0.f, 0.f};
-  uint32_t word = 0;
-  bool dirty = false;
-  int chunk = 0;
-  for (int k = 0; k < w; k++) {
-    if ((k & 31) == 0) {
-      if (dirty) D.bits[(int64_t)chunk * P.npad + i] = word;
-      chunk = k >> 5;
-      word = D.bits[(int64_t)chunk * P.npad + i];
-      dirty = false;
+  uint32_t word = NW1 ? D.bits[i] : 0u;
+  uint32_t nw = 0;  // newly broken bits of the current word
+  for (int k = 0; k < len; k++) {
+    if (!NW1 && (k & 31) == 0) {
+      if (nw) D.bits[(int64_t)((k >> 5) - 1) * P.npad + i] = word | nw;
+      word = D.bits[(int64_t)(k >> 5) * P.npad + i];
+      nw = 0;
     }
-    const int j = __ldg(D.sell_cols + base + (int64_t)k * 32);
-    if (j < 0) break;
-    float xjh[3], xjl[3], ujh[3], ujl[3], dv[3];
-    ld_hl<DIM>(D.pos32, j, xjh, xjl);
-    ld_hl<DIM>(ucur, j, ujh, ujl);
+    const int j = __ldg(colp + 32 * k);
+    Node32<DIM> nj;
+    ld_pos<DIM>(D, j, nj);
+    float ujh[3], ujl[3], dv[3];
+    ld_pair<DIM>(ucur, j, ujh, ujl);
     bool fs = (word >> (k & 31)) & 1u;
     const bool was = fs;
     bool breakable = brk_i;
     if (P.nofail && breakable) breakable = !(D.flags[j] & FLAG_NOFAIL);
-    const float s = rnp_bond32<DIM>(Q, xih, xil, uih, uil, xjh, xjl, ujh, ujl,
-                                    __ldg(D.vol32 + j), breakable, P.irrev, fs, dv);
-    if (fs != was) {
-      word |= 1u << (k & 31);
-      dirty = true;
-    }
-    fi[0] += s * dv[0];
-    fi[1] += s * dv[1];
-    if (DIM == 3) fi[2] += s * dv[2];
+    const float s = rnp_bond32<DIM>(Q, ni, uih, uil, nj, ujh, ujl, breakable, P.irrev, fs, dv);
+    if (fs != was) nw |= 1u << (k & 31);
+    fi[0] = fmaf(s, dv[0], fi[0]);
+    fi[1] = fmaf(s, dv[1], fi[1]);
+    if (DIM == 3) fi[2] = fmaf(s, dv[2], fi[2]);
   }
-  if (dirty) D.bits[(int64_t)chunk * P.npad + i] = word;
-  integrate_node32<DIM, SCHEME, FIRST>(P, D, T, A, i, fl, uih, uil, fi);
+  if (nw) D.bits[NW1 ? i : (int64_t)((len - 1) >> 5) * P.npad + i] = word | nw;
+  integrate_node32<DIM, SCHEME, FIRST>(P, Q, D, T, A, i, fl, uih, uil, fi);
 }
 
 // Warp-per-node over CSR rows; lane k of the warp owns bonds k, k+32, ...
@@ -224,13 +354,14 @@ __global__ void __launch_bounds__(256)
   const int lane = threadIdx.x & 31;
   if (i >= P.n) return;
   const float4 *ucur = D.u32[A.cur];
-  float xih[3], xil[3], uih[3], uil[3];
-  ld_hl<DIM>(D.pos32, i, xih, xil);
-  ld_hl<DIM>(ucur, i, uih, uil);
+  Node32<DIM> ni;
+  ld_pos<DIM>(D, i, ni);
+  float uih[3], uil[3];
+  ld_pair<DIM>(ucur, i, uih, uil);
   const uint8_t fl = D.flags[i];
   const bool brk_i = !(fl & FLAG_NOFAIL);
   const int64_t r0 = D.rowptr[i];
-  const int len = (int)(D.rowptr[i + 1] - r0);
+  const int len = D.rowlen[i];
   float fi[3] = {0.f, 0.f, 0.f};
   for (int b = 0; b < len; b += 32) {
     const int k = b + lane;
@@ -238,19 +369,19 @@ __global__ void __launch_bounds__(256)
     bool newly = false;
     if (k < len) {
       const int j = __ldg(D.cols + r0 + k);
-      float xjh[3], xjl[3], ujh[3], ujl[3], dv[3];
-      ld_hl<DIM>(D.pos32, j, xjh, xjl);
-      ld_hl<DIM>(ucur, j, ujh, ujl);
+      Node32<DIM> nj;
+      ld_pos<DIM>(D, j, nj);
+      float ujh[3], ujl[3], dv[3];
+      ld_pair<DIM>(ucur, j, ujh, ujl);
       bool fs = (word >> lane) & 1u;
       const bool was = fs;
       bool breakable = brk_i;
       if (P.nofail && breakable) breakable = !(D.flags[j] & FLAG_NOFAIL);
-      const float s = rnp_bond32<DIM>(Q, xih, xil, uih, uil, xjh, xjl, ujh, ujl,
-                                      __ldg(D.vol32 + j), breakable, P.irrev, fs, dv);
+      const float s = rnp_bond32<DIM>(Q, ni, uih, uil, nj, ujh, ujl, breakable, P.irrev, fs, dv);
       newly = fs != was;
-      fi[0] += s * dv[0];
-      fi[1] += s * dv[1];
-      if (DIM == 3) fi[2] += s * dv[2];
+      fi[0] = fmaf(s, dv[0], fi[0]);
+      fi[1] = fmaf(s, dv[1], fi[1]);
+      if (DIM == 3) fi[2] = fmaf(s, dv[2], fi[2]);
     }
     const uint32_t nb = __ballot_sync(0xffffffffu, newly);
     if (nb && lane == 0) D.bits[(int64_t)(b >> 5) * P.npad + i] = word | nb;
@@ -260,7 +391,18 @@ __global__ void __launch_bounds__(256)
     fi[1] += __shfl_xor_sync(0xffffffffu, fi[1], o);
     if (DIM == 3) fi[2] += __shfl_xor_sync(0xffffffffu, fi[2], o);
   }
-  if (lane == 0) integrate_node32<DIM, SCHEME, FIRST>(P, D, T, A, i, fl, uih, uil, fi);
+  if (lane == 0) integrate_node32<DIM, SCHEME, FIRST>(P, Q, D, T, A, i, fl, uih, uil, fi);
+}
+
+template <int DIM, int SCHEME, bool FIRST>
+static void launch_thread(const StepParams &P, const Params32 &Q, const DevPtrs &D,
+                          const BCTable &T, const StepArgs &a, cudaStream_t s) {
+  const int bs = 128;
+  const unsigned grid = (unsigned)((P.n + bs - 1) / bs);
+  if (P.nw1)
+    k_rnp32_thread<DIM, SCHEME, FIRST, true><<<grid, bs, 0, s>>>(P, Q, D, T, a);
+  else
+    k_rnp32_thread<DIM, SCHEME, FIRST, false><<<grid, bs, 0, s>>>(P, Q, D, T, a);
 }
 
 template <int DIM, int SCHEME>
@@ -276,12 +418,10 @@ static cudaError_t launch32(const StepParams &P, const DevPtrs &D, const BCTable
     else
       k_rnp32_warp<DIM, SCHEME, false><<<grid, bs, 0, s>>>(P, Q, D, T, a);
   } else {
-    const int bs = 128;
-    const unsigned grid = (unsigned)((P.n + bs - 1) / bs);
     if (a.first)
-      k_rnp32_thread<DIM, SCHEME, true><<<grid, bs, 0, s>>>(P, Q, D, T, a);
+      launch_thread<DIM, SCHEME, true>(P, Q, D, T, a, s);
     else
-      k_rnp32_thread<DIM, SCHEME, false><<<grid, bs, 0, s>>>(P, Q, D, T, a);
+      launch_thread<DIM, SCHEME, false>(P, Q, D, T, a, s);
   }
   return cudaGetLastError();
 }
@@ -293,6 +433,51 @@ cudaError_t launch_rnp_step_fp32(const StepParams &P, const DevPtrs &D, const BC
                                            : launch32<2, NLM_CENTRAL_DIFFERENCE>(P, D, T, a, decomp, s);
   return P.scheme == NLM_VELOCITY_VERLET ? launch32<3, NLM_VELOCITY_VERLET>(P, D, T, a, decomp, s)
                                          : launch32<3, NLM_CENTRAL_DIFFERENCE>(P, D, T, a, decomp, s);
+}
+
+// Drift after a host state upload: the second half of integrate_node32.
+template <int DIM>
+__global__ void k_drift32(const StepParams P, const Params32 Q, const DevPtrs D,
+                          const BCTable T, int cur, double t_next) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const uint8_t fl = D.flags[i];
+  const int ref = (fl & 7) ? D.bcref[i] : -1;
+  float uh[3], ul[3], vh[3], vl[3], f[3] = {0.f, 0.f, 0.f};
+  ld_pair<DIM>(D.u32[cur], i, uh, ul);
+  ld_pair<DIM>(D.v32[P.scheme == NLM_CENTRAL_DIFFERENCE ? cur : 0], i, vh, vl);
+  for (int c = 0; c < DIM; c++) f[c] = D.f32[(int64_t)(DIM == 2 ? 2 : 4) * i + c];
+  df un[3], vn[3];
+  for (int c = 0; c < DIM; c++) {
+    if (!(fl >> c & 1)) {
+      const df u{uh[c], ul[c]}, v{vh[c], vl[c]};
+      if (P.scheme == NLM_VELOCITY_VERLET) {
+        const df vh2 = df_add(v, df_cmul(Q.c_hi, Q.c_lo, f[c]));
+        un[c] = df_add(u, df_mul_c(vh2, Q.dt_hi, Q.dt_lo));
+        vn[c] = v;
+      } else {
+        const df inc = df_add(df_cmul(Q.c_hi, Q.c_lo, f[c]), df_mul_c(v, Q.dt_hi, Q.dt_lo));
+        un[c] = df_add(u, inc);
+        vn[c] = df_mul_c(df_sub(un[c], u), Q.idt_hi, Q.idt_lo);
+      }
+    } else {
+      bc_df(D, T, ref, c, t_next, un[c], vn[c]);
+    }
+  }
+  st_pair<DIM>(D.u32[1 - cur], i, un);
+  if (P.scheme == NLM_CENTRAL_DIFFERENCE) st_pair<DIM>(D.v32[1 - cur], i, vn);
+}
+
+cudaError_t launch_drift32(const StepParams &P, const DevPtrs &D, const BCTable &T, int cur,
+                           double t_next, cudaStream_t s) {
+  if (P.n == 0) return cudaSuccess;
+  const Params32 Q = make_p32(P);
+  const unsigned g = (unsigned)((P.n + 255) / 256);
+  if (P.dim == 2)
+    k_drift32<2><<<g, 256, 0, s>>>(P, Q, D, T, cur, t_next);
+  else
+    k_drift32<3><<<g, 256, 0, s>>>(P, Q, D, T, cur, t_next);
+  return cudaGetLastError();
 }
 
 }  // namespace nlm

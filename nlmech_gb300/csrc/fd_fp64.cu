@@ -215,53 +215,15 @@ __global__ void k_drift64(const StepParams P, const DevPtrs D, const BCTable T, 
   if (P.scheme == NLM_CENTRAL_DIFFERENCE) st_node<DIM>(D.v[1 - cur], i, vn);
 }
 
-template <int DIM>
-__global__ void k_drift32(const StepParams P, const DevPtrs D, const BCTable T, int cur,
-                          double t_next) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= P.n) return;
-  const uint8_t fl = D.flags[i];
-  const int ref = (fl & 7) ? D.bcref[i] : -1;
-  double ui[3], v[3], f[3], un[3] = {0., 0., 0.}, vn[3] = {0., 0., 0.};
-  ld_split<DIM>(D.u32[cur], i, ui);
-  ld_node<DIM>(D.v[P.scheme == NLM_CENTRAL_DIFFERENCE ? cur : 0], i, v);
-  ld_f32<DIM>(D.f32, i, f);
-  for (int d = 0; d < DIM; d++) {
-    if (!(fl >> d & 1)) {
-      if (P.scheme == NLM_VELOCITY_VERLET) {
-        const double fact = 0.5 * P.dt / P.rho;
-        un[d] = ui[d] + P.dt * (v[d] + fact * f[d]);
-      } else {
-        const double fact = P.dt * P.dt / P.rho;
-        un[d] = ui[d] + (fact * f[d] + P.dt * v[d]);
-        vn[d] = (un[d] - ui[d]) / P.dt;
-      }
-    } else {
-      double du, dv;
-      bc_dof(D, T, ref, d, t_next, du, dv);
-      un[d] = du;
-      vn[d] = dv;
-    }
-  }
-  st_split<DIM>(D.u32[1 - cur], i, un);
-  if (P.scheme == NLM_CENTRAL_DIFFERENCE) st_node<DIM>(D.v[1 - cur], i, vn);
-}
-
 cudaError_t launch_drift(const StepParams &P, const DevPtrs &D, const BCTable &T, int cur,
                          double t_next, bool fp32, cudaStream_t s) {
   if (P.n == 0) return cudaSuccess;
+  if (fp32) return launch_drift32(P, D, T, cur, t_next, s);
   const unsigned g = (unsigned)((P.n + 255) / 256);
-  if (fp32) {
-    if (P.dim == 2)
-      k_drift32<2><<<g, 256, 0, s>>>(P, D, T, cur, t_next);
-    else
-      k_drift32<3><<<g, 256, 0, s>>>(P, D, T, cur, t_next);
-  } else {
-    if (P.dim == 2)
-      k_drift64<2><<<g, 256, 0, s>>>(P, D, T, cur, t_next);
-    else
-      k_drift64<3><<<g, 256, 0, s>>>(P, D, T, cur, t_next);
-  }
+  if (P.dim == 2)
+    k_drift64<2><<<g, 256, 0, s>>>(P, D, T, cur, t_next);
+  else
+    k_drift64<3><<<g, 256, 0, s>>>(P, D, T, cur, t_next);
   return cudaGetLastError();
 }
 

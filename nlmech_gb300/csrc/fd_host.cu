@@ -26,6 +26,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda_fp16.h>
+
 #include "fd_internal.h"
 #include "neighbor.h"
 #include "state_io.cuh"
@@ -149,9 +151,36 @@ __global__ void k_fbc_apply(int64_t nf, int S, const int *nodes, const int *iptr
   for (int d = 0; d < S && d < 3; d++) fext[S * i + d] = fe[d];
 }
 
+__device__ inline void ld_split_any(const float4 *p, int S, int64_t i, double o[3]) {
+  if (S == 2) {
+    const float4 a = p[i];
+    o[0] = (double)a.x + (double)a.z;
+    o[1] = (double)a.y + (double)a.w;
+    o[2] = 0.;
+  } else {
+    const float4 a = p[2 * i], b = p[2 * i + 1];
+    o[0] = (double)a.x + (double)b.x;
+    o[1] = (double)a.y + (double)b.y;
+    o[2] = (double)a.z + (double)b.z;
+  }
+}
+__device__ inline void st_split_any(float4 *p, int S, int64_t i, const double v[3]) {
+  float h[3], l[3];
+  for (int d = 0; d < 3; d++) {
+    h[d] = __double2float_rn(v[d]);
+    l[d] = __double2float_rn(v[d] - (double)h[d]);
+  }
+  if (S == 2)
+    p[i] = make_float4(h[0], h[1], l[0], l[1]);
+  else {
+    p[2 * i] = make_float4(h[0], h[1], h[2], 0.f);
+    p[2 * i + 1] = make_float4(l[0], l[1], l[2], 0.f);
+  }
+}
+
 __global__ void k_bc_apply(int64_t nb, int S, int dim, const int *nodes, const int *bcref,
                            const BCEntry *bce, const uint8_t *flags, BCTable T, double time,
-                           double *u64, float4 *u32, double *v) {
+                           double *u64, float4 *u32, double *v, float4 *v32) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= nb) return;
   const int64_t i = nodes[t];
@@ -160,20 +189,11 @@ __global__ void k_bc_apply(int64_t nb, int S, int dim, const int *nodes, const i
   double uo[3], vo[3];
   if (u64) {
     for (int d = 0; d < 3; d++) uo[d] = d < S ? u64[S * i + d] : 0.;
+    for (int d = 0; d < 3; d++) vo[d] = d < S ? v[S * i + d] : 0.;
   } else {
-    if (S == 2) {
-      const float4 a = u32[i];
-      uo[0] = (double)a.x + (double)a.z;
-      uo[1] = (double)a.y + (double)a.w;
-      uo[2] = 0.;
-    } else {
-      const float4 a = u32[2 * i], b = u32[2 * i + 1];
-      uo[0] = (double)a.x + (double)b.x;
-      uo[1] = (double)a.y + (double)b.y;
-      uo[2] = (double)a.z + (double)b.z;
-    }
+    ld_split_any(u32, S, i, uo);
+    ld_split_any(v32, S, i, vo);
   }
-  for (int d = 0; d < 3; d++) vo[d] = d < S ? v[S * i + d] : 0.;
   for (int d = 0; d < dim; d++)
     if ((fl >> d & 1) && e.set[d] >= 0) {
       double du, dv;
@@ -183,20 +203,11 @@ __global__ void k_bc_apply(int64_t nb, int S, int dim, const int *nodes, const i
     }
   if (u64) {
     for (int d = 0; d < S && d < 3; d++) u64[S * i + d] = uo[d];
+    for (int d = 0; d < S && d < 3; d++) v[S * i + d] = vo[d];
   } else {
-    float h[3], l[3];
-    for (int d = 0; d < 3; d++) {
-      h[d] = __double2float_rn(uo[d]);
-      l[d] = __double2float_rn(uo[d] - (double)h[d]);
-    }
-    if (S == 2)
-      u32[i] = make_float4(h[0], h[1], l[0], l[1]);
-    else {
-      u32[2 * i] = make_float4(h[0], h[1], h[2], 0.f);
-      u32[2 * i + 1] = make_float4(l[0], l[1], l[2], 0.f);
-    }
+    st_split_any(u32, S, i, uo);
+    st_split_any(v32, S, i, vo);
   }
-  for (int d = 0; d < S && d < 3; d++) v[S * i + d] = vo[d];
 }
 
 // AoS original order (3 doubles per node) <-> internal layouts.
@@ -260,20 +271,27 @@ __global__ void k_gather_f32(int64_t n, int S, const int *perm, const float *src
   double *p = dst + 3 * (int64_t)perm[i];
   for (int d = 0; d < 3; d++) p[d] = d < S ? (double)src[S * i + d] : 0.;
 }
-__global__ void k_make_pos32(int64_t n, int S, const double *pos, float4 *pos32) {
+// FP32C position store: hi = (float)x, lo = x - hi packed as half(lo * scale).
+__global__ void k_make_pos32(int64_t n, int S, const double *pos, const double *vol, double scale,
+                             float4 *pos32, uint2 *pos32lo) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  float h[3], l[3];
+  float h[3];
+  __half l[3];
   for (int d = 0; d < 3; d++) {
     const double v = d < S ? pos[S * i + d] : 0.;
     h[d] = __double2float_rn(v);
-    l[d] = __double2float_rn(v - (double)h[d]);
+    l[d] = __float2half_rn((float)((v - (double)h[d]) * scale));
   }
-  if (S == 2)
-    pos32[i] = make_float4(h[0], h[1], l[0], l[1]);
-  else {
-    pos32[2 * i] = make_float4(h[0], h[1], h[2], 0.f);
-    pos32[2 * i + 1] = make_float4(l[0], l[1], l[2], 0.f);
+  const __half2 lxy = __halves2half2(l[0], l[1]);
+  const __half2 lz = __halves2half2(l[2], __float2half_rn(0.f));
+  const float V = (float)vol[i];
+  if (S == 2) {
+    pos32[i] = make_float4(h[0], h[1], V, *reinterpret_cast<const float *>(&lxy));
+  } else {
+    pos32[i] = make_float4(h[0], h[1], h[2], V);
+    pos32lo[i] = make_uint2(*reinterpret_cast<const unsigned *>(&lxy),
+                            *reinterpret_cast<const unsigned *>(&lz));
   }
 }
 __global__ void k_count_bits(int64_t n, int nwords, int64_t npad, const uint32_t *bits,
@@ -328,6 +346,8 @@ struct nlm_fd {
   double acc_ms = 0.;
   int64_t launches = 0;
   double bytes_per_launch = 0.;
+
+  int vidx() const { return scheme == NLM_CENTRAL_DIFFERENCE ? cur : 0; }
 
   template <class Tp>
   cudaError_t alloc(Tp **p, size_t count) {
@@ -474,7 +494,7 @@ int apply_bc(nlm_fd *h, double t) {
   k_bc_apply<<<nblk(h->n_bc_nodes, 128), 128, 0, h->stream>>>(
       h->n_bc_nodes, h->S, h->dim, h->bc_nodes, h->D.bcref, h->D.bce, h->D.flags, h->T, t,
       fp32 ? nullptr : h->D.u64[h->cur], fp32 ? h->D.u32[h->cur] : nullptr,
-      h->D.v[h->scheme == NLM_CENTRAL_DIFFERENCE ? h->cur : 0]);
+      fp32 ? nullptr : h->D.v[h->vidx()], fp32 ? h->D.v32[h->vidx()] : nullptr);
   NLM_CUDA(cudaGetLastError());
   return NLM_OK;
 }
@@ -815,19 +835,32 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
   TRY(h->alloc(&vol64, n));
   TRY(cudaMemcpyAsync(vol64, volp.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
   D.vol64 = vol64;
-  if (h->precision == NLM_PREC_FP32C) {
-    std::vector<float> v32(n);
-    for (int64_t i = 0; i < n; i++) v32[i] = (float)volp[i];
-    float *vol32;
-    TRY(h->alloc(&vol32, n));
-    TRY(cudaMemcpyAsync(vol32, v32.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
+  {
+    // row lengths (the kernels loop k < len)
+    std::vector<uint16_t> rl(n);
+    for (int64_t i = 0; i < n; i++) rl[i] = (uint16_t)(h->rowptr[i + 1] - h->rowptr[i]);
+    uint16_t *drl;
+    TRY(h->alloc(&drl, n));
+    TRY(cudaMemcpyAsync(drl, rl.data(), sizeof(uint16_t) * n, cudaMemcpyHostToDevice, s));
     TRY(cudaStreamSynchronize(s));
-    D.vol32 = vol32;
+    D.rowlen = drl;
+  }
+  P.nw1 = P.nwords == 1 ? 1 : 0;
+  if (h->precision == NLM_PREC_FP32C) {
+    double xmax = 0.;
+    for (int64_t k = 0; k < 3 * n; k++) xmax = std::max(xmax, std::fabs(d->x[k]));
+    double X = 1.;
+    while (X < xmax) X *= 2.;
+    while (X * 0.5 >= xmax && X > 1e-30) X *= 0.5;
+    P.lo_scale = std::ldexp(1.0, 24) / X;
     float4 *pos32;
-    TRY(h->alloc(&pos32, (size_t)(S / 2) * n));
-    k_make_pos32<<<nblk(n, 256), 256, 0, s>>>(n, S, nb.pos, pos32);
+    uint2 *pos32lo = nullptr;
+    TRY(h->alloc(&pos32, (size_t)n));
+    if (S == 4) TRY(h->alloc(&pos32lo, (size_t)n));
+    k_make_pos32<<<nblk(n, 256), 256, 0, s>>>(n, S, nb.pos, vol64, P.lo_scale, pos32, pos32lo);
     TRY(cudaGetLastError());
     D.pos32 = pos32;
+    D.pos32lo = pos32lo;
   }
 
   // ---- state ----
@@ -843,8 +876,13 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
     TRY(h->alloc(&D.f32, (size_t)S * n));
     TRY(cudaMemsetAsync(D.f32, 0, sizeof(float) * S * n, s));
   }
-  TRY(h->alloc(&D.v[0], (size_t)S * n));
-  TRY(h->alloc(&D.v[1], (size_t)S * n));
+  if (h->precision == NLM_PREC_FP64) {
+    TRY(h->alloc(&D.v[0], (size_t)S * n));
+    TRY(h->alloc(&D.v[1], (size_t)S * n));
+  } else {
+    TRY(h->alloc(&D.v32[0], (size_t)(S / 2) * n));
+    TRY(h->alloc(&D.v32[1], (size_t)(S / 2) * n));
+  }
   TRY(h->alloc(&D.err, 1));
   TRY(cudaMemsetAsync(D.err, 0, sizeof(int), s));
   TRY(h->alloc(&h->counter, 1));
@@ -860,7 +898,12 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
       else
         TRY(cudaMemsetAsync(D.u32[0], 0, sizeof(float4) * (S / 2) * n, s));
     }
-    if (!d->v0) TRY(cudaMemsetAsync(D.v[0], 0, sizeof(double) * S * n, s));
+    if (!d->v0) {
+      if (h->precision == NLM_PREC_FP64)
+        TRY(cudaMemsetAsync(D.v[0], 0, sizeof(double) * S * n, s));
+      else
+        TRY(cudaMemsetAsync(D.v32[0], 0, sizeof(float4) * (S / 2) * n, s));
+    }
     TRY(cudaStreamSynchronize(s));
   }
   if (rc != NLM_OK) {
@@ -875,8 +918,8 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
       per_node = 8.0 * S /*x*/ + 8 /*V*/ + 1 /*flags*/ + 8.0 * S * 2 /*u r,w*/ +
                  8.0 * S * 2 /*v r,w*/ + 8.0 * S * 2 /*f r,w*/;
     else
-      per_node = 8.0 * S /*x split*/ + 4 /*V*/ + 1 + 8.0 * S * 2 /*u split r,w*/ +
-                 8.0 * S * 2 /*v r,w*/ + 4.0 * S * 2 /*f r,w*/;
+      per_node = (S == 2 ? 16.0 : 24.0) /*x split + V*/ + 1 /*flags*/ + 2 /*row length*/ +
+                 8.0 * S * 2 /*u pair r,w*/ + 8.0 * S * 2 /*v pair r,w*/ + 4.0 * S * 2 /*f r,w*/;
     if (h->material == NLM_MAT_ELASTIC_STATE) per_node += 8.0 * 2;  // theta, m
     h->bytes_per_launch = per_bond * (double)h->nnz + per_node * (double)n;
   }
@@ -943,8 +986,10 @@ int nlm_fd_get_state(nlm_fd *h, double *u, double *v, double *f) {
     NLM_CUDA(cudaStreamSynchronize(s));
   }
   if (v) {
-    const double *src = h->D.v[h->scheme == NLM_CENTRAL_DIFFERENCE ? h->cur : 0];
-    k_gather_vec<<<g, 256, 0, s>>>(n, h->S, P, src, h->stage);
+    if (fp32)
+      k_gather_split<<<g, 256, 0, s>>>(n, h->S, P, h->D.v32[h->vidx()], h->stage);
+    else
+      k_gather_vec<<<g, 256, 0, s>>>(n, h->S, P, h->D.v[h->vidx()], h->stage);
     NLM_CUDA(cudaGetLastError());
     NLM_CUDA(cudaMemcpyAsync(v, h->stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
     NLM_CUDA(cudaStreamSynchronize(s));
@@ -979,8 +1024,10 @@ int nlm_fd_set_state(nlm_fd *h, const double *u, const double *v) {
   }
   if (v) {
     NLM_CUDA(cudaMemcpyAsync(h->stage, v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
-    k_scatter_vec<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage,
-                                    h->D.v[h->scheme == NLM_CENTRAL_DIFFERENCE ? h->cur : 0]);
+    if (h->precision == NLM_PREC_FP32C)
+      k_scatter_split<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.v32[h->vidx()]);
+    else
+      k_scatter_vec<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.v[h->vidx()]);
     NLM_CUDA(cudaGetLastError());
   }
   NLM_CUDA(cudaStreamSynchronize(s));
@@ -1106,8 +1153,10 @@ int nlm_fd_step_host(nlm_fd *h, double *u, double *v, double *f, int64_t nsteps)
     k_scatter_vec<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.u64[h->cur]);
   NLM_CUDA(cudaGetLastError());
   NLM_CUDA(cudaMemcpyAsync(h->stage, v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
-  k_scatter_vec<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage,
-                                  h->D.v[h->scheme == NLM_CENTRAL_DIFFERENCE ? h->cur : 0]);
+  if (fp32)
+    k_scatter_split<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.v32[h->vidx()]);
+  else
+    k_scatter_vec<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.v[h->vidx()]);
   NLM_CUDA(cudaGetLastError());
   NLM_CUDA(cudaMemcpyAsync(h->stage, f, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
   if (fp32)

@@ -10,8 +10,10 @@ namespace nlm {
 struct DevPtrs {
   // geometry
   const double *pos64;  // FP64: S doubles per node (S = 2 in 2-D, 4 in 3-D)
-  const float4 *pos32;  // FP32C: 2-D one float4 (xh, yh, xl, yl) per node;
-                        //        3-D two float4 (xh, yh, zh, 0), (xl, yl, zl, 0)
+  const float4 *pos32;  // FP32C: float4 (xh, yh, V, lo) in 2-D, (xh, yh, zh, V) in 3-D:
+                        // hi = (float)x, V = nodal volume, lo = half2 of
+                        // (x - hi) * lo_scale (2-D: x, y packed in .w)
+  const uint2 *pos32lo; // FP32C 3-D: half2 (xl, yl), half2 (zl, 0) scaled by lo_scale
   const double *vol64;
   const float *vol32;
   const uint8_t *flags;
@@ -24,11 +26,13 @@ struct DevPtrs {
   const int *sell_cols;     // slice-major, column-major inside a slice; -1 pads
   const int64_t *rowptr;    // CSR (n+1)
   const int *cols;          // CSR entries, rows ascending in original id
+  const uint16_t *rowlen;   // row lengths
   uint32_t *bits;           // word-major bond bits: bits[w * npad + i]
   // state (ping-pong where a step reads the old and writes the new value)
   double *u64[2];  // FP64 displacement, S per node
   float4 *u32[2];  // FP32C displacement split, same shape as pos32
-  double *v[2];    // velocity S per node (Verlet uses v[0]; CD ping-pongs)
+  double *v[2];    // FP64 velocity S per node (Verlet uses v[0]; CD ping-pongs)
+  float4 *v32[2];  // FP32C velocity as a (hi, lo) FP32 pair, shape of u32
   double *f64;     // FP64 force density, S per node
   float *f32;      // FP32C force density, S per node
   // ElasticState
@@ -61,6 +65,8 @@ cudaError_t launch_es_step_fp32(const StepParams &P, const DevPtrs &D, const BCT
 // after the host replaced the state: the second half of the step epilogue.
 cudaError_t launch_drift(const StepParams &P, const DevPtrs &D, const BCTable &T, int cur,
                          double t_next, bool fp32, cudaStream_t s);
+cudaError_t launch_drift32(const StepParams &P, const DevPtrs &D, const BCTable &T, int cur,
+                           double t_next, cudaStream_t s);
 cudaError_t launch_damage(const StepParams &P, const DevPtrs &D, int cur, bool fp32,
                           bool es, float *phi, float *Z, cudaStream_t s);
 

@@ -44,6 +44,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-steps", type=int, default=30)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--decomp", default="auto", choices=["auto", "thread", "thread1", "warp"])
     ap.add_argument("--quick", action="store_true",
                     help="FP32C timed run only (profiling driver)")
     return ap.parse_args()
@@ -212,8 +213,12 @@ def run_ours(a):
         return float(t.item())
 
     # ---- FP32-compensated (headline) ----
-    m = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_THREAD)
+    dmap = {"auto": abi.DECOMP_AUTO, "thread": abi.DECOMP_THREAD,
+            "thread1": abi.DECOMP_THREAD1, "warp": abi.DECOMP_WARP}
+    m = gpu.FDModel(p, precision=abi.FP32C, decomposition=dmap[a.decomp])
     nnz = m.nnz()
+    decomp = {1: "thread-per-node, 4-bond groups", 2: "warp-per-node",
+              3: "thread-per-node, 1 bond/iteration"}[m.decomposition()]
     m.run(a.warmup)
     barrier_sync()
     with ClockSampler(local) as cs:
@@ -248,7 +253,7 @@ def run_ours(a):
     m64.close()
 
     # ---- end to end through the host-resident drop-in call ----
-    me = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_THREAD)
+    me = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_AUTO)
     bufs = [torch.zeros((n, 3), dtype=torch.float64).pin_memory() for _ in range(3)]
     ptrs = [b.data_ptr() for b in bufs]
     me.step_host_ptr(*ptrs, nsteps=1)  # step 0 + first step (untimed)
@@ -279,7 +284,7 @@ def run_ours(a):
         "data": "synthetic (seeded jittered plate)",
         "config": {"workload": "rnp2d_plate_%dx%d_d3h_verlet" % (a.nx, a.nx), "nodes": n,
                    "bonds": nnz, "horizon": "3h", "dt": p.dt, "precision": "fp32c",
-                   "decomposition": "thread-per-node sliced-ELL",
+                   "decomposition": decomp + (" (autotuned)" if a.decomp == "auto" else ""),
                    "l2": "inputs larger than L2: %.0f MB moved per step vs 129 MB L2"
                          % (bytes_per_launch / 1e6),
                    "parallelism": "replicas" if world > 1 else "single GPU"},

@@ -64,9 +64,11 @@ enum nlm_scheme {
 };
 
 enum nlm_decomposition {
-  NLM_DECOMP_AUTO = 0,   /* pick by the autotuner                        */
-  NLM_DECOMP_THREAD = 1, /* one thread per node, sliced-ELL bond storage  */
-  NLM_DECOMP_WARP = 2    /* one warp per node, CSR bond storage           */
+  NLM_DECOMP_AUTO = 0,    /* pick by timing the candidates on the model    */
+  NLM_DECOMP_THREAD = 1,  /* one thread per node, sliced-ELL bonds taken
+                             four at a time                                */
+  NLM_DECOMP_WARP = 2,    /* one warp per node, CSR bond storage           */
+  NLM_DECOMP_THREAD1 = 3  /* one thread per node, one bond per iteration   */
 };
 
 /* Displacement_BC / Force_BC region types (loading/uLoading.cpp:38-46). */

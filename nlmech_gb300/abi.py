@@ -28,6 +28,7 @@ CENTRAL_DIFFERENCE = 1
 DECOMP_AUTO = 0
 DECOMP_THREAD = 1
 DECOMP_WARP = 2
+DECOMP_THREAD1 = 3
 # regions
 REGION = {"rectangle": 0, "line": 1, "circle": 2, "torus": 3, "cuboid": 4}
 TIME_FN = {"constant": 0, "linear": 1, "quadratic": 2, "sin": 3,

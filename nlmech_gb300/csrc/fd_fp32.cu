@@ -302,8 +302,12 @@ __device__ __forceinline__ void integrate_node32(const StepParams &P, const Para
 }
 
 // Thread-per-node, sliced-ELL bond store.  NW1: every row fits one bit word.
+// Bonds are taken four at a time: one 16-byte load brings the four neighbour
+// ids (the next group's ids are fetched while the current group is gathered
+// and evaluated), then the eight node gathers of the group are issued
+// together, so each thread keeps several independent loads in flight.
 template <int DIM, int SCHEME, bool FIRST, bool NW1>
-__global__ void __launch_bounds__(128, DIM == 2 ? 12 : 8)
+__global__ void __launch_bounds__(128, DIM == 2 ? 7 : 5)
     k_rnp32_thread(const StepParams P, const Params32 Q, const DevPtrs D, const BCTable T,
                    const StepArgs A) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -316,17 +320,77 @@ __global__ void __launch_bounds__(128, DIM == 2 ? 12 : 8)
   const uint8_t fl = D.flags[i];
   const bool brk_i = !(fl & FLAG_NOFAIL);
   const int len = D.rowlen[i];
-  const int *colp = D.sell_cols + D.sell_ptr[i >> 5] + (i & 31);
+  const int ng = (len + 3) >> 2;
+  const int4 *cp = reinterpret_cast<const int4 *>(D.sell_cols + D.sell_ptr[i >> 5]) + (i & 31);
   float fi[3] = {0.f, 0.f, 0.f};
   uint32_t word = NW1 ? D.bits[i] : 0u;
   uint32_t nw = 0;  // newly broken bits of the current word
+  int4 nxt = ng > 0 ? __ldg(cp) : make_int4(-1, -1, -1, -1);
+  for (int g = 0; g < ng; g++) {
+    const int4 cur = nxt;
+    if (g + 1 < ng) nxt = __ldg(cp + 32 * (g + 1));
+    if (!NW1 && (g & 7) == 0) {
+      if (nw) D.bits[(int64_t)((g >> 3) - 1) * P.npad + i] = word | nw;
+      word = D.bits[(int64_t)(g >> 3) * P.npad + i];
+      nw = 0;
+    }
+    const int jj[4] = {cur.x, cur.y, cur.z, cur.w};
+    Node32<DIM> nj[4];
+    float ujh[4][3], ujl[4][3];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      if (jj[q] >= 0) {
+        ld_pos<DIM>(D, jj[q], nj[q]);
+        ld_pair<DIM>(ucur, jj[q], ujh[q], ujl[q]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      if (jj[q] < 0) continue;
+      const int k = 4 * g + q;
+      float dv[3];
+      bool fs = (word >> (k & 31)) & 1u;
+      const bool was = fs;
+      bool breakable = brk_i;
+      if (P.nofail && breakable) breakable = !(D.flags[jj[q]] & FLAG_NOFAIL);
+      const float s =
+          rnp_bond32<DIM>(Q, ni, uih, uil, nj[q], ujh[q], ujl[q], breakable, P.irrev, fs, dv);
+      if (fs != was) nw |= 1u << (k & 31);
+      fi[0] = fmaf(s, dv[0], fi[0]);
+      fi[1] = fmaf(s, dv[1], fi[1]);
+      if (DIM == 3) fi[2] = fmaf(s, dv[2], fi[2]);
+    }
+  }
+  if (nw) D.bits[NW1 ? i : (int64_t)((len - 1) >> 5) * P.npad + i] = word | nw;
+  integrate_node32<DIM, SCHEME, FIRST>(P, Q, D, T, A, i, fl, uih, uil, fi);
+}
+
+// Same decomposition without the four-wide grouping (one bond per iteration).
+template <int DIM, int SCHEME, bool FIRST, bool NW1>
+__global__ void __launch_bounds__(128, DIM == 2 ? 12 : 8)
+    k_rnp32_thread1(const StepParams P, const Params32 Q, const DevPtrs D, const BCTable T,
+                    const StepArgs A) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const float4 *ucur = D.u32[A.cur];
+  Node32<DIM> ni;
+  ld_pos<DIM>(D, i, ni);
+  float uih[3], uil[3];
+  ld_pair<DIM>(ucur, i, uih, uil);
+  const uint8_t fl = D.flags[i];
+  const bool brk_i = !(fl & FLAG_NOFAIL);
+  const int len = D.rowlen[i];
+  const int *colp = D.sell_cols + D.sell_ptr[i >> 5] + 4 * (i & 31);
+  float fi[3] = {0.f, 0.f, 0.f};
+  uint32_t word = NW1 ? D.bits[i] : 0u;
+  uint32_t nw = 0;
   for (int k = 0; k < len; k++) {
     if (!NW1 && (k & 31) == 0) {
       if (nw) D.bits[(int64_t)((k >> 5) - 1) * P.npad + i] = word | nw;
       word = D.bits[(int64_t)(k >> 5) * P.npad + i];
       nw = 0;
     }
-    const int j = __ldg(colp + 32 * k);
+    const int j = __ldg(colp + (k >> 2) * 128 + (k & 3));
     Node32<DIM> nj;
     ld_pos<DIM>(D, j, nj);
     float ujh[3], ujl[3], dv[3];
@@ -396,13 +460,20 @@ __global__ void __launch_bounds__(256)
 
 template <int DIM, int SCHEME, bool FIRST>
 static void launch_thread(const StepParams &P, const Params32 &Q, const DevPtrs &D,
-                          const BCTable &T, const StepArgs &a, cudaStream_t s) {
+                          const BCTable &T, const StepArgs &a, int decomp, cudaStream_t s) {
   const int bs = 128;
   const unsigned grid = (unsigned)((P.n + bs - 1) / bs);
-  if (P.nw1)
-    k_rnp32_thread<DIM, SCHEME, FIRST, true><<<grid, bs, 0, s>>>(P, Q, D, T, a);
-  else
-    k_rnp32_thread<DIM, SCHEME, FIRST, false><<<grid, bs, 0, s>>>(P, Q, D, T, a);
+  if (decomp == NLM_DECOMP_THREAD1) {
+    if (P.nw1)
+      k_rnp32_thread1<DIM, SCHEME, FIRST, true><<<grid, bs, 0, s>>>(P, Q, D, T, a);
+    else
+      k_rnp32_thread1<DIM, SCHEME, FIRST, false><<<grid, bs, 0, s>>>(P, Q, D, T, a);
+  } else {
+    if (P.nw1)
+      k_rnp32_thread<DIM, SCHEME, FIRST, true><<<grid, bs, 0, s>>>(P, Q, D, T, a);
+    else
+      k_rnp32_thread<DIM, SCHEME, FIRST, false><<<grid, bs, 0, s>>>(P, Q, D, T, a);
+  }
 }
 
 template <int DIM, int SCHEME>
@@ -419,9 +490,9 @@ static cudaError_t launch32(const StepParams &P, const DevPtrs &D, const BCTable
       k_rnp32_warp<DIM, SCHEME, false><<<grid, bs, 0, s>>>(P, Q, D, T, a);
   } else {
     if (a.first)
-      launch_thread<DIM, SCHEME, true>(P, Q, D, T, a, s);
+      launch_thread<DIM, SCHEME, true>(P, Q, D, T, a, decomp, s);
     else
-      launch_thread<DIM, SCHEME, false>(P, Q, D, T, a, s);
+      launch_thread<DIM, SCHEME, false>(P, Q, D, T, a, decomp, s);
   }
   return cudaGetLastError();
 }

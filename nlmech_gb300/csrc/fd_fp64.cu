@@ -52,22 +52,20 @@ __global__ void __launch_bounds__(128)
   ld_node<DIM>(ucur, i, ui);
   const uint8_t fl = D.flags[i];
   const bool brk_i = !(fl & FLAG_NOFAIL);
-  const int64_t slice = i >> 5;
-  const int64_t base = D.sell_ptr[slice] + (i & 31);
-  const int w = D.sell_w[slice];
+  const int *colp = D.sell_cols + D.sell_ptr[i >> 5] + 4 * (i & 31);
+  const int len = D.rowlen[i];
   double fi[3] = {0., 0., 0.};
   uint32_t word = 0;
   bool dirty = false;
   int chunk = 0;
-  for (int k = 0; k < w; k++) {
+  for (int k = 0; k < len; k++) {
     if ((k & 31) == 0) {
       if (dirty) D.bits[(int64_t)chunk * P.npad + i] = word;
       chunk = k >> 5;
       word = D.bits[(int64_t)chunk * P.npad + i];
       dirty = false;
     }
-    const int j = __ldg(D.sell_cols + base + (int64_t)k * 32);
-    if (j < 0) break;
+    const int j = __ldg(colp + (k >> 2) * 128 + (k & 3));
     double xj[3], uj[3], e[3];
     ld_node<DIM>(D.pos64, j, xj);
     ld_node<DIM>(ucur, j, uj);

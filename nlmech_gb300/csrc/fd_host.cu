@@ -479,6 +479,64 @@ int launch_step(nlm_fd *h, const StepArgs &a) {
   return NLM_OK;
 }
 
+// Work-decomposition autotuner: time each candidate step kernel on scratch
+// copies of the arrays a step writes and keep the fastest.
+int autotune(nlm_fd *h) {
+  const int S = h->S;
+  const int64_t n = h->n;
+  cudaStream_t s = h->stream;
+  DevPtrs D = h->D;
+  float4 *sv0 = nullptr, *sv1 = nullptr;
+  float *sf = nullptr;
+  uint32_t *sb = nullptr;
+  const size_t nb = (size_t)h->P.nwords * h->P.npad;
+  cudaError_t e = cudaMalloc(&sv0, sizeof(float4) * (S / 2) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&sv1, sizeof(float4) * (S / 2) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&sf, sizeof(float) * S * n);
+  if (e == cudaSuccess) e = cudaMalloc(&sb, sizeof(uint32_t) * nb);
+  auto cleanup = [&]() { cudaFree(sv0); cudaFree(sv1); cudaFree(sf); cudaFree(sb); };
+  if (e != cudaSuccess) {
+    cleanup();
+    return cuda_fail(e, "autotune scratch");
+  }
+  cudaMemcpyAsync(sv0, D.v32[0], sizeof(float4) * (S / 2) * n, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(sv1, D.v32[0], sizeof(float4) * (S / 2) * n, cudaMemcpyDeviceToDevice, s);
+  cudaMemsetAsync(sf, 0, sizeof(float) * S * n, s);
+  cudaMemcpyAsync(sb, D.bits, sizeof(uint32_t) * nb, cudaMemcpyDeviceToDevice, s);
+  D.v32[0] = sv0;
+  D.v32[1] = sv1;
+  D.f32 = sf;
+  D.bits = sb;
+  const int cands[3] = {NLM_DECOMP_THREAD, NLM_DECOMP_THREAD1, NLM_DECOMP_WARP};
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  float best = 1e30f;
+  int pick = NLM_DECOMP_THREAD;
+  const StepArgs sa{0, false, h->time, h->time + h->dt};
+  for (int c : cands) {
+    for (int w = 0; w < 2; w++) e = launch_rnp_step_fp32(h->P, D, h->T, sa, c, s);
+    cudaEventRecord(a, s);
+    for (int r = 0; r < 5; r++) e = launch_rnp_step_fp32(h->P, D, h->T, sa, c, s);
+    cudaEventRecord(b, s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    if (e != cudaSuccess) break;
+    if (ms < best) {
+      best = ms;
+      pick = c;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaStreamSynchronize(s);
+  cleanup();
+  if (e != cudaSuccess) return cuda_fail(e, "autotune");
+  h->decomp = pick;
+  return NLM_OK;
+}
+
 int apply_fbc(nlm_fd *h, double t) {
   if (h->n_fbc_nodes == 0) return NLM_OK;
   k_fbc_apply<<<nblk(h->n_fbc_nodes, 128), 128, 0, h->stream>>>(
@@ -660,8 +718,11 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
     P.irrev = 1;
   }
   h->decomp = d->decomposition == NLM_DECOMP_AUTO ? NLM_DECOMP_THREAD : d->decomposition;
-  if (h->decomp != NLM_DECOMP_THREAD && h->decomp != NLM_DECOMP_WARP)
+  if (h->decomp != NLM_DECOMP_THREAD && h->decomp != NLM_DECOMP_WARP &&
+      h->decomp != NLM_DECOMP_THREAD1)
     return bail(fail(NLM_ERR_INVALID, "unknown decomposition"));
+  const bool want_tune = d->decomposition == NLM_DECOMP_AUTO &&
+                         d->precision == NLM_PREC_FP32C;
 
   cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
@@ -907,6 +968,10 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
     TRY(cudaStreamSynchronize(s));
   }
   if (rc != NLM_OK) {
+    *out = nullptr;
+    return bail(rc);
+  }
+  if (want_tune && (rc = autotune(h))) {
     *out = nullptr;
     return bail(rc);
   }

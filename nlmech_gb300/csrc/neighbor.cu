@@ -137,6 +137,10 @@ __global__ void k_sell_width(int64_t n, const int64_t *rowptr, int *width) {
   atomicMax(width + (i >> 5), len);
 }
 
+// Sliced ELL, 32 rows per slice, entries interleaved in groups of four: entry
+// k of lane l sits at slice_base + (k/4)*128 + 4l + k%4, so a thread fetches
+// four neighbour ids with one 16-byte load and a warp's load is 512
+// contiguous bytes.  Slice widths are multiples of 4; pads are -1.
 __global__ void k_sell_fill(int64_t n, int64_t nslices, const int64_t *rowptr, const int *cols,
                             const int64_t *sell_ptr, const int *width, int *sell_cols) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -145,10 +149,11 @@ __global__ void k_sell_fill(int64_t n, int64_t nslices, const int64_t *rowptr, c
   const int lane = (int)(t & 31);
   const int64_t i = t;
   const int w = width[s];
-  const int64_t base = sell_ptr[s] + lane;
+  const int64_t base = sell_ptr[s] + 4 * lane;
   const int64_t r0 = i < n ? rowptr[i] : 0;
   const int len = i < n ? (int)(rowptr[i + 1] - r0) : 0;
-  for (int k = 0; k < w; k++) sell_cols[base + (int64_t)k * 32] = k < len ? cols[r0 + k] : -1;
+  for (int k = 0; k < w; k++)
+    sell_cols[base + (int64_t)(k >> 2) * 128 + (k & 3)] = k < len ? cols[r0 + k] : -1;
 }
 
 // Pre-crack bits (geometry::Fracture ctor, src/geometry/fracture.cpp:20-160;
@@ -345,9 +350,11 @@ cudaError_t build_sell(int64_t n, const int64_t *rowptr, const int *cols, SellSt
   std::vector<int64_t> ptr(st.nslices + 1, 0);
   st.maxw = 0;
   for (int64_t k = 0; k < st.nslices; k++) {
-    ptr[k + 1] = ptr[k] + 32 * (int64_t)w[k];
     st.maxw = w[k] > st.maxw ? w[k] : st.maxw;
+    w[k] = (w[k] + 3) & ~3;
+    ptr[k + 1] = ptr[k] + 32 * (int64_t)w[k];
   }
+  NB_CHECK(cudaMemcpyAsync(st.width, w.data(), sizeof(int) * st.nslices, cudaMemcpyHostToDevice, s));
   st.entries = ptr[st.nslices];
   NB_CHECK(cudaMalloc(&st.ptr, sizeof(int64_t) * (st.nslices + 1)));
   NB_CHECK(cudaMemcpyAsync(st.ptr, ptr.data(), sizeof(int64_t) * (st.nslices + 1),

@@ -177,7 +177,7 @@ def test_fp32c_config0_error(gpu, oracle):
     uo, vo, fo = o.state()
     rowptr, cols = o.neighbors()
     bo = bonds_as_pairs(rowptr, cols, o.bond_state())
-    for dec in (abi.DECOMP_THREAD, abi.DECOMP_WARP):
+    for dec in (abi.DECOMP_THREAD, abi.DECOMP_THREAD1, abi.DECOMP_WARP, abi.DECOMP_AUTO):
         m = gpu.FDModel(p, precision=abi.FP32C, decomposition=dec)
         m.run(1000)
         u, v, f = m.state()

@@ -32,6 +32,7 @@ struct Params32 {
   float Ksc;            // (f_sc rbar)^2 / (1 - 1e-5)^2: |S| > S_c  <=>  S^2 r > Ksc
   float nbl2e;          // -beta * log2(e)
   float inv_lo;         // 1 / lo_scale
+  int irrev;
   int infl_type;
   float a0, a1, alpha, ibeta;
   // integrator constants as (hi, lo) pairs
@@ -58,6 +59,7 @@ static Params32 make_p32(const StepParams &P) {
   q.Ksc = (float)(sc * sc);
   q.nbl2e = (float)(-P.beta * 1.4426950408889634);
   q.inv_lo = (float)(1.0 / P.lo_scale);
+  q.irrev = P.irrev;
   q.infl_type = P.infl_type;
   q.a0 = (float)P.infl_a0;
   q.a1 = (float)P.infl_a1;
@@ -172,19 +174,29 @@ __device__ __forceinline__ void st_pair(float4 *p, int64_t j, const df v[3]) {
   }
 }
 
-// Bond force of RNPBond in FP32 (rnpBond.cpp:242-300 with contact off).
-// Returns s with F = s * xi (the 1/|xi| of the direction is folded into s).
-template <int DIM>
+// Kernel specialisations.
+enum : int {
+  OPT_CONSTJ = 1,  // constant influence function (J folded into K1)
+  OPT_NOFAIL = 2   // some nodes are non-interior (per-bond flag test needed)
+};
+
+// Bond force of RNPBond in FP32 (rnpBond.cpp:242-300 with contact off),
+// without branches.  Returns s with F = s * xi (the 1/|xi| of the direction
+// is folded into s) and updates the bond state fs.  A padding entry is passed
+// as the node itself: xi = eta = 0 gives S = 0, s = 0 and no break.
+// The volume correction min(1, (delta + h/2 - r) / h) equals the reference's
+// "if r > delta - h/2" factor away from its 1e-5 relative comparison band.
+template <int DIM, int OPT>
 __device__ __forceinline__ float rnp_bond32(const Params32 &Q, const Node32<DIM> &ni,
                                             const float uih[3], const float uil[3],
                                             const Node32<DIM> &nj, const float ujh[3],
-                                            const float ujl[3], bool breakable, bool irrev,
-                                            bool &fs, float d[3]) {
+                                            const float ujl[3], bool breakable, bool &fs,
+                                            float d[3]) {
   const float2 dl = __half22float2(__hsub2(nj.lxy, ni.lxy));
   d[0] = fmaf(dl.x, Q.inv_lo, nj.xh[0] - ni.xh[0]);
   d[1] = fmaf(dl.y, Q.inv_lo, nj.xh[1] - ni.xh[1]);
-  float e0 = (ujh[0] - uih[0]) + (ujl[0] - uil[0]);
-  float e1 = (ujh[1] - uih[1]) + (ujl[1] - uil[1]);
+  const float e0 = (ujh[0] - uih[0]) + (ujl[0] - uil[0]);
+  const float e1 = (ujh[1] - uih[1]) + (ujl[1] - uil[1]);
   float r2 = d[0] * d[0] + d[1] * d[1];
   float de = d[0] * e0 + d[1] * e1;
   if (DIM == 3) {
@@ -194,24 +206,22 @@ __device__ __forceinline__ float rnp_bond32(const Params32 &Q, const Node32<DIM>
     r2 = fmaf(d[2], d[2], r2);
     de = fmaf(d[2], e2, de);
   }
+  r2 = fmaxf(r2, 1e-30f);
   const float rinv = rsqrt_approx(r2);
   const float r = r2 * rinv;
   const float S = de * (rinv * rinv);
-  float volj = nj.vol;
-  if (r > Q.check_low_eff) volj *= (Q.check_up - r) * Q.inv_h;
-  float k = Q.K1;
-  if (Q.infl_type == 1) {
-    k *= Q.a0 + Q.a1 * (r * Q.inv_delta);
-  } else if (Q.infl_type == 2) {
+  float k = Q.K1 * nj.vol * fminf(1.f, (Q.check_up - r) * Q.inv_h);
+  if (!(OPT & OPT_CONSTJ)) {
     const float rr = r * Q.inv_delta;
-    k *= Q.alpha * ex2_approx(-rr * rr * Q.ibeta * 1.4426950408889634f);
+    k *= Q.infl_type == 1 ? Q.a0 + Q.a1 * rr
+                          : Q.alpha * ex2_approx(-rr * rr * Q.ibeta * 1.4426950408889634f);
   }
-  const float s0 = k * S * volj * rinv;
-  if (!breakable) return s0;
+  const float s0 = k * S * rinv;
   const float bs2 = S * S * r;
-  if (irrev && !fs && bs2 > Q.Ksc) fs = true;
-  if (fs) return 0.f;
-  return s0 * ex2_approx(Q.nbl2e * bs2);
+  const bool brk = (OPT & OPT_NOFAIL) ? breakable : true;
+  fs = fs || (brk && Q.irrev && bs2 > Q.Ksc);
+  const float s1 = fs ? 0.f : s0 * ex2_approx(Q.nbl2e * bs2);
+  return brk ? s1 : s0;
 }
 
 // Prescribed (du, dv) of one dof as double-float pairs.
@@ -224,7 +234,7 @@ __device__ __forceinline__ void bc_df(const DevPtrs &D, const BCTable &T, int re
 }
 
 // FP32C integrator epilogue (same phase structure as integrate_node64).
-template <int DIM, int SCHEME, bool FIRST>
+template <int DIM, int SCHEME>
 __device__ __forceinline__ void integrate_node32(const StepParams &P, const Params32 &Q,
                                                  const DevPtrs &D, const BCTable &T,
                                                  const StepArgs &A, int64_t i, uint8_t fl,
@@ -241,6 +251,7 @@ __device__ __forceinline__ void integrate_node32(const StepParams &P, const Para
   if (SCHEME == NLM_VELOCITY_VERLET) {
     float vh_[3], vl_[3];
     ld_pair<DIM>(D.v32[0], i, vh_, vl_);
+    const bool FIRST = A.first;
     float fp[3] = {0.f, 0.f, 0.f};
     if (!FIRST) {
       if (DIM == 2) {
@@ -306,7 +317,7 @@ __device__ __forceinline__ void integrate_node32(const StepParams &P, const Para
 // ids (the next group's ids are fetched while the current group is gathered
 // and evaluated), then the eight node gathers of the group are issued
 // together, so each thread keeps several independent loads in flight.
-template <int DIM, int SCHEME, bool FIRST, bool NW1>
+template <int DIM, int SCHEME, bool NW1, int OPT>
 __global__ void __launch_bounds__(128, DIM == 2 ? 7 : 5)
     k_rnp32_thread(const StepParams P, const Params32 Q, const DevPtrs D, const BCTable T,
                    const StepArgs A) {
@@ -334,39 +345,38 @@ __global__ void __launch_bounds__(128, DIM == 2 ? 7 : 5)
       word = D.bits[(int64_t)(g >> 3) * P.npad + i];
       nw = 0;
     }
-    const int jj[4] = {cur.x, cur.y, cur.z, cur.w};
+    const int ii = (int)i;
+    const int jj[4] = {cur.x < 0 ? ii : cur.x, cur.y < 0 ? ii : cur.y, cur.z < 0 ? ii : cur.z,
+                       cur.w < 0 ? ii : cur.w};
     Node32<DIM> nj[4];
     float ujh[4][3], ujl[4][3];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-      if (jj[q] >= 0) {
-        ld_pos<DIM>(D, jj[q], nj[q]);
-        ld_pair<DIM>(ucur, jj[q], ujh[q], ujl[q]);
-      }
+      ld_pos<DIM>(D, jj[q], nj[q]);
+      ld_pair<DIM>(ucur, jj[q], ujh[q], ujl[q]);
     }
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-      if (jj[q] < 0) continue;
       const int k = 4 * g + q;
       float dv[3];
-      bool fs = (word >> (k & 31)) & 1u;
-      const bool was = fs;
-      bool breakable = brk_i;
-      if (P.nofail && breakable) breakable = !(D.flags[jj[q]] & FLAG_NOFAIL);
+      const bool was = (word >> (k & 31)) & 1u;
+      bool fs = was;
+      bool breakable = true;
+      if (OPT & OPT_NOFAIL) breakable = brk_i && !(D.flags[jj[q]] & FLAG_NOFAIL);
       const float s =
-          rnp_bond32<DIM>(Q, ni, uih, uil, nj[q], ujh[q], ujl[q], breakable, P.irrev, fs, dv);
-      if (fs != was) nw |= 1u << (k & 31);
+          rnp_bond32<DIM, OPT>(Q, ni, uih, uil, nj[q], ujh[q], ujl[q], breakable, fs, dv);
+      nw |= (uint32_t)(fs && !was) << (k & 31);
       fi[0] = fmaf(s, dv[0], fi[0]);
       fi[1] = fmaf(s, dv[1], fi[1]);
       if (DIM == 3) fi[2] = fmaf(s, dv[2], fi[2]);
     }
   }
   if (nw) D.bits[NW1 ? i : (int64_t)((len - 1) >> 5) * P.npad + i] = word | nw;
-  integrate_node32<DIM, SCHEME, FIRST>(P, Q, D, T, A, i, fl, uih, uil, fi);
+  integrate_node32<DIM, SCHEME>(P, Q, D, T, A, i, fl, uih, uil, fi);
 }
 
 // Same decomposition without the four-wide grouping (one bond per iteration).
-template <int DIM, int SCHEME, bool FIRST, bool NW1>
+template <int DIM, int SCHEME, bool NW1, int OPT>
 __global__ void __launch_bounds__(128, DIM == 2 ? 12 : 8)
     k_rnp32_thread1(const StepParams P, const Params32 Q, const DevPtrs D, const BCTable T,
                     const StepArgs A) {
@@ -395,22 +405,22 @@ __global__ void __launch_bounds__(128, DIM == 2 ? 12 : 8)
     ld_pos<DIM>(D, j, nj);
     float ujh[3], ujl[3], dv[3];
     ld_pair<DIM>(ucur, j, ujh, ujl);
-    bool fs = (word >> (k & 31)) & 1u;
-    const bool was = fs;
-    bool breakable = brk_i;
-    if (P.nofail && breakable) breakable = !(D.flags[j] & FLAG_NOFAIL);
-    const float s = rnp_bond32<DIM>(Q, ni, uih, uil, nj, ujh, ujl, breakable, P.irrev, fs, dv);
-    if (fs != was) nw |= 1u << (k & 31);
+    const bool was = (word >> (k & 31)) & 1u;
+    bool fs = was;
+    bool breakable = true;
+    if (OPT & OPT_NOFAIL) breakable = brk_i && !(D.flags[j] & FLAG_NOFAIL);
+    const float s = rnp_bond32<DIM, OPT>(Q, ni, uih, uil, nj, ujh, ujl, breakable, fs, dv);
+    nw |= (uint32_t)(fs && !was) << (k & 31);
     fi[0] = fmaf(s, dv[0], fi[0]);
     fi[1] = fmaf(s, dv[1], fi[1]);
     if (DIM == 3) fi[2] = fmaf(s, dv[2], fi[2]);
   }
   if (nw) D.bits[NW1 ? i : (int64_t)((len - 1) >> 5) * P.npad + i] = word | nw;
-  integrate_node32<DIM, SCHEME, FIRST>(P, Q, D, T, A, i, fl, uih, uil, fi);
+  integrate_node32<DIM, SCHEME>(P, Q, D, T, A, i, fl, uih, uil, fi);
 }
 
 // Warp-per-node over CSR rows; lane k of the warp owns bonds k, k+32, ...
-template <int DIM, int SCHEME, bool FIRST>
+template <int DIM, int SCHEME, int OPT>
 __global__ void __launch_bounds__(256)
     k_rnp32_warp(const StepParams P, const Params32 Q, const DevPtrs D, const BCTable T,
                  const StepArgs A) {
@@ -437,12 +447,12 @@ __global__ void __launch_bounds__(256)
       ld_pos<DIM>(D, j, nj);
       float ujh[3], ujl[3], dv[3];
       ld_pair<DIM>(ucur, j, ujh, ujl);
-      bool fs = (word >> lane) & 1u;
-      const bool was = fs;
-      bool breakable = brk_i;
-      if (P.nofail && breakable) breakable = !(D.flags[j] & FLAG_NOFAIL);
-      const float s = rnp_bond32<DIM>(Q, ni, uih, uil, nj, ujh, ujl, breakable, P.irrev, fs, dv);
-      newly = fs != was;
+      const bool was = (word >> lane) & 1u;
+      bool fs = was;
+      bool breakable = true;
+      if (OPT & OPT_NOFAIL) breakable = brk_i && !(D.flags[j] & FLAG_NOFAIL);
+      const float s = rnp_bond32<DIM, OPT>(Q, ni, uih, uil, nj, ujh, ujl, breakable, fs, dv);
+      newly = fs && !was;
       fi[0] = fmaf(s, dv[0], fi[0]);
       fi[1] = fmaf(s, dv[1], fi[1]);
       if (DIM == 3) fi[2] = fmaf(s, dv[2], fi[2]);
@@ -455,24 +465,30 @@ __global__ void __launch_bounds__(256)
     fi[1] += __shfl_xor_sync(0xffffffffu, fi[1], o);
     if (DIM == 3) fi[2] += __shfl_xor_sync(0xffffffffu, fi[2], o);
   }
-  if (lane == 0) integrate_node32<DIM, SCHEME, FIRST>(P, Q, D, T, A, i, fl, uih, uil, fi);
+  if (lane == 0) integrate_node32<DIM, SCHEME>(P, Q, D, T, A, i, fl, uih, uil, fi);
 }
 
-template <int DIM, int SCHEME, bool FIRST>
-static void launch_thread(const StepParams &P, const Params32 &Q, const DevPtrs &D,
-                          const BCTable &T, const StepArgs &a, int decomp, cudaStream_t s) {
+template <int DIM, int SCHEME, int OPT>
+static void launch_opt(const StepParams &P, const Params32 &Q, const DevPtrs &D,
+                       const BCTable &T, const StepArgs &a, int decomp, cudaStream_t s) {
+  if (decomp == NLM_DECOMP_WARP) {
+    const int bs = 256;
+    const unsigned grid = (unsigned)((P.n * 32 + bs - 1) / bs);
+    k_rnp32_warp<DIM, SCHEME, OPT><<<grid, bs, 0, s>>>(P, Q, D, T, a);
+    return;
+  }
   const int bs = 128;
   const unsigned grid = (unsigned)((P.n + bs - 1) / bs);
   if (decomp == NLM_DECOMP_THREAD1) {
     if (P.nw1)
-      k_rnp32_thread1<DIM, SCHEME, FIRST, true><<<grid, bs, 0, s>>>(P, Q, D, T, a);
+      k_rnp32_thread1<DIM, SCHEME, true, OPT><<<grid, bs, 0, s>>>(P, Q, D, T, a);
     else
-      k_rnp32_thread1<DIM, SCHEME, FIRST, false><<<grid, bs, 0, s>>>(P, Q, D, T, a);
+      k_rnp32_thread1<DIM, SCHEME, false, OPT><<<grid, bs, 0, s>>>(P, Q, D, T, a);
   } else {
     if (P.nw1)
-      k_rnp32_thread<DIM, SCHEME, FIRST, true><<<grid, bs, 0, s>>>(P, Q, D, T, a);
+      k_rnp32_thread<DIM, SCHEME, true, OPT><<<grid, bs, 0, s>>>(P, Q, D, T, a);
     else
-      k_rnp32_thread<DIM, SCHEME, FIRST, false><<<grid, bs, 0, s>>>(P, Q, D, T, a);
+      k_rnp32_thread<DIM, SCHEME, false, OPT><<<grid, bs, 0, s>>>(P, Q, D, T, a);
   }
 }
 
@@ -481,18 +497,12 @@ static cudaError_t launch32(const StepParams &P, const DevPtrs &D, const BCTable
                             const StepArgs &a, int decomp, cudaStream_t s) {
   if (P.n == 0) return cudaSuccess;
   const Params32 Q = make_p32(P);
-  if (decomp == NLM_DECOMP_WARP) {
-    const int bs = 256;
-    const unsigned grid = (unsigned)((P.n * 32 + bs - 1) / bs);
-    if (a.first)
-      k_rnp32_warp<DIM, SCHEME, true><<<grid, bs, 0, s>>>(P, Q, D, T, a);
-    else
-      k_rnp32_warp<DIM, SCHEME, false><<<grid, bs, 0, s>>>(P, Q, D, T, a);
-  } else {
-    if (a.first)
-      launch_thread<DIM, SCHEME, true>(P, Q, D, T, a, decomp, s);
-    else
-      launch_thread<DIM, SCHEME, false>(P, Q, D, T, a, decomp, s);
+  const int opt = (P.infl_type == 0 ? OPT_CONSTJ : 0) | (P.nofail ? OPT_NOFAIL : 0);
+  switch (opt) {
+    case 0: launch_opt<DIM, SCHEME, 0>(P, Q, D, T, a, decomp, s); break;
+    case 1: launch_opt<DIM, SCHEME, 1>(P, Q, D, T, a, decomp, s); break;
+    case 2: launch_opt<DIM, SCHEME, 2>(P, Q, D, T, a, decomp, s); break;
+    default: launch_opt<DIM, SCHEME, 3>(P, Q, D, T, a, decomp, s); break;
   }
   return cudaGetLastError();
 }

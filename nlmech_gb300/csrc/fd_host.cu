@@ -319,6 +319,7 @@ struct nlm_fd {
   int64_t step = 0;
   bool started = false;
   int cur = 0;
+  bool rows_by_orig = true;  // device rows ordered by original id
   StepParams P{};
   BCTable T{};
   cudaStream_t stream = nullptr;
@@ -741,7 +742,11 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
   const Grid g = make_grid(d->dim, n, d->x, d->horizon);
   NeighborBuild nb;
   std::string why;
-  e = build_neighbors(nb, d->dim, n, dx, g, S, s, why);
+  // FP64 plain keeps the reference's row order (its summation order); the
+  // FP32C kernels take rows in internal order so that the k-th neighbours of
+  // a warp's nodes sit close together in memory.
+  h->rows_by_orig = h->precision == NLM_PREC_FP64;
+  e = build_neighbors(nb, d->dim, n, dx, g, S, s, why, h->rows_by_orig);
   for (void *p : {(void *)nb.perm, (void *)nb.pos, (void *)nb.rowptr, (void *)nb.cols})
     if (p) h->allocs.push_back(p);
   if (e != cudaSuccess)
@@ -1018,6 +1023,7 @@ int nlm_fd_get_neighbors(nlm_fd *h, int64_t *rowptr, int32_t *cols) {
     for (int64_t o = 0; o < n; o++) {
       const int64_t s0 = h->rowptr[inv[o]], len = h->rowptr[inv[o] + 1] - s0;
       for (int64_t k = 0; k < len; k++) cols[rowptr[o] + k] = h->perm[cc[s0 + k]];
+      if (!h->rows_by_orig) std::sort(cols + rowptr[o], cols + rowptr[o] + len);
     }
   }
   return NLM_OK;
@@ -1115,15 +1121,32 @@ int nlm_fd_get_bond_state(nlm_fd *h, uint8_t *broken) {
   const int64_t n = h->n;
   std::vector<uint32_t> bits((size_t)h->P.nwords * h->P.npad);
   NLM_CUDA(cudaMemcpyAsync(bits.data(), h->D.bits, sizeof(uint32_t) * bits.size(), cudaMemcpyDeviceToHost, h->stream));
+  std::vector<int> cc;
+  if (!h->rows_by_orig) {
+    cc.resize(h->nnz);
+    if (h->nnz)
+      NLM_CUDA(cudaMemcpyAsync(cc.data(), h->D.cols, sizeof(int) * h->nnz, cudaMemcpyDeviceToHost, h->stream));
+  }
   NLM_CUDA(cudaStreamSynchronize(h->stream));
   std::vector<int64_t> inv(n);
   for (int64_t i = 0; i < n; i++) inv[h->perm[i]] = i;
   int64_t o_off = 0;
+  std::vector<std::pair<int, uint8_t>> row;
   for (int64_t o = 0; o < n; o++) {
     const int64_t i = inv[o];
-    const int64_t len = h->rowptr[i + 1] - h->rowptr[i];
-    for (int64_t k = 0; k < len; k++)
-      broken[o_off + k] = (bits[(size_t)(k >> 5) * h->P.npad + i] >> (k & 31)) & 1u;
+    const int64_t r0 = h->rowptr[i], len = h->rowptr[i + 1] - r0;
+    if (h->rows_by_orig) {
+      for (int64_t k = 0; k < len; k++)
+        broken[o_off + k] = (bits[(size_t)(k >> 5) * h->P.npad + i] >> (k & 31)) & 1u;
+    } else {
+      // device rows are in internal order: re-sort by original id
+      row.resize(len);
+      for (int64_t k = 0; k < len; k++)
+        row[k] = {h->perm[cc[r0 + k]],
+                  (uint8_t)((bits[(size_t)(k >> 5) * h->P.npad + i] >> (k & 31)) & 1u)};
+      std::sort(row.begin(), row.end());
+      for (int64_t k = 0; k < len; k++) broken[o_off + k] = row[k].second;
+    }
     o_off += len;
   }
   return NLM_OK;

@@ -78,10 +78,13 @@ __device__ __forceinline__ bool within(const double *a, const double *b, double 
   return dLT(__dsqrt_rn(s), rad);
 }
 
+// FILL pass: rows are ordered by ascending original id (the reference's order)
+// when by_orig, else by ascending internal (Morton) index.
 template <bool FILL>
 __global__ void k_neighbors(int64_t n, int S, const double *pos, const int64_t *cell, Grid g,
                             const int64_t *cbeg, const int64_t *cend, const int *perm,
-                            int64_t *count, const int64_t *rowptr, int *cols, int *err) {
+                            int64_t *count, const int64_t *rowptr, int *cols, int *err,
+                            bool by_orig) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   double xi[3] = {pos[S * i], pos[S * i + 1], S > 2 ? pos[S * i + 2] : 0.};
@@ -116,13 +119,13 @@ __global__ void k_neighbors(int64_t n, int S, const double *pos, const int64_t *
     if (cnt > kMaxRow) atomicExch(err, DEVERR_ROW_TOO_LONG);
     return;
   }
-  // order the row by ascending original id (insertion sort, rows <= kMaxRow)
+  // order the row (insertion sort, rows <= kMaxRow)
   int *row = cols + out;
   for (int64_t a = 1; a < cnt; a++) {
     const int v = row[a];
-    const int key = perm[v];
+    const int key = by_orig ? perm[v] : v;
     int64_t b = a - 1;
-    while (b >= 0 && perm[row[b]] > key) {
+    while (b >= 0 && (by_orig ? perm[row[b]] : row[b]) > key) {
       row[b + 1] = row[b];
       b--;
     }
@@ -248,7 +251,8 @@ Grid make_grid(int dim, int64_t n, const double *x, double horizon) {
 }
 
 cudaError_t build_neighbors(NeighborBuild &nb, int dim, int64_t n, const double *d_x,
-                            const Grid &g, int S, cudaStream_t s, std::string &why) {
+                            const Grid &g, int S, cudaStream_t s, std::string &why,
+                            bool rows_by_orig) {
   nb.n = n;
   nb.S = S;
   const int bs = 256;
@@ -303,7 +307,7 @@ cudaError_t build_neighbors(NeighborBuild &nb, int dim, int64_t n, const double 
     k_cell_ranges<<<blocks(n, bs), bs, 0, s>>>(n, cell, cbeg, cend);
     NB_TRY(cudaGetLastError());
     k_neighbors<false><<<blocks(n, 128), 128, 0, s>>>(n, S, nb.pos, cell, g, cbeg, cend, nb.perm,
-                                                      cnt, nullptr, nullptr, err);
+                                                      cnt, nullptr, nullptr, err, true);
     NB_TRY(cudaGetLastError());
     int herr = 0;
     NB_TRY(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -325,7 +329,8 @@ cudaError_t build_neighbors(NeighborBuild &nb, int dim, int64_t n, const double 
   NB_TRY(cudaMalloc(&nb.cols, sizeof(int) * (nb.nnz + 1)));
   if (n > 0) {
     k_neighbors<true><<<blocks(n, 128), 128, 0, s>>>(n, S, nb.pos, cell, g, cbeg, cend, nb.perm,
-                                                     nullptr, nb.rowptr, nb.cols, err);
+                                                     nullptr, nb.rowptr, nb.cols, err,
+                                                     rows_by_orig);
     NB_TRY(cudaGetLastError());
   }
   NB_TRY(cudaStreamSynchronize(s));

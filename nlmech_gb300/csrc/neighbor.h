@@ -33,8 +33,11 @@ struct SellStore {
 };
 
 Grid make_grid(int dim, int64_t n, const double *x, double horizon);
+// rows_by_orig: order each row by ascending original id (the reference's
+// order, needed for its FP64 summation order); otherwise by internal index.
 cudaError_t build_neighbors(NeighborBuild &nb, int dim, int64_t n, const double *d_x,
-                            const Grid &g, int S, cudaStream_t s, std::string &why);
+                            const Grid &g, int S, cudaStream_t s, std::string &why,
+                            bool rows_by_orig = true);
 cudaError_t build_sell(int64_t n, const int64_t *rowptr, const int *cols, SellStore &st,
                        cudaStream_t s);
 cudaError_t apply_precrack(int64_t n, int S, const double *pos, const int64_t *rowptr,

@@ -68,13 +68,14 @@ def test_neighbor_search_edge_cases(gpu, oracle):
 
 def test_model_neighbors_and_precrack(gpu, oracle):
     p = configs.config0()
-    m = gpu.FDModel(p)
     o = oracle.OracleFD(p, grid_neighbors=False)
-    ra, ca = m.neighbors()
     rb, cb = o.neighbors()
-    assert np.array_equal(ra, rb) and np.array_equal(ca, cb)
-    assert np.array_equal(m.bond_state(), o.bond_state())
-    assert m.count_broken() == int(o.bond_state().sum())
+    for prec in (abi.FP64, abi.FP32C):
+        m = gpu.FDModel(p, precision=prec)
+        ra, ca = m.neighbors()
+        assert np.array_equal(ra, rb) and np.array_equal(ca, cb)
+        assert np.array_equal(m.bond_state(), o.bond_state())
+        assert m.count_broken() == int(o.bond_state().sum())
 
 
 def _compare_fp64(m, o, rowptr, cols, what=""):

@@ -193,10 +193,10 @@ def test_step_host_matches_run(gpu):
     continue the run bit for bit."""
     p = configs.rnp_plate(30, 1e-3, 3, 0.008, 0.1, 2e-8, 50, seed=2)
     for prec in (abi.FP64, abi.FP32C):
-        a = gpu.FDModel(p, precision=prec)
+        a = gpu.FDModel(p, precision=prec, decomposition=abi.DECOMP_THREAD)
         a.run(20)
         ua, va, fa = a.state()
-        b = gpu.FDModel(p, precision=prec)
+        b = gpu.FDModel(p, precision=prec, decomposition=abi.DECOMP_THREAD)
         u = np.zeros((p.n, 3))
         v = np.zeros((p.n, 3))
         f = np.zeros((p.n, 3))
@@ -215,7 +215,7 @@ def test_runs_are_deterministic(gpu):
     for prec in (abi.FP64, abi.FP32C):
         r = []
         for _ in range(2):
-            m = gpu.FDModel(p, precision=prec)
+            m = gpu.FDModel(p, precision=prec, decomposition=abi.DECOMP_THREAD)
             m.run(300)
             r.append(m.state() + (m.bond_state(),))
         for a, b in zip(r[0], r[1]):

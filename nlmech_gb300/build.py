@@ -18,6 +18,7 @@ LIB = os.path.join(HERE, "libnlmgpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+          "-Xcompiler", "-ffp-contract=off",
           "--expt-relaxed-constexpr", "-I", os.path.join(HERE, "..", "include")]
 # translation unit -> extra flags
 UNITS = {
@@ -25,7 +26,8 @@ UNITS = {
     "neighbor.cu": ["--fmad=false"],
     "fd_fp64.cu": ["--fmad=false"],
     "fd_fp32.cu": [],
-    "es_stub.cu": [],
+    "es_fp64.cu": ["--fmad=false"],
+    "es_fp32.cu": [],
 }
 
 

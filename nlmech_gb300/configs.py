@@ -12,7 +12,7 @@ seed.  Conventions shared by all generators:
 import numpy as np
 
 from . import abi
-from .decks import BC, Crack, MaterialDeck, Problem
+from .decks import BC, Crack, MaterialDeck, Problem  # noqa: F401
 
 
 def glass_rnp(plane_strain=False):

@@ -723,7 +723,7 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
       h->decomp != NLM_DECOMP_THREAD1)
     return bail(fail(NLM_ERR_INVALID, "unknown decomposition"));
   const bool want_tune = d->decomposition == NLM_DECOMP_AUTO &&
-                         d->precision == NLM_PREC_FP32C;
+                         d->precision == NLM_PREC_FP32C && d->material.kind == NLM_MAT_RNP_BOND;
 
   cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
@@ -948,6 +948,19 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
   } else {
     TRY(h->alloc(&D.v32[0], (size_t)(S / 2) * n));
     TRY(h->alloc(&D.v32[1], (size_t)(S / 2) * n));
+  }
+  if (h->material == NLM_MAT_ELASTIC_STATE) {
+    double *mw;
+    TRY(h->alloc(&mw, n));
+    TRY(launch_es_setup(P, D, mw, s));
+    D.mw64 = mw;
+    if (h->precision == NLM_PREC_FP64) {
+      TRY(h->alloc(&D.theta64, n));
+      TRY(cudaMemsetAsync(D.theta64, 0, sizeof(double) * n, s));
+    } else {
+      TRY(h->alloc(&D.es_ab, n));
+      TRY(cudaMemsetAsync(D.es_ab, 0, sizeof(float2) * n, s));
+    }
   }
   TRY(h->alloc(&D.err, 1));
   TRY(cudaMemsetAsync(D.err, 0, sizeof(int), s));

@@ -37,9 +37,8 @@ struct DevPtrs {
   float *f32;      // FP32C force density, S per node
   // ElasticState
   const double *mw64;     // weighted volume m_i
-  const float *mw32;
-  double *theta64;        // dilatation
-  float *theta32;
+  double *theta64;        // FP64: dilatation theta_i
+  float2 *es_ab;          // FP32C: t = a |X| + b e coefficients per node
   int *err;               // device error flag
   const int *perm_dev;    // internal -> original node id
 };
@@ -67,6 +66,7 @@ cudaError_t launch_drift(const StepParams &P, const DevPtrs &D, const BCTable &T
                          double t_next, bool fp32, cudaStream_t s);
 cudaError_t launch_drift32(const StepParams &P, const DevPtrs &D, const BCTable &T, int cur,
                            double t_next, cudaStream_t s);
+cudaError_t launch_es_setup(const StepParams &P, const DevPtrs &D, double *mw, cudaStream_t s);
 cudaError_t launch_damage(const StepParams &P, const DevPtrs &D, int cur, bool fp32,
                           bool es, float *phi, float *Z, cudaStream_t s);
 

@@ -1,0 +1,250 @@
+// fp32_common.cuh -- shared pieces of the FP32-compensated kernels:
+// constants, approximate transcendental instructions, double-float
+// arithmetic, split node loads and the double-float integrator epilogue.
+#pragma once
+
+#include <cuda_fp16.h>
+
+#include "fd_internal.h"
+#include "state_io.cuh"
+
+namespace nlm {
+
+struct Params32 {
+  float check_low_eff;  // r > this  <=>  definitelyGreaterThan(r, check_low)
+  float check_up, inv_h, inv_delta;
+  float K1;             // 4 C beta / invF (times J when J is constant)
+  float Ksc;            // (f_sc rbar)^2 / (1 - 1e-5)^2: |S| > S_c  <=>  S^2 r > Ksc
+  float nbl2e;          // -beta * log2(e)
+  float inv_lo;         // 1 / lo_scale
+  int irrev;
+  int infl_type;
+  float a0, a1, alpha, ibeta;
+  // integrator constants as (hi, lo) pairs
+  float c_hi, c_lo;     // Verlet dt/(2 rho) or CD dt^2/rho
+  float dt_hi, dt_lo;
+  float idt_hi, idt_lo; // 1/dt
+};
+
+inline void split_const(double v, float &hi, float &lo) {
+  hi = (float)v;
+  lo = (float)(v - (double)hi);
+}
+
+inline Params32 make_p32(const StepParams &P) {
+  Params32 q;
+  q.check_low_eff = (float)(P.check_low / (1.0 - 1e-5));
+  q.check_up = (float)P.check_up;
+  q.inv_h = (float)(1.0 / P.h);
+  q.inv_delta = (float)(1.0 / P.delta);
+  double k1 = 4.0 * P.C * P.beta / P.invF;
+  if (P.infl_type == 0) k1 *= P.infl_a0;
+  q.K1 = (float)k1;
+  const double sc = P.fsc * P.rbar / (1.0 - 1e-5);
+  q.Ksc = (float)(sc * sc);
+  q.nbl2e = (float)(-P.beta * 1.4426950408889634);
+  q.inv_lo = (float)(1.0 / P.lo_scale);
+  q.irrev = P.irrev;
+  q.infl_type = P.infl_type;
+  q.a0 = (float)P.infl_a0;
+  q.a1 = (float)P.infl_a1;
+  q.alpha = (float)P.infl_alpha;
+  q.ibeta = P.infl_type == 2 ? (float)(1.0 / P.infl_beta) : 0.f;
+  const double c = P.scheme == NLM_VELOCITY_VERLET ? 0.5 * P.dt / P.rho : P.dt * P.dt / P.rho;
+  split_const(c, q.c_hi, q.c_lo);
+  split_const(P.dt, q.dt_hi, q.dt_lo);
+  split_const(1.0 / P.dt, q.idt_hi, q.idt_lo);
+  return q;
+}
+
+// ---- FP32 approximate transcendental instructions -------------------------
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// ---- double-float arithmetic (error-free transformations) ------------------
+struct df {
+  float hi, lo;
+};
+__device__ __forceinline__ df two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ df fast_two_sum(float a, float b) {
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ df df_add(df x, df y) {
+  const df s = two_sum(x.hi, y.hi);
+  return fast_two_sum(s.hi, s.lo + (x.lo + y.lo));
+}
+__device__ __forceinline__ df df_sub(df x, df y) { return df_add(x, {-y.hi, -y.lo}); }
+// (c_hi + c_lo) * y for a float y, as a pair
+__device__ __forceinline__ df df_cmul(float c_hi, float c_lo, float y) {
+  const float p = c_hi * y;
+  const float e = fmaf(c_hi, y, -p);
+  return fast_two_sum(p, fmaf(c_lo, y, e));
+}
+// x * (c_hi + c_lo)
+__device__ __forceinline__ df df_mul_c(df x, float c_hi, float c_lo) {
+  const float p = x.hi * c_hi;
+  float e = fmaf(x.hi, c_hi, -p);
+  e = fmaf(x.lo, c_hi, fmaf(x.hi, c_lo, e));
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ df df_from_double(double v) {
+  const float h = __double2float_rn(v);
+  return {h, __double2float_rn(v - (double)h)};
+}
+
+// ---- node access -----------------------------------------------------------
+template <int DIM>
+struct Node32 {
+  float xh[3];
+  __half2 lxy;  // lo of (x, y), scaled
+  __half2 lz;   // lo of z (3-D), scaled
+  float vol;
+};
+
+template <int DIM>
+__device__ __forceinline__ void ld_pos(const DevPtrs &D, int64_t j, Node32<DIM> &n) {
+  if (DIM == 2) {
+    const float4 a = __ldg(D.pos32 + j);
+    n.xh[0] = a.x;
+    n.xh[1] = a.y;
+    n.xh[2] = 0.f;
+    n.vol = a.z;
+    n.lxy = *reinterpret_cast<const __half2 *>(&a.w);
+    n.lz = __floats2half2_rn(0.f, 0.f);
+  } else {
+    const float4 a = __ldg(D.pos32 + j);
+    const uint2 b = __ldg(D.pos32lo + j);
+    n.xh[0] = a.x;
+    n.xh[1] = a.y;
+    n.xh[2] = a.z;
+    n.vol = a.w;
+    n.lxy = *reinterpret_cast<const __half2 *>(&b.x);
+    n.lz = *reinterpret_cast<const __half2 *>(&b.y);
+  }
+}
+
+template <int DIM>
+__device__ __forceinline__ void ld_pair(const float4 *p, int64_t j, float h[3], float l[3]) {
+  if (DIM == 2) {
+    const float4 a = p[j];
+    h[0] = a.x; h[1] = a.y; h[2] = 0.f;
+    l[0] = a.z; l[1] = a.w; l[2] = 0.f;
+  } else {
+    const float4 a = p[2 * j], b = p[2 * j + 1];
+    h[0] = a.x; h[1] = a.y; h[2] = a.z;
+    l[0] = b.x; l[1] = b.y; l[2] = b.z;
+  }
+}
+
+template <int DIM>
+__device__ __forceinline__ void st_pair(float4 *p, int64_t j, const df v[3]) {
+  if (DIM == 2) {
+    p[j] = make_float4(v[0].hi, v[1].hi, v[0].lo, v[1].lo);
+  } else {
+    p[2 * j] = make_float4(v[0].hi, v[1].hi, v[2].hi, 0.f);
+    p[2 * j + 1] = make_float4(v[0].lo, v[1].lo, v[2].lo, 0.f);
+  }
+}
+
+// Prescribed (du, dv) of one dof as double-float pairs.
+__device__ __forceinline__ void bc_df(const DevPtrs &D, const BCTable &T, int ref, int c, double t,
+                                      df &u, df &v) {
+  double du, dv;
+  bc_dof(D, T, ref, c, t, du, dv);
+  u = df_from_double(du);
+  v = df_from_double(dv);
+}
+
+// FP32C integrator epilogue (same phase structure as integrate_node64).
+template <int DIM, int SCHEME>
+__device__ __forceinline__ void integrate_node32(const StepParams &P, const Params32 &Q,
+                                                 const DevPtrs &D, const BCTable &T,
+                                                 const StepArgs &A, int64_t i, uint8_t fl,
+                                                 const float uih[3], const float uil[3],
+                                                 const float fint[3]) {
+  float f[3] = {fint[0], fint[1], fint[2]};
+  if (fl & FLAG_FBC) {
+    double fe[3];
+    ld_node<DIM>(D.fext, i, fe);
+    for (int c = 0; c < DIM; c++) f[c] = (float)(fe[c] + (double)fint[c]);
+  }
+  const int ref = (fl & 7) ? D.bcref[i] : -1;
+  df un[3], vn[3];
+  if (SCHEME == NLM_VELOCITY_VERLET) {
+    float vh_[3], vl_[3];
+    ld_pair<DIM>(D.v32[0], i, vh_, vl_);
+    const bool FIRST = A.first;
+    float fp[3] = {0.f, 0.f, 0.f};
+    if (!FIRST) {
+      if (DIM == 2) {
+        const float2 a = reinterpret_cast<const float2 *>(D.f32)[i];
+        fp[0] = a.x;
+        fp[1] = a.y;
+      } else {
+        const float4 a = reinterpret_cast<const float4 *>(D.f32)[i];
+        fp[0] = a.x;
+        fp[1] = a.y;
+        fp[2] = a.z;
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < DIM; c++) {
+      const df v{vh_[c], vl_[c]};
+      if (!(fl >> c & 1)) {
+        const df cf = df_cmul(Q.c_hi, Q.c_lo, f[c]);
+        df vm = v;
+        if (!FIRST) vm = df_add(df_add(v, df_cmul(Q.c_hi, Q.c_lo, fp[c])), cf);
+        vn[c] = vm;
+        const df vh2 = df_add(vm, cf);
+        un[c] = df_add({uih[c], uil[c]}, df_mul_c(vh2, Q.dt_hi, Q.dt_lo));
+      } else {
+        df du, dv;
+        if (!FIRST) {
+          bc_df(D, T, ref, c, A.t_now, du, dv);
+          vn[c] = dv;
+        } else {
+          vn[c] = v;
+        }
+        bc_df(D, T, ref, c, A.t_next, du, dv);
+        un[c] = du;
+      }
+    }
+    st_pair<DIM>(D.v32[0], i, vn);
+  } else {
+    float vh_[3], vl_[3];
+    ld_pair<DIM>(D.v32[A.cur], i, vh_, vl_);
+#pragma unroll
+    for (int c = 0; c < DIM; c++) {
+      if (!(fl >> c & 1)) {
+        const df u{uih[c], uil[c]};
+        const df inc = df_add(df_cmul(Q.c_hi, Q.c_lo, f[c]),
+                              df_mul_c({vh_[c], vl_[c]}, Q.dt_hi, Q.dt_lo));
+        un[c] = df_add(u, inc);
+        vn[c] = df_mul_c(df_sub(un[c], u), Q.idt_hi, Q.idt_lo);
+      } else {
+        bc_df(D, T, ref, c, A.t_next, un[c], vn[c]);
+      }
+    }
+    st_pair<DIM>(D.v32[1 - A.cur], i, vn);
+  }
+  if (DIM == 2)
+    reinterpret_cast<float2 *>(D.f32)[i] = make_float2(f[0], f[1]);
+  else
+    reinterpret_cast<float4 *>(D.f32)[i] = make_float4(f[0], f[1], f[2], 0.f);
+  st_pair<DIM>(D.u32[1 - A.cur], i, un);
+}
+
+}  // namespace nlm

@@ -648,10 +648,14 @@ double es_t(const Model &m, int64_t i, double e, double Xlen) {
   }
   if (m.dim == 2) {
     double alpha_s;
-    if (!p.plane_strain)
-      alpha_s = (9. / mi) * (p.K + std::pow((p.nu + 1.) / (2. * p.nu - 1.), 2) * p.mu / 9.);
-    else
+    if (!p.plane_strain) {
+      // std::pow(q, 2) in the reference; a correctly rounded square either way
+      const double q = (p.nu + 1.) / (2. * p.nu - 1.);
+      alpha_s = (9. / mi) * (p.K + q * q * p.mu / 9.);
+    }
+    else {
       alpha_s = (9. / mi) * (p.K + p.mu / 9.);
+    }
     double alpha_d = (8. / mi) * p.mu;
     double e_s = m.theta[i] * Xlen / 3.;
     double e_d = e - e_s;

@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=200)
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-steps", type=int, default=30)
+    ap.add_argument("--es-steps", type=int, default=50,
+                    help="steps of the 100^3 ElasticState cube (0: skip)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--decomp", default="auto", choices=["auto", "thread", "thread1", "warp"])
     ap.add_argument("--quick", action="store_true",
@@ -252,6 +254,23 @@ def run_ours(a):
     value64 = total_bonds * a.fp64_steps / (ms64 * 1e-3)
     m64.close()
 
+    # ---- 3-D ElasticState cube (two-pass kernels), reported beside ----
+    es = None
+    if a.es_steps > 0 and not a.quick:
+        from nlmech_gb300 import configs
+        pe = configs.config2(seed=rank)
+        es = {"workload": "es3d_cube_100^3_d3h_verlet", "nodes": pe.n}
+        for prec, key, k in ((abi.FP32C, "fp32c", a.es_steps), (abi.FP64, "fp64_plain",
+                                                                  max(3, a.es_steps // 10))):
+            mm = gpu.FDModel(pe, precision=prec)
+            mm.run(2)
+            barrier_sync()
+            t = max_over_ranks(mm.run_timed(k))
+            es["bonds"] = mm.nnz()
+            es[key] = {"value": sum_over_ranks(float(mm.nnz())) * k / (t * 1e-3), "unit": UNIT,
+                       "steps": k, "ms_per_step": t / k}
+            mm.close()
+
     # ---- end to end through the host-resident drop-in call ----
     me = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_AUTO)
     bufs = [torch.zeros((n, 3), dtype=torch.float64).pin_memory() for _ in range(3)]
@@ -291,6 +310,7 @@ def run_ours(a):
         "fp64_plain": {"value": value64, "unit": UNIT, "steps": a.fp64_steps,
                        "ms_per_step": ms64 / a.fp64_steps},
         "fp32_over_fp64": value / value64,
+        "es3d": es,
         "broken_bonds_after_run": broken,
         "e2e": {"value": e2e_value, "unit": UNIT, "steps": a.e2e_steps,
                 "h2d_bytes_per_step": 3 * 3 * 8 * n, "d2h_bytes_per_step": 3 * 3 * 8 * n,

@@ -249,6 +249,35 @@ int nlm_fd_step_host(nlm_fd *h, double *u, double *v, double *f,
  * device time of the whole run (the stream is synchronized). */
 int nlm_fd_run_timed(nlm_fd *h, int64_t nsteps, double *ms);
 
+/* Replay the step loop from CUDA graphs of steps_per_graph steps (even,
+ * >= 2; 0 = plain launches).  The step-0 evaluation and any remainder run as
+ * plain launches.  Not available with Force_BC sets (returns UNSUPPORTED). */
+int nlm_fd_set_graph(nlm_fd *h, int steps_per_graph);
+
+/* ---- batched specimens -------------------------------------------------
+ * Many independent specimens (same dimension, dt, scheme and material kind;
+ * FP32-compensated RNPBond) in one node space: each step is one launch per
+ * node-count bucket over all specimens, each bucket with the decomposition
+ * the autotuner picked for it.  Per-specimen constants live in a table in
+ * device memory.  Specimen ids below are positions in the descs array. */
+typedef struct nlm_batch nlm_batch;
+
+int nlm_batch_create(const nlm_fd_desc *descs, int n_specimens, nlm_batch **out);
+int nlm_batch_destroy(nlm_batch *b);
+int nlm_batch_run(nlm_batch *b, int64_t nsteps);
+/* nlm_batch_run bracketed by CUDA events on the batch's stream. */
+int nlm_batch_run_timed(nlm_batch *b, int64_t nsteps, double *ms);
+/* Bonds of one specimen, or of all specimens when specimen == -1. */
+int nlm_batch_num_bonds(const nlm_batch *b, int specimen, int64_t *nnz);
+int nlm_batch_get_state(nlm_batch *b, int specimen, double *u, double *v, double *f);
+int nlm_batch_get_bond_state(nlm_batch *b, int specimen, uint8_t *broken);
+int nlm_batch_get_time(const nlm_batch *b, double *time, int64_t *step);
+/* Same meaning as nlm_fd_set_graph. */
+int nlm_batch_set_graph(nlm_batch *b, int steps_per_graph);
+/* Buckets (at most 8): node count and chosen decomposition of each. */
+int nlm_batch_buckets(const nlm_batch *b, int *n_buckets, int64_t *bucket_nodes,
+                      int *decomps);
+
 #ifdef __cplusplus
 }
 #endif

@@ -35,7 +35,8 @@ enum : uint8_t {
   FLAG_FIX_Y = 2,
   FLAG_FIX_Z = 4,
   FLAG_NOFAIL = 8,  // non-interior node: bonds never break (rnpBond.cpp:235-240)
-  FLAG_FBC = 16     // node carries an external force (Force_BC)
+  FLAG_FBC = 16,    // node carries an external force (Force_BC)
+  FLAG_GHOST = 32   // padding node of a batched specimen (never updated)
 };
 
 constexpr int kMaxBCSets = 32;

@@ -59,7 +59,7 @@ __device__ __forceinline__ float rnp_bond32(const Params32 &Q, const Node32<DIM>
   const float r = r2 * rinv;
   const float S = de * (rinv * rinv);
   float k = Q.K1 * nj.vol * fminf(1.f, (Q.check_up - r) * Q.inv_h);
-  if (!(OPT & OPT_CONSTJ)) {
+  if (!(OPT & OPT_CONSTJ) && Q.infl_type != 0) {  // type 0: J folded into K1
     const float rr = r * Q.inv_delta;
     k *= Q.infl_type == 1 ? Q.a0 + Q.a1 * rr
                           : Q.alpha * ex2_approx(-rr * rr * Q.ibeta * 1.4426950408889634f);
@@ -77,12 +77,14 @@ __device__ __forceinline__ float rnp_bond32(const Params32 &Q, const Node32<DIM>
 // ids (the next group's ids are fetched while the current group is gathered
 // and evaluated), then the eight node gathers of the group are issued
 // together, so each thread keeps several independent loads in flight.
-template <int DIM, int SCHEME, bool NW1, int OPT>
+template <int DIM, int SCHEME, bool NW1, int OPT, bool BATCH>
 __global__ void __launch_bounds__(128, DIM == 2 ? 7 : 5)
-    k_rnp32_thread(const StepParams P, const Params32 Q, const DevPtrs D, const BCTable T,
+    k_rnp32_thread(const StepParams P, const Params32 Q0, const DevPtrs D, const BCTable T,
                    const StepArgs A) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= P.n) return;
+  const int64_t i = A.i0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= A.i1) return;
+  if (BATCH && (D.flags[i] & FLAG_GHOST)) return;
+  const Params32 &Q = BATCH ? static_cast<const Params32 *>(D.qtab)[D.slice_spec[i >> 5]] : Q0;
   const float4 *ucur = D.u32[A.cur];
   Node32<DIM> ni;
   ld_pos<DIM>(D, i, ni);
@@ -136,12 +138,14 @@ __global__ void __launch_bounds__(128, DIM == 2 ? 7 : 5)
 }
 
 // Same decomposition without the four-wide grouping (one bond per iteration).
-template <int DIM, int SCHEME, bool NW1, int OPT>
+template <int DIM, int SCHEME, bool NW1, int OPT, bool BATCH>
 __global__ void __launch_bounds__(128, DIM == 2 ? 12 : 8)
-    k_rnp32_thread1(const StepParams P, const Params32 Q, const DevPtrs D, const BCTable T,
+    k_rnp32_thread1(const StepParams P, const Params32 Q0, const DevPtrs D, const BCTable T,
                     const StepArgs A) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= P.n) return;
+  const int64_t i = A.i0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= A.i1) return;
+  if (BATCH && (D.flags[i] & FLAG_GHOST)) return;
+  const Params32 &Q = BATCH ? static_cast<const Params32 *>(D.qtab)[D.slice_spec[i >> 5]] : Q0;
   const float4 *ucur = D.u32[A.cur];
   Node32<DIM> ni;
   ld_pos<DIM>(D, i, ni);
@@ -180,13 +184,15 @@ __global__ void __launch_bounds__(128, DIM == 2 ? 12 : 8)
 }
 
 // Warp-per-node over CSR rows; lane k of the warp owns bonds k, k+32, ...
-template <int DIM, int SCHEME, int OPT>
+template <int DIM, int SCHEME, int OPT, bool BATCH>
 __global__ void __launch_bounds__(256)
-    k_rnp32_warp(const StepParams P, const Params32 Q, const DevPtrs D, const BCTable T,
+    k_rnp32_warp(const StepParams P, const Params32 Q0, const DevPtrs D, const BCTable T,
                  const StepArgs A) {
-  const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t i = A.i0 + ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
-  if (i >= P.n) return;
+  if (i >= A.i1) return;
+  if (BATCH && (D.flags[i] & FLAG_GHOST)) return;
+  const Params32 &Q = BATCH ? static_cast<const Params32 *>(D.qtab)[D.slice_spec[i >> 5]] : Q0;
   const float4 *ucur = D.u32[A.cur];
   Node32<DIM> ni;
   ld_pos<DIM>(D, i, ni);
@@ -228,27 +234,29 @@ __global__ void __launch_bounds__(256)
   if (lane == 0) integrate_node32<DIM, SCHEME>(P, Q, D, T, A, i, fl, uih, uil, fi);
 }
 
-template <int DIM, int SCHEME, int OPT>
+template <int DIM, int SCHEME, int OPT, bool BATCH>
 static void launch_opt(const StepParams &P, const Params32 &Q, const DevPtrs &D,
                        const BCTable &T, const StepArgs &a, int decomp, cudaStream_t s) {
+  const int64_t nodes = a.i1 - a.i0;
+  if (nodes <= 0) return;
   if (decomp == NLM_DECOMP_WARP) {
     const int bs = 256;
-    const unsigned grid = (unsigned)((P.n * 32 + bs - 1) / bs);
-    k_rnp32_warp<DIM, SCHEME, OPT><<<grid, bs, 0, s>>>(P, Q, D, T, a);
+    const unsigned grid = (unsigned)((nodes * 32 + bs - 1) / bs);
+    k_rnp32_warp<DIM, SCHEME, OPT, BATCH><<<grid, bs, 0, s>>>(P, Q, D, T, a);
     return;
   }
   const int bs = 128;
-  const unsigned grid = (unsigned)((P.n + bs - 1) / bs);
+  const unsigned grid = (unsigned)((nodes + bs - 1) / bs);
   if (decomp == NLM_DECOMP_THREAD1) {
     if (P.nw1)
-      k_rnp32_thread1<DIM, SCHEME, true, OPT><<<grid, bs, 0, s>>>(P, Q, D, T, a);
+      k_rnp32_thread1<DIM, SCHEME, true, OPT, BATCH><<<grid, bs, 0, s>>>(P, Q, D, T, a);
     else
-      k_rnp32_thread1<DIM, SCHEME, false, OPT><<<grid, bs, 0, s>>>(P, Q, D, T, a);
+      k_rnp32_thread1<DIM, SCHEME, false, OPT, BATCH><<<grid, bs, 0, s>>>(P, Q, D, T, a);
   } else {
     if (P.nw1)
-      k_rnp32_thread<DIM, SCHEME, true, OPT><<<grid, bs, 0, s>>>(P, Q, D, T, a);
+      k_rnp32_thread<DIM, SCHEME, true, OPT, BATCH><<<grid, bs, 0, s>>>(P, Q, D, T, a);
     else
-      k_rnp32_thread<DIM, SCHEME, false, OPT><<<grid, bs, 0, s>>>(P, Q, D, T, a);
+      k_rnp32_thread<DIM, SCHEME, false, OPT, BATCH><<<grid, bs, 0, s>>>(P, Q, D, T, a);
   }
 }
 
@@ -258,11 +266,21 @@ static cudaError_t launch32(const StepParams &P, const DevPtrs &D, const BCTable
   if (P.n == 0) return cudaSuccess;
   const Params32 Q = make_p32(P);
   const int opt = (P.infl_type == 0 ? OPT_CONSTJ : 0) | (P.nofail ? OPT_NOFAIL : 0);
+  const bool batch = D.qtab != nullptr;
+  if (batch) {
+    // specimens may mix influence functions: the batch path always takes the
+    // general influence evaluation
+    if (P.nofail)
+      launch_opt<DIM, SCHEME, OPT_NOFAIL, true>(P, Q, D, T, a, decomp, s);
+    else
+      launch_opt<DIM, SCHEME, 0, true>(P, Q, D, T, a, decomp, s);
+    return cudaGetLastError();
+  }
   switch (opt) {
-    case 0: launch_opt<DIM, SCHEME, 0>(P, Q, D, T, a, decomp, s); break;
-    case 1: launch_opt<DIM, SCHEME, 1>(P, Q, D, T, a, decomp, s); break;
-    case 2: launch_opt<DIM, SCHEME, 2>(P, Q, D, T, a, decomp, s); break;
-    default: launch_opt<DIM, SCHEME, 3>(P, Q, D, T, a, decomp, s); break;
+    case 0: launch_opt<DIM, SCHEME, 0, false>(P, Q, D, T, a, decomp, s); break;
+    case 1: launch_opt<DIM, SCHEME, 1, false>(P, Q, D, T, a, decomp, s); break;
+    case 2: launch_opt<DIM, SCHEME, 2, false>(P, Q, D, T, a, decomp, s); break;
+    default: launch_opt<DIM, SCHEME, 3, false>(P, Q, D, T, a, decomp, s); break;
   }
   return cudaGetLastError();
 }

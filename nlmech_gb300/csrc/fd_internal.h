@@ -41,6 +41,11 @@ struct DevPtrs {
   float2 *es_ab;          // FP32C: t = a |X| + b e coefficients per node
   int *err;               // device error flag
   const int *perm_dev;    // internal -> original node id
+  // batched specimens (FP32C RNPBond): per-slice specimen id, per-specimen
+  // FP32 constants (Params32) and a global table of BC time functions
+  const int *slice_spec;
+  const void *qtab;
+  const BCTime *bct;
 };
 
 // Which buffers a launch reads/writes.
@@ -49,6 +54,8 @@ struct StepArgs {
   bool first;     // step-0 force evaluation (no velocity completion)
   double t_now;   // t_m
   double t_next;  // t_{m+1}
+  const double *tdev;  // if set: t_m = tdev[0], t_{m+1} = tdev[1] (graph replay)
+  int64_t i0, i1;      // node range of this launch (FP32C RNP kernels)
 };
 
 // Launchers (return cudaError_t of the launch).

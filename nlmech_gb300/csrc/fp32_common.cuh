@@ -213,12 +213,12 @@ __device__ __forceinline__ void integrate_node32(const StepParams &P, const Para
       } else {
         df du, dv;
         if (!FIRST) {
-          bc_df(D, T, ref, c, A.t_now, du, dv);
+          bc_df(D, T, ref, c, t_now_of(A), du, dv);
           vn[c] = dv;
         } else {
           vn[c] = v;
         }
-        bc_df(D, T, ref, c, A.t_next, du, dv);
+        bc_df(D, T, ref, c, t_next_of(A), du, dv);
         un[c] = du;
       }
     }
@@ -235,7 +235,7 @@ __device__ __forceinline__ void integrate_node32(const StepParams &P, const Para
         un[c] = df_add(u, inc);
         vn[c] = df_mul_c(df_sub(un[c], u), Q.idt_hi, Q.idt_lo);
       } else {
-        bc_df(D, T, ref, c, A.t_next, un[c], vn[c]);
+        bc_df(D, T, ref, c, t_next_of(A), un[c], vn[c]);
       }
     }
     st_pair<DIM>(D.v32[1 - A.cur], i, vn);

@@ -189,10 +189,11 @@ __device__ bool plane_cuts(const nlm_crack &c, const double *a, const double *b)
   return px >= c.lo[0] && px <= c.hi[0] && py >= c.lo[1] && py <= c.hi[1];
 }
 
-__global__ void k_precrack(int64_t n, int S, const double *pos, const int64_t *rowptr,
-                           const int *cols, nlm_crack ck, int64_t npad, uint32_t *bits) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
+__global__ void k_precrack(int64_t n, int64_t off, int S, const double *pos,
+                           const int64_t *rowptr, const int *cols, nlm_crack ck, int64_t npad,
+                           uint32_t *bits) {
+  const int64_t i = off + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= off + n) return;
   const double xi[3] = {pos[S * i], pos[S * i + 1], S > 2 ? pos[S * i + 2] : 0.};
   const int64_t r0 = rowptr[i], r1 = rowptr[i + 1];
   if (ck.kind == NLM_CRACK_PLANE) {
@@ -376,9 +377,29 @@ cudaError_t build_sell(int64_t n, const int64_t *rowptr, const int *cols, SellSt
 
 cudaError_t apply_precrack(int64_t n, int S, const double *pos, const int64_t *rowptr,
                            const int *cols, const nlm_crack &ck, int64_t npad, uint32_t *bits,
-                           cudaStream_t s) {
+                           cudaStream_t s, int64_t off) {
   if (n == 0) return cudaSuccess;
-  k_precrack<<<blocks(n, 128), 128, 0, s>>>(n, S, pos, rowptr, cols, ck, npad, bits);
+  k_precrack<<<blocks(n, 128), 128, 0, s>>>(n, off, S, pos, rowptr, cols, ck, npad, bits);
+  return cudaGetLastError();
+}
+
+__global__ void k_offset_cols(int64_t nnz, int *cols, int off) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k < nnz) cols[k] += off;
+}
+__global__ void k_offset_rowptr(int64_t n, int64_t *rowptr, int64_t off) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k < n) rowptr[k] += off;
+}
+
+cudaError_t offset_cols(int64_t nnz, int *cols, int off, cudaStream_t s) {
+  if (nnz == 0) return cudaSuccess;
+  k_offset_cols<<<blocks(nnz, 256), 256, 0, s>>>(nnz, cols, off);
+  return cudaGetLastError();
+}
+cudaError_t offset_rowptr(int64_t n, int64_t *rowptr, int64_t off, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  k_offset_rowptr<<<blocks(n, 256), 256, 0, s>>>(n, rowptr, off);
   return cudaGetLastError();
 }
 

@@ -40,8 +40,12 @@ cudaError_t build_neighbors(NeighborBuild &nb, int dim, int64_t n, const double 
                             bool rows_by_orig = true);
 cudaError_t build_sell(int64_t n, const int64_t *rowptr, const int *cols, SellStore &st,
                        cudaStream_t s);
+// Pre-crack bits of rows [off, off + n).
 cudaError_t apply_precrack(int64_t n, int S, const double *pos, const int64_t *rowptr,
                            const int *cols, const nlm_crack &ck, int64_t npad, uint32_t *bits,
-                           cudaStream_t s);
+                           cudaStream_t s, int64_t off = 0);
+// cols[k] += off, rowptr[k] += off (batched specimens).
+cudaError_t offset_cols(int64_t nnz, int *cols, int off, cudaStream_t s);
+cudaError_t offset_rowptr(int64_t n, int64_t *rowptr, int64_t off, cudaStream_t s);
 
 }  // namespace nlm

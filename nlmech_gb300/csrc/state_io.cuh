@@ -112,7 +112,16 @@ __device__ __forceinline__ void bc_dof(const DevPtrs &D, const BCTable &T, int r
   const int s = e.set[d];
   du = 0.;
   dv = 0.;
-  if (s >= 0) bc_value(T.t[s], e.umax[d], t, du, dv);
+  if (s >= 0) bc_value(D.bct ? D.bct[s] : T.t[s], e.umax[d], t, du, dv);
+}
+
+// Step times of a launch (from the arguments, or from device memory when the
+// launch is replayed from a CUDA graph).
+__device__ __forceinline__ double t_now_of(const StepArgs &A) {
+  return A.tdev ? __ldg(A.tdev) : A.t_now;
+}
+__device__ __forceinline__ double t_next_of(const StepArgs &A) {
+  return A.tdev ? __ldg(A.tdev + 1) : A.t_next;
 }
 
 // Integrator epilogue of the fused step, FP64 state (see fd_host.cu for the
@@ -149,7 +158,7 @@ __device__ __forceinline__ void integrate_node64(const StepParams &P, const DevP
           vn[d] = vh + fact * f[d];
         } else {
           double du, dv;
-          bc_dof(D, T, ref, d, A.t_now, du, dv);
+          bc_dof(D, T, ref, d, t_now_of(A), du, dv);
           vn[d] = dv;
         }
       }
@@ -162,7 +171,7 @@ __device__ __forceinline__ void integrate_node64(const StepParams &P, const DevP
         un[d] = ui[d] + P.dt * vh;
       } else {
         double du, dv;
-        bc_dof(D, T, ref, d, A.t_next, du, dv);
+        bc_dof(D, T, ref, d, t_next_of(A), du, dv);
         un[d] = du;
       }
     }
@@ -178,7 +187,7 @@ __device__ __forceinline__ void integrate_node64(const StepParams &P, const DevP
         vn[d] = (un[d] - ui[d]) / P.dt;
       } else {
         double du, dv;
-        bc_dof(D, T, ref, d, A.t_next, du, dv);
+        bc_dof(D, T, ref, d, t_next_of(A), du, dv);
         un[d] = du;
         vn[d] = dv;
       }

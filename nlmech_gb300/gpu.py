@@ -180,3 +180,79 @@ class FDModel:
         _check(load().nlm_fd_kernel_stats(self.h, C.c_int(int(reset)), C.byref(ms), C.byref(L),
                                           C.byref(b)))
         return ms.value, L.value, b.value
+
+
+def _fd_set_graph(self, steps_per_graph):
+    """Replay the step loop from CUDA graphs of this many steps (0: off)."""
+    _check(load().nlm_fd_set_graph(self.h, C.c_int(int(steps_per_graph))))
+
+
+FDModel.set_graph = _fd_set_graph
+
+
+class Batch:
+    """Many independent RNPBond specimens stepped together (FP32C)."""
+
+    def __init__(self, problems, scheme=None):
+        self.problems = list(problems)
+        descs, self._keep = [], []
+        for p in self.problems:
+            d, keep = p.desc(precision=abi.FP32C, scheme=scheme)
+            descs.append(d)
+            self._keep.append(keep)
+        arr = (abi.FDDesc * len(descs))(*descs)
+        self._keep.append(arr)
+        h = C.c_void_p()
+        _check(load().nlm_batch_create(arr, C.c_int(len(descs)), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.nlm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def nnz(self, s=-1):
+        v = C.c_int64()
+        _check(load().nlm_batch_num_bonds(self.h, C.c_int(s), C.byref(v)))
+        return v.value
+
+    def run(self, nsteps):
+        _check(load().nlm_batch_run(self.h, C.c_int64(int(nsteps))))
+
+    def run_timed(self, nsteps):
+        ms = C.c_double()
+        _check(load().nlm_batch_run_timed(self.h, C.c_int64(int(nsteps)), C.byref(ms)))
+        return ms.value
+
+    def set_graph(self, steps_per_graph):
+        _check(load().nlm_batch_set_graph(self.h, C.c_int(int(steps_per_graph))))
+
+    def state(self, s):
+        n = self.problems[s].n
+        u = np.zeros((n, 3))
+        v = np.zeros((n, 3))
+        f = np.zeros((n, 3))
+        _check(load().nlm_batch_get_state(self.h, C.c_int(s), abi.dptr(u), abi.dptr(v),
+                                          abi.dptr(f)))
+        return u, v, f
+
+    def bond_state(self, s):
+        b = np.zeros(self.nnz(s), dtype=np.uint8)
+        _check(load().nlm_batch_get_bond_state(self.h, C.c_int(s), abi.ptr(b, C.c_uint8)))
+        return b
+
+    def time(self):
+        t = C.c_double()
+        n = C.c_int64()
+        _check(load().nlm_batch_get_time(self.h, C.byref(t), C.byref(n)))
+        return t.value, n.value
+
+    def buckets(self):
+        nb = C.c_int()
+        nodes = (C.c_int64 * 8)()
+        dec = (C.c_int * 8)()
+        _check(load().nlm_batch_buckets(self.h, C.byref(nb), nodes, dec))
+        return [(nodes[k], dec[k]) for k in range(nb.value)]

@@ -278,6 +278,46 @@ int nlm_batch_set_graph(nlm_batch *b, int steps_per_graph);
 int nlm_batch_buckets(const nlm_batch *b, int *n_buckets, int64_t *bucket_nodes,
                       int *decomps);
 
+/* ---- quasi-static Newton (replaces QuasiStaticModel<T>::solver) ---------
+ * RNPBond plates: load step k sets the Displacement_BC values at time k*dt
+ * (QuasiStaticModel.cpp:537-549), then Newton iterations on the free dofs
+ * with the analytic sparse tangent and preconditioned CG until
+ * ||r|| <= tol * ||r(plain guess)||, where the plain guess is the previous
+ * load step's solution with the new boundary values.  Bonds over the
+ * critical strain break after convergence and the step is solved again. */
+typedef struct nlm_qs_params {
+  int max_newton;      /* Newton iterations per solve (Solver.Max_Iteration) */
+  double tol;          /* relative residual tolerance (default 1e-8)         */
+  int lin_max_iters;   /* CG iterations per Newton step                      */
+  double lin_tol;      /* CG relative tolerance (inexact Newton)             */
+  int break_bonds;     /* 1: staggered bond breaking after convergence       */
+  int max_break_rounds;
+} nlm_qs_params;
+
+typedef struct nlm_qs_stats {
+  int newton_iters;    /* all Newton iterations of the load step             */
+  int lin_iters;       /* all CG iterations                                   */
+  int break_rounds;    /* re-solves after bond breaking                       */
+  int used_guess;      /* 1 if the caller's guess was used (not the fallback) */
+  int64_t broken;      /* bonds broken in this step                           */
+  double res_plain;    /* ||r|| at the plain previous-step guess              */
+  double res_start;    /* ||r|| at the start point actually used             */
+  double res_final;
+  double ms;           /* wall time of the load step                         */
+} nlm_qs_stats;
+
+typedef struct nlm_qs nlm_qs;
+int nlm_qs_create(const nlm_fd_desc *desc, const nlm_qs_params *prm, nlm_qs **out);
+int nlm_qs_destroy(nlm_qs *q);
+/* One load step.  guess: 3*n displacement (original order) to start Newton
+ * from, or NULL for the plain previous-step guess; a guess whose residual
+ * exceeds the plain guess's is replaced by the plain guess. */
+int nlm_qs_load_step(nlm_qs *q, const double *guess, nlm_qs_stats *stats);
+int nlm_qs_get_state(nlm_qs *q, double *u);
+int nlm_qs_get_bond_state(nlm_qs *q, uint8_t *broken);
+int nlm_qs_damage(nlm_qs *q, float *phi, float *Z);
+int nlm_qs_num_bonds(const nlm_qs *q, int64_t *nnz);
+
 #ifdef __cplusplus
 }
 #endif

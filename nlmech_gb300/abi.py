@@ -128,3 +128,31 @@ def ptr(a, ctype):
         return C.POINTER(ctype)()
     assert a.flags["C_CONTIGUOUS"]
     return a.ctypes.data_as(C.POINTER(ctype))
+
+
+class QSParams(C.Structure):
+    _fields_ = [
+        ("max_newton", C.c_int),
+        ("tol", C.c_double),
+        ("lin_max_iters", C.c_int),
+        ("lin_tol", C.c_double),
+        ("break_bonds", C.c_int),
+        ("max_break_rounds", C.c_int),
+    ]
+
+
+class QSStats(C.Structure):
+    _fields_ = [
+        ("newton_iters", C.c_int),
+        ("lin_iters", C.c_int),
+        ("break_rounds", C.c_int),
+        ("used_guess", C.c_int),
+        ("broken", C.c_int64),
+        ("res_plain", C.c_double),
+        ("res_start", C.c_double),
+        ("res_final", C.c_double),
+        ("ms", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}

@@ -28,6 +28,7 @@ UNITS = {
     "fd_fp32.cu": [],
     "es_fp64.cu": ["--fmad=false"],
     "es_fp32.cu": [],
+    "qs.cu": [],
 }
 
 

@@ -122,3 +122,38 @@ def ensemble(nplates=256, nmin=5000, nmax=200000, seed=0, steps=1000):
         out.append(rnp_plate(nx, h, 4, frac * nx * h, speed, 2e-8, steps, seed=seed + 1000 + p,
                              name="plate%03d" % p))
     return out
+
+
+def qs_plate(nx=200, h=5e-4, ratio=3, crack_frac=0.2, crack_center=(0.5, 0.5), du=1e-6,
+             layers=3, jitter=0.0, seed=0, name=""):
+    """Quasi-static RNPBond plate: nx x nx nodes, bottom `layers` rows fixed in
+    x and y, top rows prescribed u_y = du * k at load step k (Displacement_BC,
+    linear in the load parameter with dt = 1), horizontal pre-crack of length
+    crack_frac * W centred at crack_center * W."""
+    x, vol = grid2d(nx, nx, h, jitter, seed)
+    W = nx * h
+    ubc = [
+        BC(region="rectangle", x1=-h, x2=W + h, y1=-h, y2=layers * h, direction=[1, 2],
+           time_fn="constant", time_params=[0.0], spatial_fn="constant", spatial_params=[1.0]),
+        BC(region="rectangle", x1=-h, x2=W + h, y1=W - layers * h, y2=W + h, direction=[2],
+           time_fn="linear", time_params=[du], spatial_fn="constant", spatial_params=[1.0]),
+    ]
+    cx, cy = crack_center[0] * W, crack_center[1] * W
+    L = crack_frac * W
+    cracks = [Crack(kind="edge", orientation=1, pb=(cx - 0.5 * L, cy), pt=(cx + 0.5 * L, cy))]
+    return Problem(dim=2, x=x, volume=vol, horizon=ratio * h, mesh_size=h, material=glass_rnp(),
+                   ubc=ubc, cracks=cracks, dt=1.0, steps=100, name=name)
+
+
+def config4(seed=0):
+    """200 x 200 quasi-static plate, horizon 3h, centred 0.2 W pre-crack, 100
+    load steps of 1e-6 m on the top edge, bottom edge fixed."""
+    return qs_plate(200, name="qs_rnp2d_200x200_d3h")
+
+
+def qs_training_geometry(seed, nx=200):
+    """Seeded pre-crack length U[0.1, 0.3] W and centre U[0.35, 0.65]^2 W."""
+    rng = np.random.default_rng(10_000 + seed)
+    frac = float(rng.uniform(0.1, 0.3))
+    c = (float(rng.uniform(0.35, 0.65)), float(rng.uniform(0.35, 0.65)))
+    return qs_plate(nx, crack_frac=frac, crack_center=c, name="qs_seed%d" % seed)

@@ -1,0 +1,38 @@
+// qs_internal.h -- work buffers and launchers of the quasi-static solver.
+#pragma once
+
+#include "fd_internal.h"
+
+namespace nlm {
+
+struct QSWork {
+  double *res;    // residual, DIM per node
+  double *dx;     // Newton correction
+  double *r, *z, *p, *ap;  // CG vectors
+  double *part;   // block partial sums
+  double *sc;     // device scalars
+  double *blk;    // tangent blocks per bond (3 or 6 doubles)
+  double *dblk;   // diagonal blocks per node
+  double *res0;   // force at the previous converged state
+};
+
+// count != NULL: bonds past the critical strain break during the evaluation
+// (RNPBond::getBondEF) and the number broken is added to *count.
+cudaError_t qs_residual(const StepParams &P, const DevPtrs &D, const double *u, double *res,
+                        double *blk, double *dblk, bool assemble, cudaStream_t s,
+                        unsigned long long *count = nullptr);
+cudaError_t qs_dot(const double *a, const double *b, int64_t m, double *part, double *out,
+                   cudaStream_t s);
+cudaError_t qs_cg(const StepParams &P, const DevPtrs &D, const QSWork &W, const double *rhs,
+                  double *dx, double tol, int max_iters, int check_every, int *iters,
+                  cudaStream_t s);
+cudaError_t qs_add(const StepParams &P, const double *du, double *u, cudaStream_t s);
+cudaError_t qs_bcdiff(const StepParams &P, const DevPtrs &D, const double *u,
+                      const double *uprev, double *dx, bool fixed_only, cudaStream_t s);
+cudaError_t qs_spmv(const StepParams &P, const DevPtrs &D, const double *blk, const double *dblk,
+                    const double *x, double *y, double *part, cudaStream_t s);
+cudaError_t qs_sub(int64_t m, const double *a, const double *b, double *out, cudaStream_t s);
+cudaError_t qs_break(const StepParams &P, const DevPtrs &D, const double *u,
+                     unsigned long long *count, cudaStream_t s);
+
+}  // namespace nlm

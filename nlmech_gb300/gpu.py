@@ -256,3 +256,58 @@ class Batch:
         dec = (C.c_int * 8)()
         _check(load().nlm_batch_buckets(self.h, C.byref(nb), nodes, dec))
         return [(nodes[k], dec[k]) for k in range(nb.value)]
+
+
+def qs_params(max_newton=30, tol=1e-8, lin_max_iters=20000, lin_tol=1e-4, break_bonds=True,
+              max_break_rounds=50):
+    return abi.QSParams(max_newton, tol, lin_max_iters, lin_tol, int(break_bonds),
+                        max_break_rounds)
+
+
+class QSModel:
+    """Quasi-static Newton load steps (QuasiStaticModel<RNPBond> on the GPU)."""
+
+    def __init__(self, problem, params=None):
+        self.problem = problem
+        d, self._keep = problem.desc(precision=abi.FP64)
+        self.params = params or qs_params()
+        h = C.c_void_p()
+        _check(load().nlm_qs_create(C.byref(d), C.byref(self.params), C.byref(h)))
+        self.h = h
+        self.n = problem.n
+
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.nlm_qs_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def load_step(self, guess=None):
+        """One load step; guess: (n, 3) start displacement or None (plain)."""
+        st = abi.QSStats()
+        g = None if guess is None else np.ascontiguousarray(guess, dtype=np.float64)
+        _check(load().nlm_qs_load_step(self.h, abi.dptr(g), C.byref(st)))
+        return st.as_dict()
+
+    def state(self):
+        u = np.zeros((self.n, 3))
+        _check(load().nlm_qs_get_state(self.h, abi.dptr(u)))
+        return u
+
+    def nnz(self):
+        v = C.c_int64()
+        _check(load().nlm_qs_num_bonds(self.h, C.byref(v)))
+        return v.value
+
+    def bond_state(self):
+        b = np.zeros(self.nnz(), dtype=np.uint8)
+        _check(load().nlm_qs_get_bond_state(self.h, abi.ptr(b, C.c_uint8)))
+        return b
+
+    def damage(self):
+        phi = np.zeros(self.n, dtype=np.float32)
+        Z = np.zeros(self.n, dtype=np.float32)
+        _check(load().nlm_qs_damage(self.h, abi.ptr(phi, C.c_float), abi.ptr(Z, C.c_float)))
+        return phi, Z

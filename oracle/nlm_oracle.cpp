@@ -1185,4 +1185,321 @@ int orc_qs_get(const orc_qs *h, double *u, double *fout, int64_t *nnz) {
   return NLM_OK;
 }
 
+// ===========================================================================
+// Quasi-static RNPBond (build definition; the reference has QuasiStaticModel
+// for ElasticState only, QuasiStaticModel.cpp:648).  Same load-step / Newton
+// structure as QuasiStaticModel::solver (:526-594): at load step k the
+// Displacement_BC values are applied at time k*dt, the residual is the force
+// density of FDModel::computeForce on free dofs, Newton uses the analytic
+// tangent of RNPBond's bond force with block-Jacobi preconditioned CG, and
+// stops at ||r|| <= tol * ||r(previous-step guess)||.  Bonds over the critical
+// strain break after convergence and the step is solved again.
+
+struct orc_qsr {
+  Model m;
+  int max_newton = 50, lin_max = 10000, break_bonds = 1, max_break_rounds = 50;
+  double tol = 1e-8, lin_tol = 1e-4, dt = 1.;
+  int step = 0;
+  std::vector<uint8_t> fixed;  // dof mask (dim per node)
+};
+
+namespace {
+
+inline bool qsr_breakable(const Model &m, int64_t i, int64_t j) {
+  return m.interior[i] && m.interior[j];
+}
+
+// residual (free dofs) and optionally tangent blocks (3 per bond in 2-D);
+// with update, intact bonds past the critical strain break first
+// (RNPBond::getBondEF, rnpBond.cpp:263-266) and give no force.
+int64_t qsr_residual(orc_qsr *h, const std::vector<double> &u, std::vector<double> &res,
+                     std::vector<double> *blk, std::vector<double> *dblk, bool update = false) {
+  Model &m = h->m;
+  const int dim = m.dim, NB = dim == 2 ? 3 : 6;
+  res.assign((size_t)dim * m.n, 0.);
+  if (blk) {
+    blk->assign((size_t)NB * m.cols.size(), 0.);
+    dblk->assign((size_t)NB * m.n, 0.);
+  }
+  const RNP &p = m.rnp;
+  const double check_up = m.delta + 0.5 * m.h, check_low = m.delta - 0.5 * m.h;
+  int64_t nbroken = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : nbroken)
+  for (int64_t i = 0; i < m.n; i++) {
+    double fi[3] = {0, 0, 0}, di[6] = {0, 0, 0, 0, 0, 0};
+    for (int64_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++) {
+      const int64_t j = m.cols[k];
+      const bool brk = qsr_breakable(m, i, j);
+      if (m.broken[k] && brk) continue;
+      double dx[3], du[3];
+      for (int c = 0; c < 3; c++) {
+        dx[c] = m.x[3 * j + c] - m.x[3 * i + c];
+        du[c] = u[3 * j + c] - u[3 * i + c];
+      }
+      const double rr = dot3(dx, dx), r = std::sqrt(rr);
+      const double S = dot3(dx, du) / rr;
+      double e[3] = {dx[0] / r, dx[1] / r, dx[2] / r};
+      if (update && brk && p.irrev && dGT(std::abs(S), p.fsc * (p.rbar / std::sqrt(r)))) {
+        m.broken[k] = 1;
+        nbroken++;
+        continue;
+      }
+      double volj = m.vol[j];
+      if (dGT(r, check_low)) volj = volj * ((check_up - r) / m.h);
+      const double k0 = p.J.J(r / m.delta) * 4. * p.C * p.beta / p.invF * volj;
+      const double ex = std::exp(-p.beta * r * S * S);
+      const double s = brk ? k0 * S * ex : k0 * S;
+      for (int c = 0; c < dim; c++) fi[c] += s * e[c];
+      if (blk) {
+        const double gp = brk ? k0 * std::max(1. - 2. * p.beta * r * S * S, 0.) * ex / r : k0 / r;
+        double a[6] = {gp * e[0] * e[0], gp * e[1] * e[0], gp * e[1] * e[1],
+                       gp * e[2] * e[0], gp * e[2] * e[1], gp * e[2] * e[2]};
+        for (int c = 0; c < NB; c++) {
+          (*blk)[(size_t)NB * k + c] = a[c];
+          di[c] += a[c];
+        }
+      }
+    }
+    for (int c = 0; c < dim; c++) res[(size_t)dim * i + c] = h->fixed[(size_t)dim * i + c] ? 0. : fi[c];
+    if (blk) {
+      // relative Levenberg term (as the GPU solver)
+      const double reg = 1e-8 * (dim == 2 ? 0.5 * (di[0] + di[2]) : (di[0] + di[2] + di[5]) / 3.);
+      di[0] += reg;
+      di[2] += reg;
+      if (dim == 3) di[5] += reg;
+      for (int c = 0; c < NB; c++) (*dblk)[(size_t)NB * i + c] = di[c];
+    }
+  }
+  return nbroken;
+}
+
+void sym_mul_h(int dim, const double *a, const double *x, double *y) {
+  if (dim == 2) {
+    y[0] = a[0] * x[0] + a[1] * x[1];
+    y[1] = a[1] * x[0] + a[2] * x[1];
+  } else {
+    y[0] = a[0] * x[0] + a[1] * x[1] + a[3] * x[2];
+    y[1] = a[1] * x[0] + a[2] * x[1] + a[4] * x[2];
+    y[2] = a[3] * x[0] + a[4] * x[1] + a[5] * x[2];
+  }
+}
+
+// PCG on (-K) x = b over free dofs, block-Jacobi preconditioner.
+int qsr_cg(orc_qsr *h, const std::vector<double> &blk, const std::vector<double> &dblk,
+           const std::vector<double> &b, std::vector<double> &x) {
+  Model &m = h->m;
+  const int dim = m.dim, NB = dim == 2 ? 3 : 6;
+  const size_t M = (size_t)dim * m.n;
+  auto spmv = [&](const std::vector<double> &v, std::vector<double> &y) {
+    y.assign(M, 0.);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < m.n; i++) {
+      double acc[3] = {0, 0, 0}, t[3];
+      sym_mul_h(dim, &dblk[(size_t)NB * i], &v[(size_t)dim * i], acc);
+      for (int64_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++) {
+        sym_mul_h(dim, &blk[(size_t)NB * k], &v[(size_t)dim * m.cols[k]], t);
+        for (int c = 0; c < dim; c++) acc[c] -= t[c];
+      }
+      for (int c = 0; c < dim; c++) y[(size_t)dim * i + c] = h->fixed[(size_t)dim * i + c] ? 0. : acc[c];
+    }
+  };
+  auto precond = [&](const std::vector<double> &r, std::vector<double> &z) {
+    z.assign(M, 0.);
+    for (int64_t i = 0; i < m.n; i++) {
+      const double *bb = &dblk[(size_t)NB * i];
+      double a[9];
+      if (dim == 2) {
+        a[0] = bb[0]; a[1] = bb[1]; a[2] = bb[1]; a[3] = bb[2];
+      } else {
+        a[0] = bb[0]; a[1] = bb[1]; a[2] = bb[3]; a[3] = bb[1]; a[4] = bb[2];
+        a[5] = bb[4]; a[6] = bb[3]; a[7] = bb[4]; a[8] = bb[5];
+      }
+      for (int c = 0; c < dim; c++)
+        if (h->fixed[(size_t)dim * i + c])
+          for (int q = 0; q < dim; q++) a[c * dim + q] = a[q * dim + c] = (c == q) ? 1. : 0.;
+      double rv[3] = {0, 0, 0};
+      for (int c = 0; c < dim; c++) rv[c] = h->fixed[(size_t)dim * i + c] ? 0. : r[(size_t)dim * i + c];
+      if (dim == 2) {
+        const double det = a[0] * a[3] - a[1] * a[2];
+        if (std::abs(det) > 0.) {
+          z[(size_t)dim * i] = (a[3] * rv[0] - a[1] * rv[1]) / det;
+          z[(size_t)dim * i + 1] = (-a[2] * rv[0] + a[0] * rv[1]) / det;
+        }
+      } else {
+        const double c00 = a[4] * a[8] - a[5] * a[7], c01 = a[5] * a[6] - a[3] * a[8],
+                     c02 = a[3] * a[7] - a[4] * a[6];
+        const double det = a[0] * c00 + a[1] * c01 + a[2] * c02;
+        if (std::abs(det) > 0.) {
+          const double inv[9] = {c00, a[2] * a[7] - a[1] * a[8], a[1] * a[5] - a[2] * a[4],
+                                 c01, a[0] * a[8] - a[2] * a[6], a[2] * a[3] - a[0] * a[5],
+                                 c02, a[1] * a[6] - a[0] * a[7], a[0] * a[4] - a[1] * a[3]};
+          for (int c = 0; c < 3; c++)
+            z[(size_t)dim * i + c] = (inv[3 * c] * rv[0] + inv[3 * c + 1] * rv[1] + inv[3 * c + 2] * rv[2]) / det;
+        }
+      }
+    }
+  };
+  auto dotv = [&](const std::vector<double> &a, const std::vector<double> &c) {
+    double s = 0;
+    for (size_t k = 0; k < M; k++) s += a[k] * c[k];
+    return s;
+  };
+  x.assign(M, 0.);
+  std::vector<double> r = b, z, p, ap;
+  precond(r, z);
+  p = z;
+  double rz = dotv(r, z);
+  const double rr0 = dotv(r, r);
+  if (rr0 == 0.) return 0;
+  int it = 0;
+  while (it < h->lin_max) {
+    spmv(p, ap);
+    const double pap = dotv(p, ap);
+    const double alpha = pap != 0. ? rz / pap : 0.;
+    for (size_t k = 0; k < M; k++) {
+      x[k] += alpha * p[k];
+      r[k] -= alpha * ap[k];
+    }
+    precond(r, z);
+    const double rzn = dotv(r, z);
+    const double beta = rz != 0. ? rzn / rz : 0.;
+    for (size_t k = 0; k < M; k++) p[k] = z[k] + beta * p[k];
+    rz = rzn;
+    it++;
+    if (!(dotv(r, r) > h->lin_tol * h->lin_tol * rr0)) break;
+  }
+  return it;
+}
+
+double qsr_norm(const std::vector<double> &r) {
+  double s = 0;
+  for (double v : r) s += v * v;
+  return std::sqrt(s);
+}
+
+void qsr_newton(orc_qsr *h, double target, orc_qsr_stats *st) {
+  Model &m = h->m;
+  std::vector<double> res, blk, dblk, dx;
+  for (int it = 0;; it++) {
+    const int64_t nb = qsr_residual(h, m.u, res, &blk, &dblk, h->break_bonds != 0);
+    st->broken += nb;
+    if (nb) st->break_rounds++;
+    st->res_final = qsr_norm(res);
+    if (!(st->res_final > target) || it >= h->max_newton) return;
+    st->lin_iters += qsr_cg(h, blk, dblk, res, dx);
+    for (int64_t i = 0; i < m.n; i++)
+      for (int c = 0; c < m.dim; c++) m.u[3 * i + c] += dx[(size_t)m.dim * i + c];
+    st->newton_iters++;
+  }
+}
+
+}  // namespace
+
+int orc_qsr_create(const nlm_fd_desc *d, int max_newton, double tol, int lin_max_iters,
+                   double lin_tol, int break_bonds, int max_break_rounds, orc_qsr **out) {
+  if (!d || !out) return fail(NLM_ERR_INVALID, "null argument");
+  if (d->material.kind != NLM_MAT_RNP_BOND) return fail(NLM_ERR_INVALID, "RNPBond only");
+  auto *h = new orc_qsr();
+  int rc = setup_model(d, true, h->m);
+  if (rc) {
+    delete h;
+    return rc;
+  }
+  h->max_newton = max_newton;
+  h->tol = tol;
+  h->lin_max = lin_max_iters;
+  h->lin_tol = lin_tol;
+  h->break_bonds = break_bonds;
+  h->max_break_rounds = max_break_rounds;
+  h->dt = d->dt;
+  h->fixed.assign((size_t)h->m.dim * h->m.n, 0);
+  for (int64_t i = 0; i < h->m.n; i++)
+    for (int c = 0; c < h->m.dim; c++) h->fixed[(size_t)h->m.dim * i + c] = (h->m.fix[i] >> c) & 1;
+  *out = h;
+  return NLM_OK;
+}
+
+int orc_qsr_destroy(orc_qsr *h) {
+  delete h;
+  return NLM_OK;
+}
+
+// Load step with the displacement-controlled tangent predictor: with K and f
+// at the previous converged state and the boundary increment du_c, the first
+// iterate solves (-K) du = f + K du_c on free dofs; ||f + K du_c|| is the
+// residual scale of the step.  A caller's guess u_g is used instead when the
+// same linear model, ||f + K (u_g - u_prev)||, is not larger.  Newton
+// iterations then run with bond breaking in every residual evaluation.
+int orc_qsr_load_step(orc_qsr *h, const double *guess, orc_qsr_stats *st_out) {
+  Model &m = h->m;
+  const int dim = m.dim, NB = dim == 2 ? 3 : 6;
+  orc_qsr_stats st{};
+  std::vector<double> res0, blk, dblk, dx, vd(3 * m.n, 0.);
+  const std::vector<double> uprev = m.u;
+  qsr_residual(h, m.u, res0, &blk, &dblk);
+  h->step++;
+  const double time = h->step * h->dt;
+  apply_uload(m, time, m.u.data(), vd.data());
+  // f + K d on free dofs, (K d)_i = sum_j A_ij (d_j - d_i)
+  auto linear = [&](const std::vector<double> &ucand, bool fixed_only, std::vector<double> &out) {
+    out = res0;
+    auto d = [&](int64_t a, int c) {
+      if (fixed_only && !h->fixed[(size_t)dim * a + c]) return 0.;
+      return ucand[3 * a + c] - uprev[3 * a + c];
+    };
+    for (int64_t i = 0; i < m.n; i++) {
+      double acc[3] = {0, 0, 0}, t[3], xi[3] = {0, 0, 0};
+      for (int c = 0; c < dim; c++) xi[c] = d(i, c);
+      sym_mul_h(dim, &dblk[(size_t)NB * i], xi, acc);
+      for (int64_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++) {
+        const int64_t j = m.cols[k];
+        double xj[3] = {0, 0, 0};
+        for (int c = 0; c < dim; c++) xj[c] = d(j, c);
+        sym_mul_h(dim, &blk[(size_t)NB * k], xj, t);
+        for (int c = 0; c < dim; c++) acc[c] -= t[c];
+      }
+      for (int c = 0; c < dim; c++)
+        if (!h->fixed[(size_t)dim * i + c]) out[(size_t)dim * i + c] -= acc[c];
+    }
+  };
+  std::vector<double> rhs;
+  linear(m.u, true, rhs);
+  st.res_plain = st.res_start = qsr_norm(rhs);
+  bool use_guess = false;
+  if (guess) {
+    std::vector<double> saved = m.u, rg;
+    for (int64_t k = 0; k < 3 * m.n; k++) m.u[k] = guess[k];
+    apply_uload(m, time, m.u.data(), vd.data());
+    linear(m.u, false, rg);
+    const double ng = qsr_norm(rg);
+    if (ng <= st.res_plain) {
+      use_guess = true;
+      st.used_guess = 1;
+      st.res_start = ng;
+    } else {
+      m.u = saved;
+    }
+  }
+  const double target = h->tol * st.res_plain;
+  if (!use_guess && st.res_plain > 0.) {
+    st.lin_iters += qsr_cg(h, blk, dblk, rhs, dx);
+    for (int64_t i = 0; i < m.n; i++)
+      for (int c = 0; c < dim; c++) m.u[3 * i + c] += dx[(size_t)dim * i + c];
+    st.newton_iters++;
+  }
+  qsr_newton(h, target, &st);
+  if (st_out) *st_out = st;
+  return NLM_OK;
+}
+
+int orc_qsr_get_state(const orc_qsr *h, double *u) {
+  std::copy(h->m.u.begin(), h->m.u.end(), u);
+  return NLM_OK;
+}
+
+int orc_qsr_get_bond_state(const orc_qsr *h, uint8_t *broken) {
+  std::copy(h->m.broken.begin(), h->m.broken.end(), broken);
+  return NLM_OK;
+}
+
 }  // extern "C"

@@ -90,6 +90,20 @@ int orc_qs_solve(orc_qs *h, int nsteps, int *iters, double *final_res);
  * model/util.cpp:49-59) after the final computeForces(true). */
 int orc_qs_get(const orc_qs *h, double *u, double *fout, int64_t *nnz);
 
+/* ---- quasi-static RNPBond (build definition; see nlm_oracle.cpp) ------- */
+typedef struct orc_qsr orc_qsr;
+typedef struct orc_qsr_stats {
+  int newton_iters, lin_iters, break_rounds, used_guess;
+  int64_t broken;
+  double res_plain, res_start, res_final;
+} orc_qsr_stats;
+int orc_qsr_create(const nlm_fd_desc *d, int max_newton, double tol, int lin_max_iters,
+                   double lin_tol, int break_bonds, int max_break_rounds, orc_qsr **out);
+int orc_qsr_destroy(orc_qsr *h);
+int orc_qsr_load_step(orc_qsr *h, const double *guess, orc_qsr_stats *st);
+int orc_qsr_get_state(const orc_qsr *h, double *u);
+int orc_qsr_get_bond_state(const orc_qsr *h, uint8_t *broken);
+
 #ifdef __cplusplus
 }
 #endif

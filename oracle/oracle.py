@@ -199,3 +199,54 @@ class OracleQS:
         nnz = C.c_int64()
         _check(lib().orc_qs_get(self.h, abi.dptr(u), abi.dptr(f), C.byref(nnz)))
         return u, f
+
+
+class QSRStats(C.Structure):
+    _fields_ = [
+        ("newton_iters", C.c_int),
+        ("lin_iters", C.c_int),
+        ("break_rounds", C.c_int),
+        ("used_guess", C.c_int),
+        ("broken", C.c_int64),
+        ("res_plain", C.c_double),
+        ("res_start", C.c_double),
+        ("res_final", C.c_double),
+    ]
+
+
+class OracleQSR:
+    """Quasi-static RNPBond restated on the CPU (same definition as the GPU)."""
+
+    def __init__(self, problem, max_newton=30, tol=1e-8, lin_max_iters=20000, lin_tol=1e-4,
+                 break_bonds=True, max_break_rounds=50):
+        d, self._keep = problem.desc()
+        h = C.c_void_p()
+        _check(lib().orc_qsr_create(C.byref(d), C.c_int(max_newton), C.c_double(tol),
+                                    C.c_int(lin_max_iters), C.c_double(lin_tol),
+                                    C.c_int(int(break_bonds)), C.c_int(max_break_rounds),
+                                    C.byref(h)))
+        self.h = h
+        self.n = problem.n
+        self.problem = problem
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_qsr_destroy(self.h)
+            self.h = None
+
+    def load_step(self, guess=None):
+        st = QSRStats()
+        g = None if guess is None else np.ascontiguousarray(guess, dtype=np.float64)
+        _check(lib().orc_qsr_load_step(self.h, abi.dptr(g), C.byref(st)))
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def state(self):
+        u = np.zeros((self.n, 3))
+        _check(lib().orc_qsr_get_state(self.h, abi.dptr(u)))
+        return u
+
+    def bond_state(self):
+        rp, cols = neighbors(self.problem.x, self.problem.horizon, dim=self.problem.dim)
+        b = np.zeros(len(cols), dtype=np.uint8)
+        _check(lib().orc_qsr_get_bond_state(self.h, abi.ptr(b, C.c_uint8)))
+        return b

@@ -1,0 +1,72 @@
+"""GPU quasi-static Newton (RNPBond) against the oracle's restatement.
+
+Both stop at ||r|| <= 1e-8 ||r(previous-step guess)||; converged states agree
+to well below the displacement scale, and the broken-bond sets match."""
+import numpy as np
+import pytest
+
+from nlmech_gb300 import configs
+
+pytestmark = pytest.mark.gpu
+
+
+def pairs(rowptr, cols, broken):
+    rows = np.repeat(np.arange(len(rowptr) - 1), np.diff(rowptr))
+    sel = broken.astype(bool)
+    return set(zip(rows[sel].tolist(), cols[sel].tolist()))
+
+
+def test_qs_elastic_steps_match_oracle(gpu, oracle):
+    """Below the fracture load: identical algorithm, states equal to ~1e-9."""
+    p = configs.qs_plate(48, h=5e-4, du=4e-8)
+    q = gpu.QSModel(p, gpu.qs_params(lin_tol=1e-6))
+    o = oracle.OracleQSR(p, lin_tol=1e-6)
+    for k in range(6):
+        s = q.load_step()
+        so = o.load_step()
+        assert s["res_final"] <= 1e-8 * s["res_plain"]
+        assert so["res_final"] <= 1e-8 * so["res_plain"]
+        assert s["res_plain"] == pytest.approx(so["res_plain"], rel=1e-9)
+        assert s["newton_iters"] == so["newton_iters"]
+        u, uo = q.state(), o.state()
+        assert np.abs(u - uo).max() <= 1e-9 * np.abs(uo).max()
+
+
+def test_qs_fracture_steps_match_oracle(gpu, oracle):
+    """Crack growth during Newton: converged states and broken-bond sets agree
+    (break decisions at the threshold can flip with summation order)."""
+    p = configs.qs_plate(48, h=5e-4, du=1e-6)
+    prm = dict(max_newton=60)
+    q = gpu.QSModel(p, gpu.qs_params(lin_tol=1e-6, **prm))
+    o = oracle.OracleQSR(p, lin_tol=1e-6, **prm)
+    rowptr, cols = oracle.neighbors(p.x, p.horizon)
+    for k in range(4):
+        s = q.load_step()
+        so = o.load_step()
+        assert s["res_final"] <= 1e-8 * s["res_plain"], (k, s)
+        assert so["res_final"] <= 1e-8 * so["res_plain"], (k, so)
+    bo = pairs(rowptr, cols, o.bond_state())
+    assert len(bo) > 1000
+    assert len(pairs(rowptr, cols, q.bond_state()) ^ bo) <= 0.01 * len(bo)
+    u, uo = q.state(), o.state()
+    assert np.linalg.norm(u - uo) <= 1e-3 * np.linalg.norm(uo)
+
+
+def test_qs_guess_and_fallback(gpu):
+    p = configs.qs_plate(40, h=5e-4, du=2e-6)
+    q = gpu.QSModel(p)
+    q.load_step()
+    u1 = q.state()
+    # a guess far worse than the previous step is rejected
+    s = q.load_step(guess=u1 + 1e-3)
+    assert s["used_guess"] == 0 and s["res_start"] == s["res_plain"]
+    # the converged answer of the same step is accepted and needs no iteration
+    q2 = gpu.QSModel(p)
+    q2.load_step()
+    q2.load_step()
+    u2 = q2.state()
+    q3 = gpu.QSModel(p)
+    q3.load_step()
+    s3 = q3.load_step(guess=u2)
+    assert s3["used_guess"] == 1
+    assert s3["newton_iters"] <= 1

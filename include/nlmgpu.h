@@ -193,6 +193,25 @@ int nlm_set_device(int device);
 int nlm_neighbor_search(int dim, int64_t n, const double *x, double horizon,
                         int64_t *rowptr, int32_t *cols);
 
+/* Same result as nlm_neighbor_search, with no device allocation.  No
+ * counterpart in the reference (it allocates through its std::vector
+ * neighbour lists); this entry serves callers that must not allocate device
+ * memory: a host whose free HBM is already held by a pool allocator, or a run
+ * that rebuilds neighbours while other streams work and cannot take the
+ * device-wide synchronisation that cudaFree implies.  All intermediates live
+ * in one file-scope __device__ array of 22,545,152 bytes; inputs above
+ * n = 65,536 nodes, 262,144 grid cells, 4,194,304 bonds or 512 entries in a
+ * row are rejected with NLM_ERR_INVALID.  The per-cell counters, scatter
+ * cursors and error word of the scratch must start at zero; each call clears
+ * them itself before its first kernel.  Calls that overlap in time on the
+ * same device (two host threads) race on that one array: serialise them.  The
+ * first call on a device looks up the array's address (cudaGetSymbolAddress,
+ * with that device current); make it before any stream capture on that
+ * device.  Works on the calling thread's current device and per-thread
+ * default stream, and returns after the results are on the host. */
+int nlm_neighbor_search_noalloc(int dim, int64_t n, const double *x, double horizon,
+                                int64_t *rowptr, int32_t *cols);
+
 /* ---- explicit finite-difference model (replaces model::FDModel<T>) ----- */
 typedef struct nlm_fd nlm_fd;
 

@@ -29,6 +29,7 @@ UNITS = {
     "es_fp64.cu": ["--fmad=false"],
     "es_fp32.cu": [],
     "qs.cu": [],
+    "noalloc.cu": ["--fmad=false"],
 }
 
 

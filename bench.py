@@ -46,7 +46,10 @@ def parse():
     ap.add_argument("--es-steps", type=int, default=50,
                     help="steps of the 100^3 ElasticState cube (0: skip)")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--decomp", default="auto", choices=["auto", "thread", "thread1", "warp"])
+    ap.add_argument("--qs-steps", type=int, default=100,
+                    help="quasi-static load steps of the learned vs plain warm-start comparison "
+                         "(200 x 200 plate); 0 skips it")
+    ap.add_argument("--decomp", default="auto", choices=["auto", "thread", "thread1", "warp", "tile"])
     ap.add_argument("--workload", default="plate", choices=["plate", "ensemble"],
                     help="plate: 1000x1000 RNPBond plate (headline); ensemble: 256 plates "
                          "of 5k-200k nodes batched, against sequential single-plate runs")
@@ -222,11 +225,12 @@ def run_ours(a):
 
     # ---- FP32-compensated (headline) ----
     dmap = {"auto": abi.DECOMP_AUTO, "thread": abi.DECOMP_THREAD,
-            "thread1": abi.DECOMP_THREAD1, "warp": abi.DECOMP_WARP}
+            "thread1": abi.DECOMP_THREAD1, "warp": abi.DECOMP_WARP, "tile": abi.DECOMP_TILE}
     m = gpu.FDModel(p, precision=abi.FP32C, decomposition=dmap[a.decomp])
     nnz = m.nnz()
     decomp = {1: "thread-per-node, 4-bond groups", 2: "warp-per-node",
-              3: "thread-per-node, 1 bond/iteration"}[m.decomposition()]
+              3: "thread-per-node, 1 bond/iteration",
+              4: "256-node tiles staged in shared memory"}.get(m.decomposition(), "?")
     m.run(a.warmup)
     barrier_sync()
     with ClockSampler(local) as cs:
@@ -239,7 +243,8 @@ def run_ours(a):
     if a.quick:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "quick": True,
-                              "ms_per_step": ms / a.steps, "steps": a.steps}))
+                              "ms_per_step": ms / a.steps, "steps": a.steps,
+                              "decomposition": decomp, "clocks": clocks}))
         return 0
     # per-launch kernel time of the step kernel (separate timed pass)
     m.set_timing(True)
@@ -328,10 +333,32 @@ def run_ours(a):
                      "kernel_ms": kms, "bytes_per_launch": bytes_per_launch},
         "clocks": clocks,
     }
+    if a.qs_steps > 0 and not a.quick:
+        out["qs_warm_start"] = qs_warm_start(a.qs_steps)
     if not a.no_cpu:
         out["cpu_baseline"] = cpu_baseline(a.nx, a.cpu_steps)
     print(json.dumps(out))
     return 0
+
+
+def qs_warm_start(steps):
+    """Quasi-static Newton on the 200 x 200 pre-cracked RNP plate (top edge
+    +1e-6 m per load step, bottom fixed, relative residual 1e-8): plain
+    previous-step start vs the learned BF16 MLP start, wall time of the whole
+    load-step loop including feature building and inference."""
+    from nlmech_gb300 import configs, warmstart as ws
+    if not os.path.exists(ws.WEIGHTS):
+        return {"unavailable": "warm-start weights not found"}
+    z = np.load(ws.WEIGHTS)
+    model = ws.load_model()
+    p = configs.config4()
+    res = ws.evaluate(model, [p], steps, log=lambda *_: None)[p.name]
+    res.update({"workload": "qs_rnp2d_200x200_d3h_precrack0.2W", "load_steps": steps,
+                "tolerance": "||r|| <= 1e-8 ||r0|| every load step",
+                "mlp": "10 -> 128 x 3 -> 2, bf16 GEMMs with fp32 accumulation",
+                "trained_on": "%d load steps of %d seeded pre-crack geometries (held out here)"
+                              % (int(z["steps"]) * len(z["seeds"]), len(z["seeds"]))})
+    return res
 
 
 def run_ensemble(a):

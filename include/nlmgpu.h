@@ -68,7 +68,9 @@ enum nlm_decomposition {
   NLM_DECOMP_THREAD = 1,  /* one thread per node, sliced-ELL bonds taken
                              four at a time                                */
   NLM_DECOMP_WARP = 2,    /* one warp per node, CSR bond storage           */
-  NLM_DECOMP_THREAD1 = 3  /* one thread per node, one bond per iteration   */
+  NLM_DECOMP_THREAD1 = 3, /* one thread per node, one bond per iteration   */
+  NLM_DECOMP_TILE = 4     /* FP32C 2-D: 256-node tiles with their halo staged
+                             in shared memory, 16-bit tile-local bond ids  */
 };
 
 /* Displacement_BC / Force_BC region types (loading/uLoading.cpp:38-46). */
@@ -107,7 +109,7 @@ enum nlm_crack_kind {
 enum nlm_no_fail {
   NLM_NOFAIL_OFF = 0,     /* BaseInterior: every node interior            */
   NLM_NOFAIL_COMPUTE = 1, /* ComputeInterior: bbox minus tolerance        */
-  NLM_NOFAIL_DATA = 2     /* DataInterior: stored flags (all set)         */
+  NLM_NOFAIL_DATA = 2     /* DataInterior: the same flags, stored         */
 };
 
 /* ---- descriptions --------------------------------------------------- */
@@ -309,8 +311,12 @@ typedef struct nlm_qs_params {
   double tol;          /* relative residual tolerance (default 1e-8)         */
   int lin_max_iters;   /* CG iterations per Newton step                      */
   double lin_tol;      /* CG relative tolerance (inexact Newton)             */
-  int break_bonds;     /* 1: staggered bond breaking after convergence       */
-  int max_break_rounds;
+  int break_bonds;     /* 1: bonds past the critical strain break during
+                          every residual evaluation (RNPBond::getBondEF)    */
+  int max_break_rounds;  /* unused (kept for layout compatibility)          */
+  double guess_accept; /* a guess is used only if its linearised residual is
+                          at most guess_accept times that of the plain
+                          start (<= 0: 0.1)                                  */
 } nlm_qs_params;
 
 typedef struct nlm_qs_stats {
@@ -336,6 +342,39 @@ int nlm_qs_get_state(nlm_qs *q, double *u);
 int nlm_qs_get_bond_state(nlm_qs *q, uint8_t *broken);
 int nlm_qs_damage(nlm_qs *q, float *phi, float *Z);
 int nlm_qs_num_bonds(const nlm_qs *q, int64_t *nnz);
+
+/* ---- learned warm start of the quasi-static solver --------------------
+ * No counterpart in the reference (its QuasiStaticModel starts every load
+ * step from the previous displacement).  A per-node MLP
+ *   n_in -> n_hidden (ReLU) x n_layers -> n_out (linear)
+ * predicts the start displacement that nlm_qs_load_step receives as its
+ * guess.  Parameters are FP32 (Adam master copy); every GEMM rounds its
+ * operands to BF16 and accumulates in FP32 on the tensor cores.
+ *
+ * Parameter layout (nlm_mlp_get_params / set_params), for layer l = 0..n_layers
+ * with padded widths d_0 = roundup(n_in, 16), d_1..d_n_layers =
+ * roundup(n_hidden, 16), d_{n_layers+1} = roundup(n_out, 8):
+ *   W_l[d_l][d_{l+1}] row-major (input index major), then b_l[d_{l+1}].
+ * Padding rows and columns are zero and stay zero under training.
+ * x: rows x n_in, y and targets t: rows x n_out, float, host memory. */
+typedef struct nlm_mlp nlm_mlp;
+int nlm_mlp_create(int n_in, int n_hidden, int n_layers, int n_out, uint64_t seed,
+                   nlm_mlp **out);
+int nlm_mlp_destroy(nlm_mlp *h);
+int nlm_mlp_num_params(const nlm_mlp *h, int64_t *count);
+int nlm_mlp_get_params(nlm_mlp *h, float *params);
+int nlm_mlp_set_params(nlm_mlp *h, const float *params);
+/* Inference: y = net(x). */
+int nlm_mlp_forward(nlm_mlp *h, const float *x, int64_t rows, float *y);
+/* Mean squared error over rows x n_out and its gradient (params layout);
+ * loss and grads may be NULL. */
+int nlm_mlp_grad(nlm_mlp *h, const float *x, const float *t, int64_t rows, float *loss,
+                 float *grads);
+/* Upload a training set (kept on the device). */
+int nlm_mlp_set_data(nlm_mlp *h, const float *x, const float *t, int64_t rows);
+/* Minibatch Adam over the uploaded set (reshuffled each epoch from seed);
+ * losses[e] = mean batch loss of epoch e (NULL to skip the readback). */
+int nlm_mlp_train(nlm_mlp *h, int epochs, int batch, float lr, uint64_t seed, float *losses);
 
 #ifdef __cplusplus
 }

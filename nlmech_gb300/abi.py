@@ -29,6 +29,7 @@ DECOMP_AUTO = 0
 DECOMP_THREAD = 1
 DECOMP_WARP = 2
 DECOMP_THREAD1 = 3
+DECOMP_TILE = 4
 # regions
 REGION = {"rectangle": 0, "line": 1, "circle": 2, "torus": 3, "cuboid": 4}
 TIME_FN = {"constant": 0, "linear": 1, "quadratic": 2, "sin": 3,
@@ -138,6 +139,7 @@ class QSParams(C.Structure):
         ("lin_tol", C.c_double),
         ("break_bonds", C.c_int),
         ("max_break_rounds", C.c_int),
+        ("guess_accept", C.c_double),
     ]
 
 

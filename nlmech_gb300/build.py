@@ -30,6 +30,7 @@ UNITS = {
     "es_fp32.cu": [],
     "qs.cu": [],
     "noalloc.cu": ["--fmad=false"],
+    "mlp.cu": [],
 }
 
 

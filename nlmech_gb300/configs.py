@@ -127,16 +127,21 @@ def ensemble(nplates=256, nmin=5000, nmax=200000, seed=0, steps=1000):
 def qs_plate(nx=200, h=5e-4, ratio=3, crack_frac=0.2, crack_center=(0.5, 0.5), du=1e-6,
              layers=3, jitter=0.0, seed=0, name=""):
     """Quasi-static RNPBond plate: nx x nx nodes, bottom `layers` rows fixed in
-    x and y, top rows prescribed u_y = du * k at load step k (Displacement_BC,
-    linear in the load parameter with dt = 1), horizontal pre-crack of length
-    crack_frac * W centred at crack_center * W."""
+    x and y, top rows clamped in x and prescribed u_y = du * k at load step k
+    (Displacement_BC, linear in the load parameter with dt = 1), horizontal
+    pre-crack of length crack_frac * W centred at crack_center * W.  Clamping
+    the top rows in x leaves no rigid-body mode once the crack has separated
+    the plate."""
     x, vol = grid2d(nx, nx, h, jitter, seed)
     W = nx * h
+    top = dict(region="rectangle", x1=-h, x2=W + h, y1=W - layers * h, y2=W + h)
     ubc = [
         BC(region="rectangle", x1=-h, x2=W + h, y1=-h, y2=layers * h, direction=[1, 2],
            time_fn="constant", time_params=[0.0], spatial_fn="constant", spatial_params=[1.0]),
-        BC(region="rectangle", x1=-h, x2=W + h, y1=W - layers * h, y2=W + h, direction=[2],
-           time_fn="linear", time_params=[du], spatial_fn="constant", spatial_params=[1.0]),
+        BC(direction=[1], time_fn="constant", time_params=[0.0], spatial_fn="constant",
+           spatial_params=[1.0], **top),
+        BC(direction=[2], time_fn="linear", time_params=[du], spatial_fn="constant",
+           spatial_params=[1.0], **top),
     ]
     cx, cy = crack_center[0] * W, crack_center[1] * W
     L = crack_frac * W

@@ -234,11 +234,113 @@ __global__ void __launch_bounds__(256)
   if (lane == 0) integrate_node32<DIM, SCHEME>(P, Q, D, T, A, i, fl, uih, uil, fi);
 }
 
+// Tile kernel (2-D): a block stages the positions and displacements of its
+// kTileNodes nodes and of their halo in shared memory with coalesced loads,
+// then runs the thread-per-node bond loop of k_rnp32_thread on the staged
+// copies through 16-bit tile-local neighbour ids (half the bytes of the
+// global ids).  Bond order and arithmetic are those of k_rnp32_thread, so the
+// two decompositions give bit-identical results.
+__device__ __forceinline__ void node_from_f4(const float4 a, Node32<2> &n) {
+  n.xh[0] = a.x;
+  n.xh[1] = a.y;
+  n.xh[2] = 0.f;
+  n.vol = a.z;
+  n.lxy = *reinterpret_cast<const __half2 *>(&a.w);
+  n.lz = __floats2half2_rn(0.f, 0.f);
+}
+
+template <int SCHEME, bool NW1, int OPT>
+__global__ void __launch_bounds__(kTileNodes, 3)
+    k_rnp32_tile(const StepParams P, const Params32 Q, const DevPtrs D, const BCTable T,
+                 const StepArgs A) {
+  __shared__ float4 s_pos[kTileMaxLocal];
+  __shared__ float4 s_u[kTileMaxLocal];
+  __shared__ uint8_t s_fl[(OPT & OPT_NOFAIL) ? kTileMaxLocal : 1];
+  const int64_t t0 = (int64_t)blockIdx.x * kTileNodes;
+  const int h0 = D.tile_hptr[blockIdx.x];
+  const int nh = D.tile_hptr[blockIdx.x + 1] - h0;
+  const int nt = (int)min((int64_t)kTileNodes, P.n - t0);
+  const float4 *ucur = D.u32[A.cur];
+  for (int e = threadIdx.x; e < kTileNodes + nh; e += blockDim.x) {
+    if (e < kTileNodes && e >= nt) continue;
+    const int64_t g = e < kTileNodes ? t0 + e : (int64_t)D.tile_halo[h0 + e - kTileNodes];
+    s_pos[e] = __ldg(D.pos32 + g);
+    s_u[e] = ucur[g];
+    if (OPT & OPT_NOFAIL) s_fl[e] = D.flags[g];
+  }
+  __syncthreads();
+  const int il = threadIdx.x;
+  if (il >= nt) return;
+  const int64_t i = t0 + il;
+  Node32<2> ni;
+  node_from_f4(s_pos[il], ni);
+  float uih[3], uil[3];
+  {
+    const float4 a = s_u[il];
+    uih[0] = a.x; uih[1] = a.y; uih[2] = 0.f;
+    uil[0] = a.z; uil[1] = a.w; uil[2] = 0.f;
+  }
+  const uint8_t fl = D.flags[i];
+  const bool brk_i = !(fl & FLAG_NOFAIL);
+  const int len = D.rowlen[i];
+  const int ng = (len + 3) >> 2;
+  const uint2 *lp = reinterpret_cast<const uint2 *>(D.tile_lidx + D.sell_ptr[i >> 5]) + (i & 31);
+  float fi[3] = {0.f, 0.f, 0.f};
+  uint32_t word = NW1 ? D.bits[i] : 0u;
+  uint32_t nw = 0;
+  uint2 nxt = ng > 0 ? __ldg(lp) : make_uint2(0u, 0u);
+  for (int g = 0; g < ng; g++) {
+    const uint2 cur = nxt;
+    if (g + 1 < ng) nxt = __ldg(lp + 32 * (g + 1));
+    if (!NW1 && (g & 7) == 0) {
+      if (nw) D.bits[(int64_t)((g >> 3) - 1) * P.npad + i] = word | nw;
+      word = D.bits[(int64_t)(g >> 3) * P.npad + i];
+      nw = 0;
+    }
+    const int jl[4] = {(int)(cur.x & 0xffffu), (int)(cur.x >> 16), (int)(cur.y & 0xffffu),
+                       (int)(cur.y >> 16)};
+    Node32<2> nj[4];
+    float ujh[4][3], ujl[4][3];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      node_from_f4(s_pos[jl[q]], nj[q]);
+      const float4 a = s_u[jl[q]];
+      ujh[q][0] = a.x; ujh[q][1] = a.y; ujh[q][2] = 0.f;
+      ujl[q][0] = a.z; ujl[q][1] = a.w; ujl[q][2] = 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int k = 4 * g + q;
+      float dv[3];
+      const bool was = (word >> (k & 31)) & 1u;
+      bool fs = was;
+      bool breakable = true;
+      if (OPT & OPT_NOFAIL) breakable = brk_i && !(s_fl[jl[q]] & FLAG_NOFAIL);
+      const float sc =
+          rnp_bond32<2, OPT>(Q, ni, uih, uil, nj[q], ujh[q], ujl[q], breakable, fs, dv);
+      nw |= (uint32_t)(fs && !was) << (k & 31);
+      fi[0] = fmaf(sc, dv[0], fi[0]);
+      fi[1] = fmaf(sc, dv[1], fi[1]);
+    }
+  }
+  if (nw) D.bits[NW1 ? i : (int64_t)((len - 1) >> 5) * P.npad + i] = word | nw;
+  integrate_node32<2, SCHEME>(P, Q, D, T, A, i, fl, uih, uil, fi);
+}
+
 template <int DIM, int SCHEME, int OPT, bool BATCH>
 static void launch_opt(const StepParams &P, const Params32 &Q, const DevPtrs &D,
                        const BCTable &T, const StepArgs &a, int decomp, cudaStream_t s) {
   const int64_t nodes = a.i1 - a.i0;
   if (nodes <= 0) return;
+  if (DIM == 2 && !BATCH && decomp == NLM_DECOMP_TILE) {
+    // the tile store covers the whole node range [0, n)
+    const unsigned grid = (unsigned)((P.n + kTileNodes - 1) / kTileNodes);
+    if (P.nw1)
+      k_rnp32_tile<SCHEME, true, OPT><<<grid, kTileNodes, 0, s>>>(P, Q, D, T, a);
+    else
+      k_rnp32_tile<SCHEME, false, OPT><<<grid, kTileNodes, 0, s>>>(P, Q, D, T, a);
+    return;
+  }
   if (decomp == NLM_DECOMP_WARP) {
     const int bs = 256;
     const unsigned grid = (unsigned)((nodes * 32 + bs - 1) / bs);

@@ -24,6 +24,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include <cuda_fp16.h>
@@ -328,6 +329,7 @@ struct nlm_fd {
   std::vector<void *> allocs;
   DevPtrs D{};
   int64_t nslices = 0, sell_entries = 0;
+  bool tile_ok = false;  // tile store built (NLM_DECOMP_TILE available)
   // host copies
   std::vector<int> perm;    // internal -> original
   std::vector<int64_t> rowptr;  // internal CSR offsets (host copy)
@@ -386,6 +388,24 @@ bool finite_all(const double *a, int64_t n) {
   for (int64_t i = 0; i < n; i++)
     if (!std::isfinite(a[i])) return false;
   return true;
+}
+
+// No-fail flags (ComputeInterior / DataInterior, interiorFlags.cpp:57-100,
+// :146-185): a node is not interior when it lies within tol of the mesh
+// bounding box.  fe::Mesh::computeBBox (mesh.cpp:311-324) starts both corners
+// at the origin and only widens them, so the box always contains the origin.
+void nofail_flags(const double *x, int64_t n, double tol, std::vector<uint8_t> &interior) {
+  double lo[3] = {0., 0., 0.}, hi[3] = {0., 0., 0.};
+  for (int64_t i = 0; i < n; i++)
+    for (int dd = 0; dd < 3; dd++) {
+      if (hLT(x[3 * i + dd], lo[dd])) lo[dd] = x[3 * i + dd];
+      if (hLT(hi[dd], x[3 * i + dd])) hi[dd] = x[3 * i + dd];
+    }
+  for (int64_t i = 0; i < n; i++) {
+    const double *p = x + 3 * i;
+    interior[i] = !(hLT(p[0], lo[0] + tol) || hLT(p[1], lo[1] + tol) ||
+                    hGT(p[0], hi[0] - tol) || hGT(p[1], hi[1] - tol));
+  }
 }
 
 // RNPBond constants (rnpBond.cpp:23-97, computeParameters :99-189) and the
@@ -494,6 +514,82 @@ int launch_step(nlm_fd *h, const StepArgs &a0) {
   return NLM_OK;
 }
 
+// Tile store of NLM_DECOMP_TILE (FP32C, 2-D): tile t = internal nodes
+// [256 t, 256 t + 256); its halo = the nodes outside the tile its rows
+// reach, ascending.  Each bond stores its neighbour's index in the tile's
+// staged list (tile nodes 0..255, halo from 256), in the sliced layout of
+// sell_cols; padding entries point at the row's own node.  If some tile needs
+// more than kTileMaxLocal staged nodes the store is not built.
+int build_tiles(nlm_fd *h, const int64_t *sell_ptr_dev) {
+  const int64_t n = h->n, nt = (n + kTileNodes - 1) / kTileNodes;
+  std::vector<int> cols(h->nnz);
+  std::vector<int64_t> sptr(h->nslices + 1);
+  NLM_CUDA(cudaMemcpyAsync(cols.data(), h->D.cols, sizeof(int) * h->nnz, cudaMemcpyDeviceToHost,
+                           h->stream));
+  NLM_CUDA(cudaMemcpyAsync(sptr.data(), sell_ptr_dev, sizeof(int64_t) * (h->nslices + 1),
+                           cudaMemcpyDeviceToHost, h->stream));
+  NLM_CUDA(cudaStreamSynchronize(h->stream));
+  const std::vector<int64_t> &rp = h->rowptr;
+  std::vector<std::vector<int>> halo(nt);
+  std::vector<uint16_t> lidx(h->sell_entries + 4, 0);
+  std::vector<int> too_big(1, 0);
+  unsigned nthr = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  auto work = [&](unsigned w) {
+    for (int64_t t = w; t < nt; t += nthr) {
+      const int64_t a = t * kTileNodes, b = std::min(n, a + kTileNodes);
+      std::vector<int> &hl = halo[t];
+      for (int64_t q = rp[a]; q < rp[b]; q++)
+        if (cols[q] < a || cols[q] >= b) hl.push_back(cols[q]);
+      std::sort(hl.begin(), hl.end());
+      hl.erase(std::unique(hl.begin(), hl.end()), hl.end());
+      if (kTileNodes + (int64_t)hl.size() > kTileMaxLocal) {
+        too_big[0] = 1;
+        continue;
+      }
+      for (int64_t i = a; i < b; i++) {
+        const int64_t base = sptr[i >> 5] + 4 * (i & 31);
+        const int64_t len = rp[i + 1] - rp[i];
+        const int64_t wdt = (sptr[(i >> 5) + 1] - sptr[i >> 5]) / 32;
+        for (int64_t k = 0; k < wdt; k++) {
+          int loc = (int)(i - a);
+          if (k < len) {
+            const int j = cols[rp[i] + k];
+            loc = (j >= a && j < b) ? (int)(j - a)
+                                    : kTileNodes + (int)(std::lower_bound(hl.begin(), hl.end(), j) -
+                                                         hl.begin());
+          }
+          lidx[base + (k >> 2) * 128 + (k & 3)] = (uint16_t)loc;
+        }
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (unsigned w = 0; w < nthr; w++) pool.emplace_back(work, w);
+  for (auto &th : pool) th.join();
+  if (too_big[0]) {
+    h->tile_ok = false;
+    return NLM_OK;
+  }
+  std::vector<int> hptr(nt + 1, 0);
+  for (int64_t t = 0; t < nt; t++) hptr[t + 1] = hptr[t] + (int)halo[t].size();
+  std::vector<int> hall(std::max(1, hptr[nt]));
+  for (int64_t t = 0; t < nt; t++) std::copy(halo[t].begin(), halo[t].end(), hall.begin() + hptr[t]);
+  uint16_t *d_l = nullptr;
+  int *d_hp = nullptr, *d_h = nullptr;
+  NLM_CUDA(h->alloc(&d_l, lidx.size()));
+  NLM_CUDA(h->alloc(&d_hp, hptr.size()));
+  NLM_CUDA(h->alloc(&d_h, hall.size()));
+  NLM_CUDA(cudaMemcpyAsync(d_l, lidx.data(), sizeof(uint16_t) * lidx.size(), cudaMemcpyHostToDevice, h->stream));
+  NLM_CUDA(cudaMemcpyAsync(d_hp, hptr.data(), sizeof(int) * hptr.size(), cudaMemcpyHostToDevice, h->stream));
+  NLM_CUDA(cudaMemcpyAsync(d_h, hall.data(), sizeof(int) * hall.size(), cudaMemcpyHostToDevice, h->stream));
+  NLM_CUDA(cudaStreamSynchronize(h->stream));
+  h->D.tile_lidx = d_l;
+  h->D.tile_hptr = d_hp;
+  h->D.tile_halo = d_h;
+  h->tile_ok = true;
+  return NLM_OK;
+}
+
 // Work-decomposition autotuner: time each candidate step kernel on scratch
 // copies of the arrays a step writes and keep the fastest.
 int autotune(nlm_fd *h) {
@@ -522,7 +618,8 @@ int autotune(nlm_fd *h) {
   D.v32[1] = sv1;
   D.f32 = sf;
   D.bits = sb;
-  const int cands[3] = {NLM_DECOMP_THREAD, NLM_DECOMP_THREAD1, NLM_DECOMP_WARP};
+  std::vector<int> cands = {NLM_DECOMP_THREAD, NLM_DECOMP_THREAD1, NLM_DECOMP_WARP};
+  if (h->tile_ok) cands.push_back(NLM_DECOMP_TILE);
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
@@ -783,8 +880,12 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
   }
   h->decomp = d->decomposition == NLM_DECOMP_AUTO ? NLM_DECOMP_THREAD : d->decomposition;
   if (h->decomp != NLM_DECOMP_THREAD && h->decomp != NLM_DECOMP_WARP &&
-      h->decomp != NLM_DECOMP_THREAD1)
+      h->decomp != NLM_DECOMP_THREAD1 && h->decomp != NLM_DECOMP_TILE)
     return bail(fail(NLM_ERR_INVALID, "unknown decomposition"));
+  const bool tile_able = d->precision == NLM_PREC_FP32C && d->material.kind == NLM_MAT_RNP_BOND &&
+                         d->dim == 2;
+  if (h->decomp == NLM_DECOMP_TILE && !tile_able)
+    return bail(fail(NLM_ERR_UNSUPPORTED, "the tile decomposition is for FP32C 2-D RNPBond"));
   const bool want_tune = d->decomposition == NLM_DECOMP_AUTO &&
                          d->precision == NLM_PREC_FP32C && d->material.kind == NLM_MAT_RNP_BOND;
 
@@ -843,6 +944,12 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
   TRY(h->alloc(&bits, (size_t)P.nwords * P.npad));
   TRY(cudaMemsetAsync(bits, 0, sizeof(uint32_t) * P.nwords * P.npad, s));
   D.bits = bits;
+  if (tile_able && (h->decomp == NLM_DECOMP_TILE || want_tune)) {
+    int rc_t = build_tiles(h, st.ptr);
+    if (rc_t) return bail(rc_t);
+    if (h->decomp == NLM_DECOMP_TILE && !h->tile_ok)
+      return bail(fail(NLM_ERR_UNSUPPORTED, "a tile's halo exceeds the tile store limit"));
+  }
   for (int c = 0; c < d->n_cracks; c++) {
     if (d->cracks[c].kind == NLM_CRACK_EDGE && d->dim != 2)
       return bail(fail(NLM_ERR_INVALID, "edge pre-cracks are 2-D only (input.cpp:298-307)"));
@@ -871,20 +978,7 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
     for (int k = 0; k < 4; k++) h->T.t[sidx].p[k] = bc.time_params[k];
   }
   h->T.nsets = d->n_ubc;
-  if (d->no_fail == NLM_NOFAIL_COMPUTE) {
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int64_t i = 0; i < n; i++)
-      for (int dd = 0; dd < 3; dd++) {
-        if (hLT(d->x[3 * i + dd], lo[dd])) lo[dd] = d->x[3 * i + dd];
-        if (hLT(hi[dd], d->x[3 * i + dd])) hi[dd] = d->x[3 * i + dd];
-      }
-    const double tol = d->no_fail_tol;
-    for (int64_t i = 0; i < n; i++) {
-      const double *p = d->x + 3 * i;
-      interior[i] = !(hLT(p[0], lo[0] + tol) || hLT(p[1], lo[1] + tol) ||
-                      hGT(p[0], hi[0] - tol) || hGT(p[1], hi[1] - tol));
-    }
-  }
+  if (d->no_fail != NLM_NOFAIL_OFF) nofail_flags(d->x, n, d->no_fail_tol, interior);
   // force BC items per node, in set order
   std::vector<std::vector<FBCItem>> fitems(n);
   for (int sidx = 0; sidx < d->n_fbc; sidx++) {
@@ -1772,19 +1866,7 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
             wumax[3 * i + dd] = um;
           }
       }
-    if (d.no_fail == NLM_NOFAIL_COMPUTE) {
-      double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-      for (int64_t i = 0; i < d.n_nodes; i++)
-        for (int dd = 0; dd < 3; dd++) {
-          if (hLT(d.x[3 * i + dd], lo[dd])) lo[dd] = d.x[3 * i + dd];
-          if (hLT(hi[dd], d.x[3 * i + dd])) hi[dd] = d.x[3 * i + dd];
-        }
-      for (int64_t i = 0; i < d.n_nodes; i++) {
-        const double *p = d.x + 3 * i;
-        interior[i] = !(hLT(p[0], lo[0] + d.no_fail_tol) || hLT(p[1], lo[1] + d.no_fail_tol) ||
-                        hGT(p[0], hi[0] - d.no_fail_tol) || hGT(p[1], hi[1] - d.no_fail_tol));
-      }
-    }
+    if (d.no_fail != NLM_NOFAIL_OFF) nofail_flags(d.x, d.n_nodes, d.no_fail_tol, interior);
     for (int64_t i = 0; i < d.n_nodes; i++) {
       const int64_t g = b->off[s] + i;
       const int o = b->perm[s][i];
@@ -2204,9 +2286,14 @@ int nlm_qs_create(const nlm_fd_desc *desc, const nlm_qs_params *prm, nlm_qs **ou
   const int64_t n = h->n, m = (int64_t)h->dim * n, nnz = h->nnz;
   const int NB = h->dim == 2 ? 3 : 6;
   cudaError_t e = cudaSuccess;
-  for (double **p : {&q->W.res, &q->W.dx, &q->W.r, &q->W.z, &q->W.p, &q->W.ap, &q->W.res0})
+  for (double **p : {&q->W.res, &q->W.dx, &q->W.r, &q->W.z, &q->W.p, &q->W.p2, &q->W.ap,
+                     &q->W.res0})
     if (e == cudaSuccess) e = q->alloc(p, m);
-  if (e == cudaSuccess) e = q->alloc(&q->W.part, (m + 255) / 256 + 1);
+  if (e == cudaSuccess) e = q->alloc(&q->W.part, std::max<int64_t>((m + 255) / 256 + 1, qs_cg_stride(n)));
+  if (e == cudaSuccess) e = q->alloc(&q->W.cgpart, 3 * qs_cg_stride(n));
+  if (e == cudaSuccess) e = q->alloc(&q->W.cgs, 4);
+  if (e == cudaSuccess) e = q->alloc(&q->W.ticket, 4);
+  if (e == cudaSuccess) e = cudaMemset(q->W.ticket, 0, 4 * sizeof(unsigned));
   if (e == cudaSuccess) e = q->alloc(&q->W.sc, 8);
   if (e == cudaSuccess) e = q->alloc(&q->W.blk, (size_t)NB * (nnz + 1));
   if (e == cudaSuccess) e = q->alloc(&q->W.dblk, (size_t)NB * n);
@@ -2260,7 +2347,13 @@ int nlm_qs_load_step(nlm_qs *q, const double *guess, nlm_qs_stats *stats) {
       return cuda_fail(e, "qs guess");
     double rg = 0.;
     if ((rc = qs_linear_norm(q, &rg))) return rc;
-    if (rg <= st.res_plain) {
+    // the guess must cut the linearised residual of the plain start clearly:
+    // a start no better than the plain one (e.g. the previous state itself)
+    // would put the bonds next to the loaded layer past their critical
+    // strain in the first residual evaluation, which the tangent predictor
+    // of the plain start avoids
+    const double acc = q->prm.guess_accept > 0. ? q->prm.guess_accept : 0.1;
+    if (rg <= acc * st.res_plain) {
       use_guess = true;
       st.used_guess = 1;
       st.res_start = rg;

@@ -46,7 +46,19 @@ struct DevPtrs {
   const int *slice_spec;
   const void *qtab;
   const BCTime *bct;
+  // tile store (FP32C 2-D, NLM_DECOMP_TILE): per bond the index of its
+  // neighbour in the tile's staged node list (the tile's kTileNodes nodes,
+  // then its halo), same slice layout as sell_cols; per tile the halo ids
+  const uint16_t *tile_lidx;
+  const int *tile_hptr;  // tiles + 1
+  const int *tile_halo;
 };
+
+// Tile decomposition: kTileNodes consecutive (Morton-ordered) nodes per
+// block; a tile whose node list (tile + halo) exceeds kTileMaxLocal disables
+// the decomposition for the handle.
+constexpr int kTileNodes = 256;
+constexpr int kTileMaxLocal = 1280;
 
 // Which buffers a launch reads/writes.
 struct StepArgs {

@@ -29,6 +29,8 @@
 // ||f|| <= tol * ||f + K du_c||.  Softening bonds (1 - 2 beta r S^2 < 0)
 // are left out of the tangent so the preconditioned CG matrix stays SPD.
 
+#include <vector>
+
 #include "fd_internal.h"
 #include "qs_internal.h"
 #include "state_io.cuh"
@@ -160,33 +162,45 @@ __device__ __forceinline__ void block_sum(double v, double *part) {
   }
 }
 
-// y = (-K) x on free dofs (fixed dofs give 0), plus the partial sums of x.y.
+// z = (D_i)^-1 r on the free dofs of node i: the diagonal block b (packed
+// symmetric) with the rows and columns of fixed dofs replaced by identity;
+// rv is zero on fixed dofs.  A singular block gives z = 0.
 template <int DIM>
-__global__ void k_qs_spmv(const StepParams P, const DevPtrs D, const double *blk,
-                          const double *dblk, const double *x, double *y, double *part) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  constexpr int NB = DIM == 2 ? 3 : 6;
-  double dot = 0.;
-  if (i < P.n) {
-    const uint8_t fl = D.flags[i];
-    double xi[3] = {0., 0., 0.}, acc[3] = {0., 0., 0.};
-    for (int c = 0; c < DIM; c++) xi[c] = x[DIM * i + c];
-    double t[3];
-    sym_mul(DIM, dblk + NB * i, xi, acc);
-    for (int64_t q = D.rowptr[i]; q < D.rowptr[i + 1]; q++) {
-      const int j = D.cols[q];
-      double xj[3] = {0., 0., 0.};
-      for (int c = 0; c < DIM; c++) xj[c] = x[DIM * j + c];
-      sym_mul(DIM, blk + NB * q, xj, t);
-      for (int c = 0; c < DIM; c++) acc[c] -= t[c];
+__device__ __forceinline__ void block_jacobi(const double *b, uint8_t fl, const double rv[3],
+                                             double zv[3]) {
+  double a[9];
+  if (DIM == 2) {
+    a[0] = b[0]; a[1] = b[1]; a[2] = b[1]; a[3] = b[2];
+  } else {
+    a[0] = b[0]; a[1] = b[1]; a[2] = b[3];
+    a[3] = b[1]; a[4] = b[2]; a[5] = b[4];
+    a[6] = b[3]; a[7] = b[4]; a[8] = b[5];
+  }
+  for (int c = 0; c < DIM; c++)
+    if (fl >> c & 1)
+      for (int q = 0; q < DIM; q++) {
+        a[c * DIM + q] = (c == q) ? 1. : 0.;
+        a[q * DIM + c] = (c == q) ? 1. : 0.;
+      }
+  zv[0] = zv[1] = zv[2] = 0.;
+  if (DIM == 2) {
+    const double det = a[0] * a[3] - a[1] * a[2];
+    if (fabs(det) > 0.) {
+      zv[0] = (a[3] * rv[0] - a[1] * rv[1]) / det;
+      zv[1] = (-a[2] * rv[0] + a[0] * rv[1]) / det;
     }
-    for (int c = 0; c < DIM; c++) {
-      const double yc = (fl >> c & 1) ? 0. : acc[c];
-      y[DIM * i + c] = yc;
-      dot += xi[c] * yc;
+  } else {
+    const double c00 = a[4] * a[8] - a[5] * a[7], c01 = a[5] * a[6] - a[3] * a[8],
+                 c02 = a[3] * a[7] - a[4] * a[6];
+    const double det = a[0] * c00 + a[1] * c01 + a[2] * c02;
+    if (fabs(det) > 0.) {
+      const double inv[9] = {c00, a[2] * a[7] - a[1] * a[8], a[1] * a[5] - a[2] * a[4],
+                             c01, a[0] * a[8] - a[2] * a[6], a[2] * a[3] - a[0] * a[5],
+                             c02, a[1] * a[6] - a[0] * a[7], a[0] * a[4] - a[1] * a[3]};
+      for (int c = 0; c < 3; c++)
+        zv[c] = (inv[3 * c] * rv[0] + inv[3 * c + 1] * rv[1] + inv[3 * c + 2] * rv[2]) / det;
     }
   }
-  block_sum(dot, part);
 }
 
 // Block-Jacobi preconditioner: z_i = (D_i)^-1 r_i on the free dofs of node i
@@ -199,42 +213,9 @@ __global__ void k_qs_precond(const StepParams P, const DevPtrs D, const double *
   double dot = 0.;
   if (i < P.n) {
     const uint8_t fl = D.flags[i];
-    double a[9];  // full block
-    const double *b = dblk + NB * i;
-    if (DIM == 2) {
-      a[0] = b[0]; a[1] = b[1]; a[2] = b[1]; a[3] = b[2];
-    } else {
-      a[0] = b[0]; a[1] = b[1]; a[2] = b[3];
-      a[3] = b[1]; a[4] = b[2]; a[5] = b[4];
-      a[6] = b[3]; a[7] = b[4]; a[8] = b[5];
-    }
-    // remove fixed dofs: identity rows / columns
-    for (int c = 0; c < DIM; c++)
-      if (fl >> c & 1)
-        for (int q = 0; q < DIM; q++) {
-          a[c * DIM + q] = (c == q) ? 1. : 0.;
-          a[q * DIM + c] = (c == q) ? 1. : 0.;
-        }
-    double rv[3] = {0., 0., 0.}, zv[3] = {0., 0., 0.};
+    double rv[3] = {0., 0., 0.}, zv[3];
     for (int c = 0; c < DIM; c++) rv[c] = (fl >> c & 1) ? 0. : r[DIM * i + c];
-    if (DIM == 2) {
-      const double det = a[0] * a[3] - a[1] * a[2];
-      if (fabs(det) > 0.) {
-        zv[0] = (a[3] * rv[0] - a[1] * rv[1]) / det;
-        zv[1] = (-a[2] * rv[0] + a[0] * rv[1]) / det;
-      }
-    } else {
-      const double c00 = a[4] * a[8] - a[5] * a[7], c01 = a[5] * a[6] - a[3] * a[8],
-                   c02 = a[3] * a[7] - a[4] * a[6];
-      const double det = a[0] * c00 + a[1] * c01 + a[2] * c02;
-      if (fabs(det) > 0.) {
-        const double inv[9] = {c00, a[2] * a[7] - a[1] * a[8], a[1] * a[5] - a[2] * a[4],
-                               c01, a[0] * a[8] - a[2] * a[6], a[2] * a[3] - a[0] * a[5],
-                               c02, a[1] * a[6] - a[0] * a[7], a[0] * a[4] - a[1] * a[3]};
-        for (int c = 0; c < 3; c++)
-          zv[c] = (inv[3 * c] * rv[0] + inv[3 * c + 1] * rv[1] + inv[3 * c + 2] * rv[2]) / det;
-      }
-    }
+    block_jacobi<DIM>(dblk + NB * i, fl, rv, zv);
     for (int c = 0; c < DIM; c++) {
       z[DIM * i + c] = zv[c];
       dot += rv[c] * zv[c];
@@ -259,27 +240,189 @@ __global__ void k_qs_sum(const double *part, int64_t n, double *out) {
   }
 }
 
-// x += alpha p, r -= alpha Ap with alpha = rz / pAp (device scalars).
-__global__ void k_qs_axpy(int64_t m, const double *s_rz, const double *s_pap, const double *p,
-                          const double *ap, double *x, double *r) {
-  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (k >= m) return;
-  const double pap = *s_pap;
-  const double alpha = pap != 0. ? *s_rz / pap : 0.;
-  x[k] += alpha * p[k];
-  r[k] -= alpha * ap[k];
+// Final stage of a two-stage sum, done by the last block of a launch to
+// finish (atomic ticket after a memory fence; no block waits for another).
+// The partials are summed in a fixed order (thread t takes t, t + 256, ...,
+// then a fixed tree), so the total does not depend on which block is last.
+// The ticket counter is reset for the next launch.
+__device__ __forceinline__ bool last_block(unsigned *ticket) {
+  __shared__ bool is_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    is_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  return is_last;
 }
 
-// p = z + beta p with beta = rz_new / rz_old; then rz_old = rz_new (thread 0).
-__global__ void k_qs_pupdate(int64_t m, const double *s_rznew, double *s_rzold, const double *z,
-                             double *p) {
-  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (k >= m) return;
-  const double old = *s_rzold;
-  const double beta = old != 0. ? *s_rznew / old : 0.;
-  p[k] = z[k] + beta * p[k];
+__device__ __forceinline__ void finish_sums(int nsum, const double *pa, double *ta,
+                                            const double *pb, double *tb, unsigned *ticket) {
+  __threadfence();
+  const int nb = (int)gridDim.x;
+  double va = 0., vb = 0.;
+  for (int k = threadIdx.x; k < nb; k += blockDim.x) {
+    va += __ldcg(pa + k);
+    if (nsum > 1) vb += __ldcg(pb + k);
+  }
+  __shared__ double sh[2][32];
+  for (int o = 16; o > 0; o >>= 1) {
+    va += __shfl_xor_sync(0xffffffffu, va, o);
+    vb += __shfl_xor_sync(0xffffffffu, vb, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sh[0][w] = va;
+    sh[1][w] = vb;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const bool in = l < (int)(blockDim.x >> 5);
+    va = in ? sh[0][l] : 0.;
+    vb = in ? sh[1][l] : 0.;
+    for (int o = 16; o > 0; o >>= 1) {
+      va += __shfl_xor_sync(0xffffffffu, va, o);
+      vb += __shfl_xor_sync(0xffffffffu, vb, o);
+    }
+    if (l == 0) {
+      *ta = va;
+      if (nsum > 1) *tb = vb;
+      *ticket = 0u;
+    }
+  }
 }
-__global__ void k_qs_copy_scalar(const double *src, double *dst) { *dst = *src; }
+
+// Two block sums at once (partials of block blockIdx.x).
+__device__ __forceinline__ void block_sum2(double va, double vb, double *pa, double *pb) {
+  __shared__ double sh[2][32];
+  for (int o = 16; o > 0; o >>= 1) {
+    va += __shfl_xor_sync(0xffffffffu, va, o);
+    vb += __shfl_xor_sync(0xffffffffu, vb, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sh[0][w] = va;
+    sh[1][w] = vb;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const bool in = l < (int)(blockDim.x >> 5);
+    va = in ? sh[0][l] : 0.;
+    vb = in ? sh[1][l] : 0.;
+    for (int o = 16; o > 0; o >>= 1) {
+      va += __shfl_xor_sync(0xffffffffu, va, o);
+      vb += __shfl_xor_sync(0xffffffffu, vb, o);
+    }
+    if (l == 0) {
+      pa[blockIdx.x] = va;
+      pb[blockIdx.x] = vb;
+    }
+  }
+}
+
+// Lanes per node in the tangent products: a row (about 26 bonds at
+// horizon 3h) is split over kG lanes so that a 40,000-node plate still puts
+// enough warps on every SM to hide the latency of the neighbour gathers.
+constexpr int kG = 8;
+
+// One PCG iteration k in two launches.  Vectors: p_k lives in pbuf[k & 1],
+// rz_k = r_k.z_k as partials in rzp[k & 1].
+// First launch (DIR): beta = rz_k / rz_{k-1}, p_k = z_k + beta p_{k-1} (own
+// rows stored, neighbour values formed on the fly from z and p_{k-1}), Ap_k =
+// (-K) p_k, partials of p_k.Ap_k.  Without DIR: y = (-K) x with x = z.
+template <int DIM, bool DIR>
+__global__ void __launch_bounds__(256) k_cg_dir_spmv(
+    int64_t n, const uint8_t *flags, const int64_t *rowptr, const int *cols, const double *blk,
+    const double *dblk, const double *z, const double *pold, double *pnew, double *ap,
+    const double *rz_cur, const double *rz_prev, double *pap_part, unsigned *ticket,
+    double *pap_total) {
+  double beta = 0.;
+  if (DIR) {
+    const double rzc = *rz_cur, rzo = *rz_prev;
+    beta = rzo != 0. ? rzc / rzo : 0.;
+  }
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t i = t / kG;
+  const int g = (int)(t % kG);
+  constexpr int NB = DIM == 2 ? 3 : 6;
+  double acc[3] = {0., 0., 0.}, tv[3];
+  if (i < n) {
+    const int64_t q1 = rowptr[i + 1];
+    for (int64_t q = rowptr[i] + g; q < q1; q += kG) {
+      const int j = cols[q];
+      double pj[3] = {0., 0., 0.};
+      for (int c = 0; c < DIM; c++)
+        pj[c] = DIR ? z[DIM * j + c] + beta * pold[DIM * j + c] : z[DIM * j + c];
+      sym_mul(DIM, blk + NB * q, pj, tv);
+      for (int c = 0; c < DIM; c++) acc[c] -= tv[c];
+    }
+  }
+  for (int o = kG / 2; o > 0; o >>= 1)
+    for (int c = 0; c < DIM; c++) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+  double dot = 0.;
+  if (i < n && g == 0) {
+    const uint8_t fl = flags[i];
+    double pi[3] = {0., 0., 0.};
+    for (int c = 0; c < DIM; c++) {
+      pi[c] = DIR ? z[DIM * i + c] + beta * pold[DIM * i + c] : z[DIM * i + c];
+      if (DIR) pnew[DIM * i + c] = pi[c];
+    }
+    sym_mul(DIM, dblk + NB * i, pi, tv);
+    for (int c = 0; c < DIM; c++) {
+      const double yc = (fl >> c & 1) ? 0. : acc[c] + tv[c];
+      ap[DIM * i + c] = yc;
+      dot += pi[c] * yc;
+    }
+  }
+  block_sum(dot, pap_part);
+  if (DIR && last_block(ticket)) finish_sums(1, pap_part, pap_total, nullptr, nullptr, ticket);
+}
+
+static unsigned grp_blocks(int64_t n) { return (unsigned)((n * kG + 255) / 256); }
+
+int64_t qs_cg_stride(int64_t n) { return (int64_t)grp_blocks(n) + 2; }
+
+// Second launch: alpha = rz_k / p_k.Ap_k, x += alpha p_k, r -= alpha Ap_k,
+// z = (D_i)^-1 r (block Jacobi, fixed dofs removed), partials of
+// rz_{k+1} = r.z and of r.r.
+template <int DIM>
+__global__ void k_cg_update(int64_t n, const uint8_t *flags, const double *dblk,
+                            const double *p, const double *ap, double *x, double *r, double *z,
+                            const double *rz_cur, const double *pap_total, double *rz_part,
+                            double *rr_part, unsigned *ticket, double *rz_next,
+                            double *rr_total) {
+  const double rzc = *rz_cur, pap = *pap_total;
+  const double alpha = pap != 0. ? rzc / pap : 0.;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  constexpr int NB = DIM == 2 ? 3 : 6;
+  double drz = 0., drr = 0.;
+  if (i < n) {
+    const uint8_t fl = flags[i];
+    double rv[3] = {0., 0., 0.}, zv[3] = {0., 0., 0.};
+    for (int c = 0; c < DIM; c++) {
+      const int64_t k = DIM * i + c;
+      x[k] += alpha * p[k];
+      const double rk = r[k] - alpha * ap[k];
+      r[k] = rk;
+      drr += rk * rk;
+      rv[c] = (fl >> c & 1) ? 0. : rk;
+    }
+    block_jacobi<DIM>(dblk + NB * i, fl, rv, zv);
+    for (int c = 0; c < DIM; c++) {
+      z[DIM * i + c] = zv[c];
+      drz += rv[c] * zv[c];
+    }
+  }
+  block_sum2(drz, drr, rz_part, rr_part);
+  if (last_block(ticket)) finish_sums(2, rz_part, rz_next, rr_part, rr_total, ticket);
+}
+
+__global__ void k_cg_seed(double *rz_prev, double *pold, int64_t m) {
+  // rz_{-1} = 1 and p_{-1} = 0 so that p_0 = z_0
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k < m) pold[k] = 0.;
+  if (k == 0) *rz_prev = 1.;
+}
 
 // Bonds of the converged state that exceed the critical strain break.
 template <int DIM>
@@ -370,21 +513,23 @@ cudaError_t qs_cg(const StepParams &P, const DevPtrs &D, const QSWork &W, const 
                   cudaStream_t s) {
   const int dim = P.dim;
   const int64_t m = (int64_t)dim * P.n;
-  const unsigned gn = qblk(P.n), gm = qblk(m);
+  const unsigned gn = qblk(P.n), gg = grp_blocks(P.n);
+  const int64_t stride = qs_cg_stride(P.n);
+  // partials: pAp (K1 blocks), rz and r.r (K2 blocks); totals on the device:
+  // rz_k in tot[k & 1], pAp in tot[2], r.r in tot[3]
+  double *pap_p = W.cgpart, *rz_p = W.cgpart + stride, *rr_p = W.cgpart + 2 * stride;
+  double *tot = W.cgs;
+  double *pbuf[2] = {W.p, W.p2};
   cudaError_t e;
-  // x = 0, r = rhs, z = M^-1 r, p = z
   if ((e = cudaMemsetAsync(dx, 0, sizeof(double) * m, s))) return e;
   if ((e = cudaMemcpyAsync(W.r, rhs, sizeof(double) * m, cudaMemcpyDeviceToDevice, s))) return e;
-  auto precond = [&]() {
-    if (dim == 2)
-      k_qs_precond<2><<<gn, 256, 0, s>>>(P, D, W.dblk, W.r, W.z, W.part);
-    else
-      k_qs_precond<3><<<gn, 256, 0, s>>>(P, D, W.dblk, W.r, W.z, W.part);
-    k_qs_sum<<<1, 256, 0, s>>>(W.part, gn, W.sc + 2);
-  };
-  precond();
-  k_qs_copy_scalar<<<1, 1, 0, s>>>(W.sc + 2, W.sc + 0);
-  if ((e = cudaMemcpyAsync(W.p, W.z, sizeof(double) * m, cudaMemcpyDeviceToDevice, s))) return e;
+  // z_0 = M^-1 r_0 and rz_0; rz_{-1} = 1, p_{-1} = 0
+  if (dim == 2)
+    k_qs_precond<2><<<gn, 256, 0, s>>>(P, D, W.dblk, W.r, W.z, rz_p);
+  else
+    k_qs_precond<3><<<gn, 256, 0, s>>>(P, D, W.dblk, W.r, W.z, rz_p);
+  k_qs_sum<<<1, 256, 0, s>>>(rz_p, gn, tot + 0);
+  k_cg_seed<<<qblk(m), 256, 0, s>>>(tot + 1, pbuf[1], m);
   double rr0 = 0.;
   if ((e = qs_dot(W.r, W.r, m, W.part, W.sc + 3, s))) return e;
   if ((e = cudaMemcpyAsync(&rr0, W.sc + 3, sizeof(double), cudaMemcpyDeviceToHost, s))) return e;
@@ -397,19 +542,28 @@ cudaError_t qs_cg(const StepParams &P, const DevPtrs &D, const QSWork &W, const 
   }
   while (it < max_iters) {
     for (int q = 0; q < check_every && it < max_iters; q++, it++) {
-      if (dim == 2)
-        k_qs_spmv<2><<<gn, 256, 0, s>>>(P, D, W.blk, W.dblk, W.p, W.ap, W.part);
-      else
-        k_qs_spmv<3><<<gn, 256, 0, s>>>(P, D, W.blk, W.dblk, W.p, W.ap, W.part);
-      k_qs_sum<<<1, 256, 0, s>>>(W.part, gn, W.sc + 1);
-      k_qs_axpy<<<gm, 256, 0, s>>>(m, W.sc + 0, W.sc + 1, W.p, W.ap, dx, W.r);
-      precond();
-      k_qs_pupdate<<<gm, 256, 0, s>>>(m, W.sc + 2, W.sc + 0, W.z, W.p);
-      k_qs_copy_scalar<<<1, 1, 0, s>>>(W.sc + 2, W.sc + 0);
+      const int cur = it & 1, prv = cur ^ 1;
+      if (dim == 2) {
+        k_cg_dir_spmv<2, true><<<gg, 256, 0, s>>>(P.n, D.flags, D.rowptr, D.cols, W.blk,
+                                                  W.dblk, W.z, pbuf[prv], pbuf[cur], W.ap,
+                                                  tot + cur, tot + prv, pap_p, W.ticket,
+                                                  tot + 2);
+        k_cg_update<2><<<gn, 256, 0, s>>>(P.n, D.flags, W.dblk, pbuf[cur], W.ap, dx, W.r, W.z,
+                                          tot + cur, tot + 2, rz_p, rr_p, W.ticket + 1,
+                                          tot + prv, tot + 3);
+      } else {
+        k_cg_dir_spmv<3, true><<<gg, 256, 0, s>>>(P.n, D.flags, D.rowptr, D.cols, W.blk,
+                                                  W.dblk, W.z, pbuf[prv], pbuf[cur], W.ap,
+                                                  tot + cur, tot + prv, pap_p, W.ticket,
+                                                  tot + 2);
+        k_cg_update<3><<<gn, 256, 0, s>>>(P.n, D.flags, W.dblk, pbuf[cur], W.ap, dx, W.r, W.z,
+                                          tot + cur, tot + 2, rz_p, rr_p, W.ticket + 1,
+                                          tot + prv, tot + 3);
+      }
     }
+    if ((e = cudaGetLastError())) return e;
     double rr = 0.;
-    if ((e = qs_dot(W.r, W.r, m, W.part, W.sc + 3, s))) return e;
-    if ((e = cudaMemcpyAsync(&rr, W.sc + 3, sizeof(double), cudaMemcpyDeviceToHost, s))) return e;
+    if ((e = cudaMemcpyAsync(&rr, tot + 3, sizeof(double), cudaMemcpyDeviceToHost, s))) return e;
     if ((e = cudaStreamSynchronize(s))) return e;
     if (!(rr > target)) break;
   }
@@ -444,10 +598,15 @@ cudaError_t qs_bcdiff(const StepParams &P, const DevPtrs &D, const double *u,
 
 cudaError_t qs_spmv(const StepParams &P, const DevPtrs &D, const double *blk, const double *dblk,
                     const double *x, double *y, double *part, cudaStream_t s) {
+  // part: grp_blocks(n) partials of x.y
   if (P.dim == 2)
-    k_qs_spmv<2><<<qblk(P.n), 256, 0, s>>>(P, D, blk, dblk, x, y, part);
+    k_cg_dir_spmv<2, false><<<grp_blocks(P.n), 256, 0, s>>>(
+        P.n, D.flags, D.rowptr, D.cols, blk, dblk, x, nullptr, nullptr, y, nullptr, nullptr,
+        part, nullptr, nullptr);
   else
-    k_qs_spmv<3><<<qblk(P.n), 256, 0, s>>>(P, D, blk, dblk, x, y, part);
+    k_cg_dir_spmv<3, false><<<grp_blocks(P.n), 256, 0, s>>>(
+        P.n, D.flags, D.rowptr, D.cols, blk, dblk, x, nullptr, nullptr, y, nullptr, nullptr,
+        part, nullptr, nullptr);
   return cudaGetLastError();
 }
 

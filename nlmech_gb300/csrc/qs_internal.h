@@ -9,6 +9,10 @@ struct QSWork {
   double *res;    // residual, DIM per node
   double *dx;     // Newton correction
   double *r, *z, *p, *ap;  // CG vectors
+  double *p2;     // second search-direction buffer (iteration parity)
+  double *cgpart; // CG partial sums: 3 arrays of qs_cg_stride(n) entries
+  double *cgs;    // CG totals on the device (4)
+  unsigned *ticket;  // last-block tickets of the two CG launches (start at 0)
   double *part;   // block partial sums
   double *sc;     // device scalars
   double *blk;    // tangent blocks per bond (3 or 6 doubles)
@@ -26,6 +30,8 @@ cudaError_t qs_dot(const double *a, const double *b, int64_t m, double *part, do
 cudaError_t qs_cg(const StepParams &P, const DevPtrs &D, const QSWork &W, const double *rhs,
                   double *dx, double tol, int max_iters, int check_every, int *iters,
                   cudaStream_t s);
+// Entries per partial-sum array of the CG (4 arrays live in QSWork::cgpart).
+int64_t qs_cg_stride(int64_t n);
 cudaError_t qs_add(const StepParams &P, const double *du, double *u, cudaStream_t s);
 cudaError_t qs_bcdiff(const StepParams &P, const DevPtrs &D, const double *u,
                       const double *uprev, double *dx, bool fixed_only, cudaStream_t s);

@@ -259,9 +259,9 @@ class Batch:
 
 
 def qs_params(max_newton=30, tol=1e-8, lin_max_iters=20000, lin_tol=1e-4, break_bonds=True,
-              max_break_rounds=50):
+              max_break_rounds=50, guess_accept=0.1):
     return abi.QSParams(max_newton, tol, lin_max_iters, lin_tol, int(break_bonds),
-                        max_break_rounds)
+                        max_break_rounds, guess_accept)
 
 
 class QSModel:
@@ -311,3 +311,77 @@ class QSModel:
         Z = np.zeros(self.n, dtype=np.float32)
         _check(load().nlm_qs_damage(self.h, abi.ptr(phi, C.c_float), abi.ptr(Z, C.c_float)))
         return phi, Z
+
+
+def mlp_layout(n_in, n_hidden, n_layers, n_out):
+    """[(d_in, d_out, w_offset, b_offset)] of the nlm_mlp parameter vector."""
+    r16 = lambda v: (v + 15) // 16 * 16
+    dims = [r16(n_in)] + [r16(n_hidden)] * n_layers + [(n_out + 7) // 8 * 8]
+    out, off = [], 0
+    for l in range(n_layers + 1):
+        di, do = dims[l], dims[l + 1]
+        out.append((di, do, off, off + di * do))
+        off += di * do + do
+    return out
+
+
+class MLP:
+    """Per-node MLP with BF16 tensor-core GEMMs (nlm_mlp_*)."""
+
+    def __init__(self, n_in=10, n_hidden=128, n_layers=3, n_out=2, seed=0):
+        self.shape = (n_in, n_hidden, n_layers, n_out)
+        h = C.c_void_p()
+        _check(load().nlm_mlp_create(C.c_int(n_in), C.c_int(n_hidden), C.c_int(n_layers),
+                                     C.c_int(n_out), C.c_uint64(seed), C.byref(h)))
+        self.h = h
+        c = C.c_int64()
+        _check(load().nlm_mlp_num_params(self.h, C.byref(c)))
+        self.nparams = c.value
+        self.layout = mlp_layout(*self.shape)
+
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.nlm_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def params(self):
+        p = np.zeros(self.nparams, dtype=np.float32)
+        _check(load().nlm_mlp_get_params(self.h, abi.ptr(p, C.c_float)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.nparams
+        _check(load().nlm_mlp_set_params(self.h, abi.ptr(p, C.c_float)))
+
+    def forward(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.zeros((x.shape[0], self.shape[3]), dtype=np.float32)
+        _check(load().nlm_mlp_forward(self.h, abi.ptr(x, C.c_float), C.c_int64(x.shape[0]),
+                                      abi.ptr(y, C.c_float)))
+        return y
+
+    def grad(self, x, t):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        g = np.zeros(self.nparams, dtype=np.float32)
+        loss = C.c_float()
+        _check(load().nlm_mlp_grad(self.h, abi.ptr(x, C.c_float), abi.ptr(t, C.c_float),
+                                   C.c_int64(x.shape[0]), C.byref(loss), abi.ptr(g, C.c_float)))
+        return loss.value, g
+
+    def set_data(self, x, t):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        _check(load().nlm_mlp_set_data(self.h, abi.ptr(x, C.c_float), abi.ptr(t, C.c_float),
+                                       C.c_int64(x.shape[0])))
+
+    def train(self, epochs, batch=4096, lr=1e-3, seed=0, losses=True):
+        out = np.zeros(max(epochs, 1), dtype=np.float32)
+        _check(load().nlm_mlp_train(self.h, C.c_int(epochs), C.c_int(batch), C.c_float(lr),
+                                    C.c_uint64(seed),
+                                    abi.ptr(out, C.c_float) if losses else None))
+        return out[:epochs]

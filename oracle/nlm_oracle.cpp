@@ -480,8 +480,11 @@ int setup_model(const nlm_fd_desc *d, bool grid, Model &m) {
   }
   // interior flags (interiorFlags.cpp:27-100, 121-191)
   m.interior.assign(m.n, 1);
-  if (d->no_fail == NLM_NOFAIL_COMPUTE && m.n > 0) {
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  if (d->no_fail != NLM_NOFAIL_OFF && m.n > 0) {
+    // fe::Mesh::computeBBox (mesh.cpp:311-324): both corners start at the
+    // origin; DataInterior (:146-185) stores the same flags ComputeInterior
+    // computes
+    double lo[3] = {0., 0., 0.}, hi[3] = {0., 0., 0.};
     for (int64_t i = 0; i < m.n; i++)  // fe::Mesh bounding box
       for (int dd = 0; dd < 3; dd++) {
         if (dLT(m.x[3 * i + dd], lo[dd])) lo[dd] = m.x[3 * i + dd];
@@ -1472,7 +1475,7 @@ int orc_qsr_load_step(orc_qsr *h, const double *guess, orc_qsr_stats *st_out) {
     apply_uload(m, time, m.u.data(), vd.data());
     linear(m.u, false, rg);
     const double ng = qsr_norm(rg);
-    if (ng <= st.res_plain) {
+    if (ng <= 0.1 * st.res_plain) {  // guess_accept = 0.1 (nlm_qs_params default)
       use_guess = true;
       st.used_guess = 1;
       st.res_start = ng;

@@ -250,3 +250,100 @@ class OracleQSR:
         b = np.zeros(len(cols), dtype=np.uint8)
         _check(lib().orc_qsr_get_bond_state(self.h, abi.ptr(b, C.c_uint8)))
         return b
+
+
+# ---- the reference's own RNPBond sources (oracle/refshim) -------------------
+REF_TREE = os.environ.get("NLMECH_REFERENCE", "/root/reference")
+REF_LIB = os.path.join(HERE, "_ref", "libref_rnp.so")
+_ref = None
+
+
+def refshim_available():
+    """True if libref_rnp.so exists or the reference tree is here to build it."""
+    return os.path.exists(REF_LIB) or os.path.isdir(os.path.join(REF_TREE, "src"))
+
+
+def build_refshim():
+    """Compile the reference's RNPBond sources with oracle/refshim/Makefile."""
+    if not os.path.isdir(os.path.join(REF_TREE, "src")):
+        if os.path.exists(REF_LIB):
+            return REF_LIB
+        raise RuntimeError("reference tree not found at %s" % REF_TREE)
+    subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(HERE, "refshim"),
+                           "REF=" + REF_TREE])
+    return REF_LIB
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        build_refshim()
+        L = C.CDLL(REF_LIB)
+        L.ref_rnp_last_error.restype = C.c_char_p
+        _ref = L
+    return _ref
+
+
+class RefRNP:
+    """The reference's Neighbor, Fracture, InteriorFlags, ULoading/FLoading
+    and RNPBond::getBondEF driven through FDModel's velocity-Verlet loop."""
+
+    def __init__(self, problem):
+        d, self._keep = problem.desc()
+        h = C.c_void_p()
+        self._chk(ref_lib().ref_rnp_create(C.byref(d), C.byref(h)))
+        self.h = h
+        self.n = problem.n
+
+    @staticmethod
+    def _chk(rc):
+        if rc != 0:
+            raise RuntimeError("refshim error: %s" % ref_lib().ref_rnp_last_error().decode())
+
+    def __del__(self):
+        if getattr(self, "h", None) and _ref is not None:
+            _ref.ref_rnp_destroy(self.h)
+            self.h = None
+
+    def nnz(self):
+        v = C.c_int64()
+        self._chk(ref_lib().ref_rnp_num_bonds(self.h, C.byref(v)))
+        return v.value
+
+    def neighbors(self):
+        rowptr = np.zeros(self.n + 1, dtype=np.int64)
+        cols = np.zeros(self.nnz(), dtype=np.int32)
+        self._chk(ref_lib().ref_rnp_get_neighbors(self.h, abi.ptr(rowptr, C.c_int64),
+                                                  abi.ptr(cols, C.c_int32)))
+        return rowptr, cols
+
+    def bond_state(self):
+        b = np.zeros(self.nnz(), dtype=np.uint8)
+        self._chk(ref_lib().ref_rnp_get_bond_state(self.h, abi.ptr(b, C.c_uint8)))
+        return b
+
+    def fixity(self):
+        f = np.zeros(self.n, dtype=np.uint8)
+        self._chk(ref_lib().ref_rnp_get_fixity(self.h, abi.ptr(f, C.c_uint8)))
+        return f
+
+    def run(self, nsteps):
+        self._chk(ref_lib().ref_rnp_run(self.h, C.c_int64(nsteps)))
+
+    def state(self):
+        u = np.zeros((self.n, 3))
+        v = np.zeros((self.n, 3))
+        f = np.zeros((self.n, 3))
+        self._chk(ref_lib().ref_rnp_get_state(self.h, abi.dptr(u), abi.dptr(v), abi.dptr(f)))
+        return u, v, f
+
+    def time(self):
+        t = C.c_double()
+        n = C.c_int64()
+        self._chk(ref_lib().ref_rnp_get_time(self.h, C.byref(t), C.byref(n)))
+        return t.value, n.value
+
+    def sc(self, r):
+        v = C.c_double()
+        self._chk(ref_lib().ref_rnp_sc(self.h, C.c_double(r), C.byref(v)))
+        return v.value

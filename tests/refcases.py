@@ -1,0 +1,56 @@
+"""Problems shared by the refshim tests and the reference golden fixtures."""
+import numpy as np
+
+from nlmech_gb300 import abi, configs
+from nlmech_gb300.decks import BC
+
+
+def fracture_plate():
+    """48 x 48 plate, horizon 3h, 12 mm pre-crack, +-0.5 m/s: the crack grows
+    within 300 steps."""
+    return configs.rnp_plate(48, 1e-3, 3, 0.012, 0.5, 2e-8, 300, seed=7)
+
+
+def loads_nofail_plate():
+    """Force BCs (linear and sin in time, constant and linear_y in space), a
+    sin-in-time displacement BC, a computed no-fail layer and the linear
+    influence function."""
+    p = configs.rnp_plate(40, 1e-3, 3, 0.01, 0.3, 2e-8, 200, seed=11)
+    p.material.influence_type = 1
+    p.material.influence_params = []
+    p.fbc = [BC(region="rectangle", x1=0.0, x2=0.004, y1=0.0, y2=0.04, direction=[1],
+                time_fn="linear", time_params=[1.0], spatial_fn="constant",
+                spatial_params=[-2e12]),
+             BC(region="rectangle", x1=0.0, x2=0.002, y1=0.0, y2=0.04, direction=[1, 2],
+                time_fn="sin", time_params=[1.0, 2e4], spatial_fn="linear_y",
+                spatial_params=[1e14])]
+    p.ubc.append(BC(region="rectangle", x1=0.036, x2=0.041, y1=0.01, y2=0.03, direction=[1],
+                    time_fn="sin", time_params=[1e-7, 5e4], spatial_fn="constant",
+                    spatial_params=[1.0]))
+    p.no_fail = abi.NOFAIL_COMPUTE
+    p.no_fail_tol = 2e-3
+    return p
+
+
+def cube3d(n=12, seed=5):
+    """3-D RNPBond cube n^3 (h = 1 mm, horizon 3h), no displacement BC,
+    seeded random initial velocities of +-0.5 m/s in every direction."""
+    x, vol = configs.grid3d(n, n, n, 1e-3, seed=seed)
+    p = configs.rnp_plate(8, 1e-3, 3, 0.0, 0.1, 2e-8, 100)
+    p.dim = 3
+    p.x, p.volume = x, vol
+    p.horizon = 3e-3
+    p.cracks = []
+    p.ubc = []
+    rng = np.random.default_rng(seed)
+    p.v0 = rng.uniform(-0.5, 0.5, size=(x.shape[0], 3))
+    return p
+
+
+# name -> (problem, Verlet steps) of the committed reference outputs
+# (tests/golden/rnp_ref_<name>.npz)
+GOLDEN_CASES = {
+    "fracture_plate": (fracture_plate, 300),
+    "loads_nofail_plate": (loads_nofail_plate, 200),
+    "cube3d": (cube3d, 100),
+}

@@ -60,6 +60,11 @@ def test_qs_guess_and_fallback(gpu):
     # a guess far worse than the previous step is rejected
     s = q.load_step(guess=u1 + 1e-3)
     assert s["used_guess"] == 0 and s["res_start"] == s["res_plain"]
+    # so is one no better than the plain start (the previous state itself)
+    q4 = gpu.QSModel(p)
+    q4.load_step()
+    s4 = q4.load_step(guess=q4.state())
+    assert s4["used_guess"] == 0
     # the converged answer of the same step is accepted and needs no iteration
     q2 = gpu.QSModel(p)
     q2.load_step()

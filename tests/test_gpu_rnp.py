@@ -178,7 +178,8 @@ def test_fp32c_config0_error(gpu, oracle):
     uo, vo, fo = o.state()
     rowptr, cols = o.neighbors()
     bo = bonds_as_pairs(rowptr, cols, o.bond_state())
-    for dec in (abi.DECOMP_THREAD, abi.DECOMP_THREAD1, abi.DECOMP_WARP, abi.DECOMP_AUTO):
+    for dec in (abi.DECOMP_THREAD, abi.DECOMP_THREAD1, abi.DECOMP_WARP, abi.DECOMP_TILE,
+                abi.DECOMP_AUTO):
         m = gpu.FDModel(p, precision=abi.FP32C, decomposition=dec)
         m.run(1000)
         u, v, f = m.state()
@@ -220,3 +221,23 @@ def test_runs_are_deterministic(gpu):
             r.append(m.state() + (m.bond_state(),))
         for a, b in zip(r[0], r[1]):
             assert np.array_equal(a, b)
+
+
+def test_tile_decomposition_bit_identical_to_thread(gpu):
+    """The tile kernel runs the thread kernel's bond loop on staged copies:
+    same bond order, same arithmetic, bit-identical state."""
+    for p in (configs.config0(), configs.rnp_plate(48, 1e-3, 3, 0.012, 0.5, 2e-8, 300, seed=7)):
+        a = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_THREAD)
+        b = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_TILE)
+        assert b.decomposition() == abi.DECOMP_TILE
+        a.run(300)
+        b.run(300)
+        for x, y in zip(a.state(), b.state()):
+            assert np.array_equal(x, y)
+        assert np.array_equal(a.bond_state(), b.bond_state())
+
+
+def test_tile_decomposition_rejected_where_unsupported(gpu):
+    p = configs.config0()
+    with pytest.raises(gpu.NLMError):
+        gpu.FDModel(p, precision=abi.FP64, decomposition=abi.DECOMP_TILE)

@@ -152,6 +152,9 @@ typedef struct nlm_material {
   double bond_params[2];    /* C, beta when not computed from classical    */
   double es_sc;             /* ElasticState critical stretch; <= 0: no breaking */
   int es_ref_compat;        /* 1: keep the reference's 3-D e_d = 0          */
+  int apply_contact;        /* No_Penetration: normal contact force between
+                               the nodes of a broken bond (rnpBond.cpp:79-88,
+                               :281-291); explicit single-model runs only    */
 } nlm_material;
 
 typedef struct nlm_fd_desc {
@@ -338,6 +341,13 @@ int nlm_qs_destroy(nlm_qs *q);
  * from, or NULL for the plain previous-step guess; a guess whose residual
  * exceeds the plain guess's is replaced by the plain guess. */
 int nlm_qs_load_step(nlm_qs *q, const double *guess, nlm_qs_stats *stats);
+/* Same with n_cand candidate starts (n_cand x 3n, Point3 layout): each is
+ * judged by the linear model of the residual at the previous converged
+ * state and the best is used if its linearised residual is at most
+ * guess_accept times that of the plain start; stats->used_guess is then the
+ * 1-based index of the chosen candidate (0: plain start). */
+int nlm_qs_load_step_candidates(nlm_qs *q, const double *guesses, int n_cand,
+                                nlm_qs_stats *stats);
 int nlm_qs_get_state(nlm_qs *q, double *u);
 int nlm_qs_get_bond_state(nlm_qs *q, uint8_t *broken);
 int nlm_qs_damage(nlm_qs *q, float *phi, float *Z);

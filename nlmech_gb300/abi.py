@@ -87,6 +87,7 @@ class Material(C.Structure):
         ("bond_params", C.c_double * 2),
         ("es_sc", C.c_double),
         ("es_ref_compat", C.c_int),
+        ("apply_contact", C.c_int),
     ]
 
 

@@ -64,6 +64,8 @@ struct StepParams {
   double delta, h, check_up, check_low;
   double C, beta, rbar, invF, fsc;
   int irrev;
+  int contact;        // normal contact between the nodes of broken bonds
+  double contact_kn, contact_rc;  // K 18 / (pi delta^5), 0.9 h (rnpBond.cpp:79-88)
   int nofail;         // 1 when some node is non-interior (no-fail region)
   int infl_type;
   double infl_a0, infl_a1, infl_alpha, infl_beta;

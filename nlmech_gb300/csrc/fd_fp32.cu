@@ -25,7 +25,8 @@ namespace nlm {
 // Kernel specialisations.
 enum : int {
   OPT_CONSTJ = 1,  // constant influence function (J folded into K1)
-  OPT_NOFAIL = 2   // some nodes are non-interior (per-bond flag test needed)
+  OPT_NOFAIL = 2,  // some nodes are non-interior (per-bond flag test needed)
+  OPT_CONTACT = 4  // normal contact force on broken bonds (No_Penetration)
 };
 
 // Bond force of RNPBond in FP32 (rnpBond.cpp:242-300 with contact off),
@@ -68,6 +69,22 @@ __device__ __forceinline__ float rnp_bond32(const Params32 &Q, const Node32<DIM>
   const float bs2 = S * S * r;
   const bool brk = (OPT & OPT_NOFAIL) ? breakable : true;
   fs = fs || (brk && Q.irrev && bs2 > Q.Ksc);
+  if ((OPT & OPT_CONTACT) && brk && fs) {
+    // broken bond: normal contact only (rnpBond.cpp:281-291), along the
+    // deformed bond y = xi + eta; F = -max(0, Kn Vi Vj/(Vi+Vj) (Rc - |y|)/|y|) y
+    const float y0 = d[0] + e0, y1 = d[1] + e1;
+    float yy = y0 * y0 + y1 * y1;
+    if (DIM == 3) {
+      d[2] = d[2] + ((ujh[2] - uih[2]) + (ujl[2] - uil[2]));
+      yy = fmaf(d[2], d[2], yy);
+    }
+    d[0] = y0;
+    d[1] = y1;
+    const float R = sqrtf(yy);
+    const float vj = nj.vol * fminf(1.f, (Q.check_up - r) * Q.inv_h);
+    const float sf = Q.kn * (ni.vol * vj / (ni.vol + vj)) * (Q.rc - R) / R;
+    return -fmaxf(sf, 0.f);
+  }
   const float s1 = fs ? 0.f : s0 * ex2_approx(Q.nbl2e * bs2);
   return brk ? s1 : s0;
 }
@@ -367,7 +384,8 @@ static cudaError_t launch32(const StepParams &P, const DevPtrs &D, const BCTable
                             const StepArgs &a, int decomp, cudaStream_t s) {
   if (P.n == 0) return cudaSuccess;
   const Params32 Q = make_p32(P);
-  const int opt = (P.infl_type == 0 ? OPT_CONSTJ : 0) | (P.nofail ? OPT_NOFAIL : 0);
+  const int opt = (P.infl_type == 0 ? OPT_CONSTJ : 0) | (P.nofail ? OPT_NOFAIL : 0) |
+                  (P.contact ? OPT_CONTACT : 0);
   const bool batch = D.qtab != nullptr;
   if (batch) {
     // specimens may mix influence functions: the batch path always takes the
@@ -382,7 +400,11 @@ static cudaError_t launch32(const StepParams &P, const DevPtrs &D, const BCTable
     case 0: launch_opt<DIM, SCHEME, 0, false>(P, Q, D, T, a, decomp, s); break;
     case 1: launch_opt<DIM, SCHEME, 1, false>(P, Q, D, T, a, decomp, s); break;
     case 2: launch_opt<DIM, SCHEME, 2, false>(P, Q, D, T, a, decomp, s); break;
-    default: launch_opt<DIM, SCHEME, 3, false>(P, Q, D, T, a, decomp, s); break;
+    case 3: launch_opt<DIM, SCHEME, 3, false>(P, Q, D, T, a, decomp, s); break;
+    case 4: launch_opt<DIM, SCHEME, 4, false>(P, Q, D, T, a, decomp, s); break;
+    case 5: launch_opt<DIM, SCHEME, 5, false>(P, Q, D, T, a, decomp, s); break;
+    case 6: launch_opt<DIM, SCHEME, 6, false>(P, Q, D, T, a, decomp, s); break;
+    default: launch_opt<DIM, SCHEME, 7, false>(P, Q, D, T, a, decomp, s); break;
   }
   return cudaGetLastError();
 }

@@ -16,7 +16,7 @@ namespace nlm {
 template <int DIM>
 __device__ __forceinline__ double rnp_bond64(const StepParams &P, const double xi[3],
                                              const double ui[3], const double xj[3],
-                                             const double uj[3], double volj,
+                                             const double uj[3], double &volj,
                                              bool breakable, bool &fs, double e[3]) {
   double dx = xj[0] - xi[0], dy = xj[1] - xi[1];
   double dz = DIM == 3 ? xj[2] - xi[2] : 0.0;
@@ -52,6 +52,7 @@ __global__ void __launch_bounds__(128)
   ld_node<DIM>(ucur, i, ui);
   const uint8_t fl = D.flags[i];
   const bool brk_i = !(fl & FLAG_NOFAIL);
+  const double voli = __ldg(D.vol64 + i);
   const int *colp = D.sell_cols + D.sell_ptr[i >> 5] + 4 * (i & 31);
   const int len = D.rowlen[i];
   double fi[3] = {0., 0., 0.};
@@ -73,7 +74,8 @@ __global__ void __launch_bounds__(128)
     const bool was = fs;
     bool breakable = brk_i;
     if (P.nofail && breakable) breakable = !(D.flags[j] & FLAG_NOFAIL);
-    double s = rnp_bond64<DIM>(P, xi, ui, xj, uj, __ldg(D.vol64 + j), breakable, fs, e);
+    double volj = __ldg(D.vol64 + j);
+    double s = rnp_bond64<DIM>(P, xi, ui, xj, uj, volj, breakable, fs, e);
     if (fs != was) {
       word |= 1u << (k & 31);
       dirty = true;
@@ -82,6 +84,17 @@ __global__ void __launch_bounds__(128)
       fi[0] = fi[0] + s * e[0];
       fi[1] = fi[1] + s * e[1];
       if (DIM == 3) fi[2] = fi[2] + s * e[2];
+    } else if (P.contact) {
+      // normal contact of a broken bond (rnpBond.cpp:281-291):
+      // y = (x_j + u_j) - (x_i + u_i), f += -max(0, Kn Vi Vj/(Vi+Vj) (Rc - |y|)/|y|) y
+      double y[3];
+      for (int c = 0; c < 3; c++) y[c] = (xj[c] + uj[c]) - (xi[c] + ui[c]);
+      const double R = sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
+      double sf = P.contact_kn * (voli * volj / (voli + volj)) * (P.contact_rc - R) / R;
+      if (sf < 0.) sf = 0.;
+      fi[0] = fi[0] + (0. + -sf * y[0]);
+      fi[1] = fi[1] + (0. + -sf * y[1]);
+      if (DIM == 3) fi[2] = fi[2] + (0. + -sf * y[2]);
     }
   }
   if (dirty) D.bits[(int64_t)chunk * P.npad + i] = word;

@@ -411,6 +411,7 @@ void nofail_flags(const double *x, int64_t n, double tol, std::vector<uint8_t> &
 // RNPBond constants (rnpBond.cpp:23-97, computeParameters :99-189) and the
 // influence function (influenceFn.h:85-402).
 int rnp_constants(const nlm_material &m, int dim, double delta, StepParams &P) {
+  double Kbulk = 0.;
   P.infl_type = m.influence_type;
   const int np = m.n_influence_params;
   double M = 0.;
@@ -475,11 +476,21 @@ int rnp_constants(const nlm_material &m, int dim, double delta, StepParams &P) {
       P.C = 2. * Gc / (3. * M);
       P.beta = 5. * lambda / (P.C * M);
     }
+    Kbulk = K;
   } else {
     P.C = m.bond_params[0];
     P.beta = m.bond_params[1];
+    // computeMaterialProperties (rnpBond.cpp:190-211): nu = 0.33, lambda
+    // from C and beta, then E and K
+    const double nu = 0.33;
+    const double lambda = dim == 2 ? P.C * M * P.beta / 4. : P.C * M * P.beta / 5.;
+    const double E = lambda * (1. + nu) * (1. - 2. * nu) / nu;
+    Kbulk = E / (3. * (1. - 2. * nu));
   }
   P.rbar = std::sqrt(0.5 / P.beta);
+  // contact between the nodes of broken bonds (RNPBond ctor, rnpBond.cpp:79-88)
+  P.contact = m.apply_contact ? 1 : 0;
+  P.contact_kn = m.apply_contact ? Kbulk * 18. / (M_PI * std::pow(delta, 5)) : 0.;
   if (!(P.C > 0.) || !(P.beta > 0.)) return fail(NLM_ERR_INVALID, "RNPBond constants not positive");
   return NLM_OK;
 }
@@ -865,6 +876,7 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
   int rc;
   if (h->material == NLM_MAT_RNP_BOND) {
     if ((rc = rnp_constants(d->material, d->dim, d->horizon, P))) return bail(rc);
+    P.contact_rc = 0.9 * d->mesh_size;
   } else {
     const nlm_material &m = d->material;
     if (!(m.K > 0.) || !(m.G > 0.)) return bail(fail(NLM_ERR_INVALID, "ElasticState needs K and G"));
@@ -1837,6 +1849,7 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
     Ps.lo_scale = P.lo_scale;
     int rc = rnp_constants(d.material, d.dim, d.horizon, Ps);
     if (rc) return bail(rc);
+    if (Ps.contact) return bail(fail(NLM_ERR_UNSUPPORTED, "contact forces are not batched"));
     qtab[s] = make_p32(Ps);
     for (int64_t q = b->off[s] / 32; q < (b->off[s] + d.n_nodes + 31) / 32; q++) slice_spec[q] = s;
     for (int c = 0; c < d.n_cracks; c++) {
@@ -2179,6 +2192,7 @@ struct nlm_qs {
   QSWork W{};
   unsigned long long *count = nullptr;
   double *saved = nullptr;  // plain start point while a guess is evaluated
+  double *cand = nullptr;   // best candidate start so far
   std::vector<void *> allocs;
   ~nlm_qs() {
     if (fd) nlm_fd_destroy(fd);  // frees the stream first
@@ -2268,6 +2282,8 @@ int nlm_qs_create(const nlm_fd_desc *desc, const nlm_qs_params *prm, nlm_qs **ou
   *out = nullptr;
   if (desc->material.kind != NLM_MAT_RNP_BOND)
     return fail(NLM_ERR_UNSUPPORTED, "the GPU quasi-static solver is for RNPBond");
+  if (desc->material.apply_contact)
+    return fail(NLM_ERR_UNSUPPORTED, "the quasi-static solver has no contact term");
   if (prm->max_newton < 1 || !(prm->tol > 0.) || prm->lin_max_iters < 1 || !(prm->lin_tol > 0.))
     return fail(NLM_ERR_INVALID, "bad solver parameters");
   nlm_fd_desc d = *desc;
@@ -2299,6 +2315,7 @@ int nlm_qs_create(const nlm_fd_desc *desc, const nlm_qs_params *prm, nlm_qs **ou
   if (e == cudaSuccess) e = q->alloc(&q->W.dblk, (size_t)NB * n);
   if (e == cudaSuccess) e = q->alloc(&q->count, 1);
   if (e == cudaSuccess) e = q->alloc(&q->saved, (size_t)h->S * n);
+  if (e == cudaSuccess) e = q->alloc(&q->cand, (size_t)h->S * n);
   if (e != cudaSuccess) {
     delete q;
     return cuda_fail(e, "qs buffers");
@@ -2314,7 +2331,13 @@ int nlm_qs_destroy(nlm_qs *q) {
 }
 
 int nlm_qs_load_step(nlm_qs *q, const double *guess, nlm_qs_stats *stats) {
+  return nlm_qs_load_step_candidates(q, guess, guess ? 1 : 0, stats);
+}
+
+int nlm_qs_load_step_candidates(nlm_qs *q, const double *guesses, int n_cand,
+                                nlm_qs_stats *stats) {
   if (!q) return fail(NLM_ERR_INVALID, "null handle");
+  if (n_cand < 0 || (n_cand > 0 && !guesses)) return fail(NLM_ERR_INVALID, "bad candidates");
   auto t0 = std::chrono::steady_clock::now();
   nlm_fd *h = q->fd;
   nlm_qs_stats st{};
@@ -2338,25 +2361,37 @@ int nlm_qs_load_step(nlm_qs *q, const double *guess, nlm_qs_stats *stats) {
   st.res_start = st.res_plain;
   NLM_CUDA(cudaMemcpyAsync(q->W.r, q->W.res, sizeof(double) * m, cudaMemcpyDeviceToDevice, s));
   bool use_guess = false;
-  if (guess) {
-    NLM_CUDA(cudaMemcpyAsync(h->stage, guess, sizeof(double) * 3 * h->n, cudaMemcpyHostToDevice, s));
-    k_scatter_vec<<<nblk(h->n, 256), 256, 0, s>>>(h->n, h->S, h->dim, h->D.perm_dev, h->stage, u);
-    NLM_CUDA(cudaGetLastError());
-    if ((rc = apply_bc(h, h->time))) return rc;
-    if ((e = qs_bcdiff(h->P, h->D, u, q->saved, q->W.dx, false, s)) != cudaSuccess)
-      return cuda_fail(e, "qs guess");
-    double rg = 0.;
-    if ((rc = qs_linear_norm(q, &rg))) return rc;
-    // the guess must cut the linearised residual of the plain start clearly:
-    // a start no better than the plain one (e.g. the previous state itself)
-    // would put the bonds next to the loaded layer past their critical
-    // strain in the first residual evaluation, which the tangent predictor
-    // of the plain start avoids
+  if (n_cand > 0) {
+    // each candidate start is judged by the linear model of the residual at
+    // the previous converged state; the best one is kept if it cuts the
+    // linearised residual of the plain start clearly (a start no better than
+    // the plain one, e.g. the previous state itself, would put the bonds next
+    // to the loaded layer past their critical strain in the first residual
+    // evaluation, which the tangent predictor of the plain start avoids)
     const double acc = q->prm.guess_accept > 0. ? q->prm.guess_accept : 0.1;
-    if (rg <= acc * st.res_plain) {
+    int best = -1;
+    double best_rg = 0.;
+    for (int c = 0; c < n_cand; c++) {
+      NLM_CUDA(cudaMemcpyAsync(h->stage, guesses + (size_t)3 * h->n * c,
+                               sizeof(double) * 3 * h->n, cudaMemcpyHostToDevice, s));
+      k_scatter_vec<<<nblk(h->n, 256), 256, 0, s>>>(h->n, h->S, h->dim, h->D.perm_dev, h->stage, u);
+      NLM_CUDA(cudaGetLastError());
+      if ((rc = apply_bc(h, h->time))) return rc;
+      if ((e = qs_bcdiff(h->P, h->D, u, q->saved, q->W.dx, false, s)) != cudaSuccess)
+        return cuda_fail(e, "qs guess");
+      double rg = 0.;
+      if ((rc = qs_linear_norm(q, &rg))) return rc;
+      if (best < 0 || rg < best_rg) {
+        best = c;
+        best_rg = rg;
+        if (n_cand > 1) NLM_CUDA(cudaMemcpyAsync(q->cand, u, bytes, cudaMemcpyDeviceToDevice, s));
+      }
+    }
+    if (best >= 0 && best_rg <= acc * st.res_plain) {
       use_guess = true;
-      st.used_guess = 1;
-      st.res_start = rg;
+      st.used_guess = best + 1;
+      st.res_start = best_rg;
+      if (n_cand > 1) NLM_CUDA(cudaMemcpyAsync(u, q->cand, bytes, cudaMemcpyDeviceToDevice, s));
     } else {
       NLM_CUDA(cudaMemcpyAsync(u, q->saved, bytes, cudaMemcpyDeviceToDevice, s));
       if ((rc = apply_bc(h, h->time))) return rc;

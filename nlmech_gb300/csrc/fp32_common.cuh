@@ -20,6 +20,7 @@ struct Params32 {
   int irrev;
   int infl_type;
   float a0, a1, alpha, ibeta;
+  float kn, rc;         // contact: K 18 / (pi delta^5), 0.9 h
   // integrator constants as (hi, lo) pairs
   float c_hi, c_lo;     // Verlet dt/(2 rho) or CD dt^2/rho
   float dt_hi, dt_lo;
@@ -54,6 +55,8 @@ inline Params32 make_p32(const StepParams &P) {
   split_const(c, q.c_hi, q.c_lo);
   split_const(P.dt, q.dt_hi, q.dt_lo);
   split_const(1.0 / P.dt, q.idt_hi, q.idt_lo);
+  q.kn = P.contact ? (float)P.contact_kn : 0.f;
+  q.rc = (float)P.contact_rc;
   return q;
 }
 

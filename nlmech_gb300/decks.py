@@ -97,6 +97,7 @@ class MaterialDeck:
     bond_params: List[float] = field(default_factory=lambda: [0.0, 0.0])
     es_sc: float = 0.0
     es_ref_compat: bool = False
+    apply_contact: bool = False
 
     def to_c(self):
         m = abi.Material()
@@ -114,6 +115,7 @@ class MaterialDeck:
         m.bond_params[0], m.bond_params[1] = self.bond_params[:2]
         m.es_sc = self.es_sc
         m.es_ref_compat = int(self.es_ref_compat)
+        m.apply_contact = int(self.apply_contact)
         return m
 
 

@@ -284,9 +284,17 @@ class QSModel:
     def __del__(self):
         self.close()
 
-    def load_step(self, guess=None):
-        """One load step; guess: (n, 3) start displacement or None (plain)."""
+    def load_step(self, guess=None, candidates=None):
+        """One load step from the plain start, a guess ((n, 3) displacement)
+        or the best of several candidate starts (list of (n, 3)); stats
+        "used_guess" is the 1-based index of the start used (0: plain)."""
         st = abi.QSStats()
+        if candidates is not None:
+            g = np.ascontiguousarray(np.stack([np.asarray(c, dtype=np.float64).reshape(-1, 3)
+                                               for c in candidates]))
+            _check(load().nlm_qs_load_step_candidates(self.h, abi.dptr(g), C.c_int(g.shape[0]),
+                                                      C.byref(st)))
+            return st.as_dict()
         g = None if guess is None else np.ascontiguousarray(guess, dtype=np.float64)
         _check(load().nlm_qs_load_step(self.h, abi.dptr(g), C.byref(st)))
         return st.as_dict()

@@ -9,11 +9,13 @@ step k from local features.  The start handed to nlm_qs_load_step is
 where du_{k-1} = u_{k-1} - u_{k-2} is the last increment, s the magnitude of
 the prescribed boundary increment per step and y the network output, so the
 network learns how the increment changes from one step to the next.
-nlm_qs_load_step keeps the guess only if its linearised residual is no
-larger than the one of the plain start (the previous displacement with the
-new boundary values, QuasiStaticModel::solver, QuasiStaticModel.cpp:280-312);
-otherwise it starts from the plain guess.  Newton then runs to the same
-tolerance either way.
+The solver receives two candidate starts, this one and the repeated last
+increment (u_{k-1} + du_{k-1}), judges both by the linear model of the
+residual at the previous converged state and keeps the better one if it
+cuts the linearised residual of the plain start (the previous displacement
+with the new boundary values, QuasiStaticModel::solver,
+QuasiStaticModel.cpp:280-312) at least tenfold; otherwise it starts from the
+plain start.  Newton then runs to the same tolerance either way.
 
 Features per node (float32, in this order):
   0, 1  reference position (x - x_min) / W, (y - y_min) / W
@@ -139,12 +141,13 @@ def run_steps(problem, nsteps, params=None, model=None, record=False, log=None,
     for k in range(nsteps):
         hist = model is not None or record or secant
         F = fb.rows(k, d1, d2, phi) if (model is not None or record) else None
-        guess = None
         if model is not None:
-            guess = fb.guess(u_prev, d1, model.forward(F), phi, deadzone)
+            st = q.load_step(candidates=[fb.guess(u_prev, d1, None, phi),
+                                         fb.guess(u_prev, d1, model.forward(F), phi, deadzone)])
         elif secant:
-            guess = fb.guess(u_prev, d1, None, phi)
-        st = q.load_step(guess)
+            st = q.load_step(fb.guess(u_prev, d1, None, phi))
+        else:
+            st = q.load_step()
         if hist:
             # history for the next step's features (the plain run needs none)
             u = q.state()[:, :2]
@@ -174,7 +177,8 @@ def summary(run):
     tol_ok = all(s["res_final"] <= 1e-8 * s["res_plain"] for s in st)
     return {"newton_iters": int(sum(s["newton_iters"] for s in st)),
             "cg_iters": int(sum(s["lin_iters"] for s in st)),
-            "guess_used": int(sum(s["used_guess"] for s in st)),
+            "guess_used": int(sum(1 for s in st if s["used_guess"])),
+            "network_start_used": int(sum(1 for s in st if s["used_guess"] == 2)),
             "wall_s": round(run["wall_s"], 4),
             "solver_ms": round(sum(s["ms"] for s in st), 2),
             "all_steps_converged": bool(tol_ok)}

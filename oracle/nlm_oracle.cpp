@@ -114,6 +114,9 @@ Influence make_influence(const nlm_material &m, int dim) {
 // RNPBond constants (src/material/pd/rnpBond.cpp:23-189).
 struct RNP {
   double C = 0, beta = 0, rbar = 0, invF = 0, M = 0, nu = 0, lambda = 0;
+  double K = 0;                          // bulk modulus as the deck ends up with it
+  bool contact = false;
+  double kn = 0, rc = 0;                 // contact constants (ctor :79-88)
   double fsc = 1;
   bool irrev = true;
   Influence J;
@@ -144,6 +147,7 @@ int make_rnp(const nlm_material &m, int dim, double horizon, RNP &r) {
     double lambda = E * nu / ((1. + nu) * (1. - 2. * nu)); // toLambdaE
     r.nu = nu;
     r.lambda = lambda;
+    r.K = K;
     if (dim == 2) {
       r.C = M_PI * Gc / (4. * r.M);
       r.beta = 4. * lambda / (r.C * r.M);
@@ -154,8 +158,16 @@ int make_rnp(const nlm_material &m, int dim, double horizon, RNP &r) {
   } else {
     r.C = m.bond_params[0];
     r.beta = m.bond_params[1];
+    // computeMaterialProperties (:190-211)
+    r.nu = 0.33;
+    r.lambda = dim == 2 ? r.C * r.M * r.beta / 4. : r.C * r.M * r.beta / 5.;
+    const double E = r.lambda * (1. + r.nu) * (1. - 2. * r.nu) / r.nu;  // toELambda
+    r.K = E / (3. * (1. - 2. * r.nu));                                   // toK
   }
   r.rbar = std::sqrt(0.5 / r.beta);
+  // contact between the nodes of broken bonds (ctor :79-88); Rc set with h
+  r.contact = m.apply_contact != 0;
+  if (r.contact) r.kn = r.K * 18. / (M_PI * std::pow(horizon, 5));
   return NLM_OK;
 }
 
@@ -441,6 +453,7 @@ int setup_model(const nlm_fd_desc *d, bool grid, Model &m) {
   int rc;
   if (m.mat.kind == NLM_MAT_RNP_BOND) {
     if ((rc = make_rnp(m.mat, m.dim, m.delta, m.rnp))) return rc;
+    m.rnp.rc = 0.9 * m.h;
   } else {
     if ((rc = make_es(m.mat, m.dim, m.es))) return rc;
   }
@@ -606,6 +619,18 @@ inline void rnp_bond(const Model &m, const double *u, int64_t i, int64_t k,
     } else {
       en = influence * p.C / p.invF * volj;
       s = 0.;
+      if (p.contact) {
+        // normal contact force between the nodes of the broken bond (:281-291)
+        const double voli = m.vol[i];
+        double y[3];
+        for (int c = 0; c < 3; c++) y[c] = (xj[c] + uj[c]) - (xi[c] + ui[c]);
+        const double R = std::sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
+        double sf = p.kn * (voli * volj / (voli + volj)) * (p.rc - R) / R;
+        if (sf < 0.) sf = 0.;
+        for (int c = 0; c < 3; c++) force[c] = 0. + -sf * y[c];
+        if (energy) *energy = en;
+        return;
+      }
     }
   } else {
     en = (influence * p.C * p.beta * rji * Sji * Sji / p.invF) * volj;

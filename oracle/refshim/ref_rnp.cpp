@@ -285,6 +285,7 @@ int ref_rnp_create(const nlm_fd_desc *d, ref_rnp **out) {
     md.d_matData.d_Gc = m.Gc;
     md.d_matData.d_KIc = m.KIc;
     md.d_density = m.density;
+    md.d_applyContact = m.apply_contact != 0;
 
     h->u.assign(n, util::Point3());
     h->v.assign(n, util::Point3());

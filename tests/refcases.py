@@ -47,10 +47,24 @@ def cube3d(n=12, seed=5):
     return p
 
 
+def contact_plate():
+    """32 x 32 plate with a pre-crack, no boundary loads, seeded random
+    initial velocities of +-2 m/s: bonds break and broken-bond nodes come
+    within the contact radius, so the No_Penetration contact force acts."""
+    p = configs.rnp_plate(32, 1e-3, 3, 0.008, 0.0, 2e-8, 300, seed=3)
+    p.ubc = []
+    rng = np.random.default_rng(4)
+    p.v0 = np.zeros((p.n, 3))
+    p.v0[:, :2] = rng.uniform(-2.0, 2.0, size=(p.n, 2))
+    p.material.apply_contact = True
+    return p
+
+
 # name -> (problem, Verlet steps) of the committed reference outputs
 # (tests/golden/rnp_ref_<name>.npz)
 GOLDEN_CASES = {
     "fracture_plate": (fracture_plate, 300),
     "loads_nofail_plate": (loads_nofail_plate, 200),
     "cube3d": (cube3d, 100),
+    "contact_plate": (contact_plate, 300),
 }

@@ -16,7 +16,8 @@ from refcases import GOLDEN_CASES
 pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-RTOL = {"fracture_plate": 1e-12, "loads_nofail_plate": 1e-11, "cube3d": 1e-12}
+RTOL = {"fracture_plate": 1e-12, "loads_nofail_plate": 1e-11, "cube3d": 1e-12,
+        "contact_plate": 1e-12}
 
 
 def _pairs(rowptr, cols, b):
@@ -56,3 +57,19 @@ def test_fp32c_matches_reference_golden(gpu):
         assert np.linalg.norm(u - z["u"]) <= 1e-5 * np.linalg.norm(z["u"])
         diff = len(_pairs(z["rowptr"], z["cols"], m.bond_state()) ^ ref)
         assert diff <= 1e-3 * len(ref), (diff, len(ref))
+
+
+def test_fp32c_contact_against_reference_golden(gpu):
+    """Contact forces in FP32C on a fragmenting plate (random +-2 m/s
+    velocities): chaotic, so the bar is looser than the config bars."""
+    make, steps = GOLDEN_CASES["contact_plate"]
+    z = np.load(os.path.join(GOLDEN, "rnp_ref_contact_plate.npz"))
+    ref = _pairs(z["rowptr"], z["cols"], z["broken"])
+    m = gpu.FDModel(make(), precision=abi.FP32C, decomposition=abi.DECOMP_THREAD)
+    m.run(steps)
+    u = m.state()[0]
+    err = np.linalg.norm(u - z["u"]) / np.linalg.norm(z["u"])
+    diff = len(_pairs(z["rowptr"], z["cols"], m.bond_state()) ^ ref)
+    print("fp32c contact: rel L2 %.3e, differing broken bonds %d of %d" % (err, diff, len(ref)))
+    assert err <= 1e-3
+    assert diff <= 1e-2 * len(ref)

@@ -14,7 +14,7 @@ import pytest
 from nlmech_gb300 import configs
 from oracle import oracle as orc
 
-from refcases import GOLDEN_CASES, cube3d, fracture_plate, loads_nofail_plate
+from refcases import GOLDEN_CASES, contact_plate, cube3d, fracture_plate, loads_nofail_plate
 
 needs_ref = pytest.mark.skipif(not orc.refshim_available(),
                                reason="reference source tree not present")
@@ -63,6 +63,11 @@ def test_refshim_3d_bit_exact():
 
 
 @needs_ref
+def test_refshim_contact_bit_exact():
+    _same_run(contact_plate(), 300, chunks=3)
+
+
+@needs_ref
 def test_refshim_critical_stretch():
     p = configs.config0()
     r = orc.RefRNP(p)
@@ -77,7 +82,7 @@ import os  # noqa: E402
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-@pytest.mark.parametrize("name", ["fracture_plate", "loads_nofail_plate", "cube3d"])
+@pytest.mark.parametrize("name", sorted(GOLDEN_CASES))
 def test_oracle_matches_reference_golden(name):
     make, steps = GOLDEN_CASES[name]
     z = np.load(os.path.join(GOLDEN, "rnp_ref_%s.npz" % name))

@@ -2193,6 +2193,12 @@ struct nlm_qs {
   unsigned long long *count = nullptr;
   double *saved = nullptr;  // plain start point while a guess is evaluated
   double *cand = nullptr;   // best candidate start so far
+  // FP64 Krylov solves from now on, for Newton corrections and for tangent
+  // predictors respectively: set once a solve of that kind has not converged
+  // in FP32 within its iteration cap (the tangent of this specimen is then
+  // too ill-conditioned for FP32 recurrences)
+  bool cg64 = false;
+  bool cg64_predictor = false;
   std::vector<void *> allocs;
   ~nlm_qs() {
     if (fd) nlm_fd_destroy(fd);  // frees the stream first
@@ -2248,6 +2254,7 @@ int qs_newton(nlm_qs *q, double target, nlm_qs_stats *st) {
     if (!(st->res_final > target) || it >= q->prm.max_newton) return NLM_OK;
     int li = 0;
     e = qs_cg(h->P, h->D, q->W, q->W.res, q->W.dx, q->prm.lin_tol, q->prm.lin_max_iters, 8, &li,
+              &q->cg64,
               h->stream);
     if (e == cudaSuccess) e = qs_add(h->P, q->W.dx, u, h->stream);
     if (e != cudaSuccess) return cuda_fail(e, "qs linear solve");
@@ -2307,7 +2314,12 @@ int nlm_qs_create(const nlm_fd_desc *desc, const nlm_qs_params *prm, nlm_qs **ou
     if (e == cudaSuccess) e = q->alloc(p, m);
   if (e == cudaSuccess) e = q->alloc(&q->W.part, std::max<int64_t>((m + 255) / 256 + 1, qs_cg_stride(n)));
   if (e == cudaSuccess) e = q->alloc(&q->W.cgpart, 3 * qs_cg_stride(n));
-  if (e == cudaSuccess) e = q->alloc(&q->W.cgs, 4);
+  if (e == cudaSuccess) e = q->alloc(&q->W.cgs, 8);
+  for (float **p : {&q->W.r32, &q->W.z32, &q->W.p32, &q->W.p32b, &q->W.ap32, &q->W.x32})
+    if (e == cudaSuccess) e = q->alloc(p, m);
+  if (e == cudaSuccess) e = q->alloc(&q->W.blk32, (size_t)(NB == 3 ? 4 : 8) * (nnz + 1));
+  if (e == cudaSuccess) e = q->alloc(&q->W.dblk32, (size_t)NB * n);
+  q->W.nnz = nnz;
   if (e == cudaSuccess) e = q->alloc(&q->W.ticket, 4);
   if (e == cudaSuccess) e = cudaMemset(q->W.ticket, 0, 4 * sizeof(unsigned));
   if (e == cudaSuccess) e = q->alloc(&q->W.sc, 8);
@@ -2403,7 +2415,8 @@ int nlm_qs_load_step_candidates(nlm_qs *q, const double *guesses, int n_cand,
     NLM_CUDA(cudaMemcpyAsync(q->W.res, q->W.r, sizeof(double) * m, cudaMemcpyDeviceToDevice, s));
     NLM_CUDA(cudaMemcpyAsync(q->W.ap, q->W.res, sizeof(double) * m, cudaMemcpyDeviceToDevice, s));
     int li = 0;
-    e = qs_cg(h->P, h->D, q->W, q->W.ap, q->W.dx, q->prm.lin_tol, q->prm.lin_max_iters, 8, &li, s);
+    e = qs_cg(h->P, h->D, q->W, q->W.ap, q->W.dx, q->prm.lin_tol, q->prm.lin_max_iters, 8, &li,
+              &q->cg64_predictor, s);
     if (e == cudaSuccess) e = qs_add(h->P, q->W.dx, u, s);
     if (e != cudaSuccess) return cuda_fail(e, "qs predictor solve");
     st.lin_iters += li;

@@ -29,6 +29,7 @@
 // ||f|| <= tol * ||f + K du_c||.  Softening bonds (1 - 2 beta r S^2 < 0)
 // are left out of the tangent so the preconditioned CG matrix stays SPD.
 
+#include <algorithm>
 #include <vector>
 
 #include "fd_internal.h"
@@ -137,7 +138,8 @@ __global__ void k_qs_force(const StepParams P, const DevPtrs D, const double *u,
   if (UPD && newly) atomicAdd(count, (unsigned long long)newly);
 }
 
-__device__ __forceinline__ void sym_mul(int dim, const double *a, const double *x, double *y) {
+template <typename T>
+__device__ __forceinline__ void sym_mul(int dim, const T *a, const T *x, T *y) {
   if (dim == 2) {
     y[0] = a[0] * x[0] + a[1] * x[1];
     y[1] = a[1] * x[0] + a[2] * x[1];
@@ -165,10 +167,9 @@ __device__ __forceinline__ void block_sum(double v, double *part) {
 // z = (D_i)^-1 r on the free dofs of node i: the diagonal block b (packed
 // symmetric) with the rows and columns of fixed dofs replaced by identity;
 // rv is zero on fixed dofs.  A singular block gives z = 0.
-template <int DIM>
-__device__ __forceinline__ void block_jacobi(const double *b, uint8_t fl, const double rv[3],
-                                             double zv[3]) {
-  double a[9];
+template <int DIM, typename T>
+__device__ __forceinline__ void block_jacobi(const T *b, uint8_t fl, const T rv[3], T zv[3]) {
+  T a[9];
   if (DIM == 2) {
     a[0] = b[0]; a[1] = b[1]; a[2] = b[1]; a[3] = b[2];
   } else {
@@ -179,22 +180,22 @@ __device__ __forceinline__ void block_jacobi(const double *b, uint8_t fl, const 
   for (int c = 0; c < DIM; c++)
     if (fl >> c & 1)
       for (int q = 0; q < DIM; q++) {
-        a[c * DIM + q] = (c == q) ? 1. : 0.;
-        a[q * DIM + c] = (c == q) ? 1. : 0.;
+        a[c * DIM + q] = (c == q) ? T(1) : T(0);
+        a[q * DIM + c] = (c == q) ? T(1) : T(0);
       }
-  zv[0] = zv[1] = zv[2] = 0.;
+  zv[0] = zv[1] = zv[2] = T(0);
   if (DIM == 2) {
-    const double det = a[0] * a[3] - a[1] * a[2];
-    if (fabs(det) > 0.) {
+    const T det = a[0] * a[3] - a[1] * a[2];
+    if (fabs(det) > T(0)) {
       zv[0] = (a[3] * rv[0] - a[1] * rv[1]) / det;
       zv[1] = (-a[2] * rv[0] + a[0] * rv[1]) / det;
     }
   } else {
-    const double c00 = a[4] * a[8] - a[5] * a[7], c01 = a[5] * a[6] - a[3] * a[8],
-                 c02 = a[3] * a[7] - a[4] * a[6];
-    const double det = a[0] * c00 + a[1] * c01 + a[2] * c02;
-    if (fabs(det) > 0.) {
-      const double inv[9] = {c00, a[2] * a[7] - a[1] * a[8], a[1] * a[5] - a[2] * a[4],
+    const T c00 = a[4] * a[8] - a[5] * a[7], c01 = a[5] * a[6] - a[3] * a[8],
+            c02 = a[3] * a[7] - a[4] * a[6];
+    const T det = a[0] * c00 + a[1] * c01 + a[2] * c02;
+    if (fabs(det) > T(0)) {
+      const T inv[9] = {c00, a[2] * a[7] - a[1] * a[8], a[1] * a[5] - a[2] * a[4],
                              c01, a[0] * a[8] - a[2] * a[6], a[2] * a[3] - a[0] * a[5],
                              c02, a[1] * a[6] - a[0] * a[7], a[0] * a[4] - a[1] * a[3]};
       for (int c = 0; c < 3; c++)
@@ -215,7 +216,7 @@ __global__ void k_qs_precond(const StepParams P, const DevPtrs D, const double *
     const uint8_t fl = D.flags[i];
     double rv[3] = {0., 0., 0.}, zv[3];
     for (int c = 0; c < DIM; c++) rv[c] = (fl >> c & 1) ? 0. : r[DIM * i + c];
-    block_jacobi<DIM>(dblk + NB * i, fl, rv, zv);
+    block_jacobi<DIM, double>(dblk + NB * i, fl, rv, zv);
     for (int c = 0; c < DIM; c++) {
       z[DIM * i + c] = zv[c];
       dot += rv[c] * zv[c];
@@ -407,7 +408,7 @@ __global__ void k_cg_update(int64_t n, const uint8_t *flags, const double *dblk,
       drr += rk * rk;
       rv[c] = (fl >> c & 1) ? 0. : rk;
     }
-    block_jacobi<DIM>(dblk + NB * i, fl, rv, zv);
+    block_jacobi<DIM, double>(dblk + NB * i, fl, rv, zv);
     for (int c = 0; c < DIM; c++) {
       z[DIM * i + c] = zv[c];
       drz += rv[c] * zv[c];
@@ -422,6 +423,209 @@ __global__ void k_cg_seed(double *rz_prev, double *pold, int64_t m) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k < m) pold[k] = 0.;
   if (k == 0) *rz_prev = 1.;
+}
+
+// ---- FP32 Krylov solve ---------------------------------------------------
+// The Newton correction only has to cut the residual by lin_tol (1e-4), so
+// the tangent blocks, the CG vectors, the SpMV and every per-thread
+// operation run in FP32: GB300 issues FP64 at a small fraction of its FP32
+// rate, and even a few FP64 operations per thread (a step-length division,
+// FP64 partial sums) made these launches FP64-pipe bound.  Block sums are
+// formed in FP32 and stored as FP64 partials; the sum over blocks and the
+// step lengths alpha, beta are computed in FP64 once per launch, by its last
+// block.  The residual, its norm and the Newton update u += dx stay FP64.
+
+__global__ void k_to_f32(int64_t n, const double *a, float *b) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k < n) b[k] = (float)a[k];
+}
+// Tangent blocks to FP32, padded to nb_out floats per bond (16-byte loads).
+__global__ void k_blk_to_f32(int64_t nbonds, int nb_in, int nb_out, const double *a, float *b) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= nbonds) return;
+  for (int c = 0; c < nb_out; c++) b[nb_out * q + c] = c < nb_in ? (float)a[nb_in * q + c] : 0.f;
+}
+__global__ void k_to_f64(int64_t n, const float *a, double *b) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k < n) b[k] = (double)a[k];
+}
+
+__device__ __forceinline__ void block_sum_f(float v, double *part) {
+  __shared__ float sh[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = l < (int)(blockDim.x >> 5) ? sh[l] : 0.f;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (l == 0) part[blockIdx.x] = (double)v;
+  }
+}
+__device__ __forceinline__ void block_sum2_f(float va, float vb, double *pa, double *pb) {
+  __shared__ float sh[2][32];
+  for (int o = 16; o > 0; o >>= 1) {
+    va += __shfl_xor_sync(0xffffffffu, va, o);
+    vb += __shfl_xor_sync(0xffffffffu, vb, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sh[0][w] = va;
+    sh[1][w] = vb;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const bool in = l < (int)(blockDim.x >> 5);
+    va = in ? sh[0][l] : 0.f;
+    vb = in ? sh[1][l] : 0.f;
+    for (int o = 16; o > 0; o >>= 1) {
+      va += __shfl_xor_sync(0xffffffffu, va, o);
+      vb += __shfl_xor_sync(0xffffffffu, vb, o);
+    }
+    if (l == 0) {
+      pa[blockIdx.x] = (double)va;
+      pb[blockIdx.x] = (double)vb;
+    }
+  }
+}
+
+template <int DIM>
+__global__ void k_qs_precond32(int64_t n, const uint8_t *flags, const float *dblk,
+                               const float *r, float *z, double *part) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  constexpr int NB = DIM == 2 ? 3 : 6;
+  float dot = 0.f;
+  if (i < n) {
+    const uint8_t fl = flags[i];
+    float rv[3] = {0.f, 0.f, 0.f}, zv[3];
+    for (int c = 0; c < DIM; c++) rv[c] = (fl >> c & 1) ? 0.f : r[DIM * i + c];
+    block_jacobi<DIM, float>(dblk + NB * i, fl, rv, zv);
+    for (int c = 0; c < DIM; c++) {
+      z[DIM * i + c] = zv[c];
+      dot = fmaf(rv[c], zv[c], dot);
+    }
+  }
+  block_sum_f(dot, part);
+}
+
+// Device scalars of the FP32 CG: tot[0..1] = rz_k by parity, tot[2] = pAp,
+// tot[3] = r.r (FP64); fs[0] = alpha, fs[1] = beta (FP32, fs = tot + 4).
+
+// FP32 form of the first CG launch (see k_cg_dir_spmv).  Its last block
+// forms alpha_k = rz_k / pAp_k for the second launch.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_cg32_dir_spmv(
+    int64_t n, const uint8_t *flags, const int64_t *rowptr, const int *cols, const float *blk,
+    const float *dblk, const float *z, const float *pold, float *pnew, float *ap,
+    const double *rz_cur, double *pap_part, unsigned *ticket, double *pap_total, float *fs) {
+  const float beta = fs[1];
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t i = t / kG;
+  const int g = (int)(t % kG);
+  constexpr int NB = DIM == 2 ? 3 : 6;  // diagonal blocks (per node)
+  constexpr int NP = DIM == 2 ? 4 : 8;  // bond blocks, padded for 16-byte loads
+  float acc[3] = {0.f, 0.f, 0.f}, tv[3];
+  if (i < n) {
+    const int64_t q1 = rowptr[i + 1];
+    // four bonds per pass: all ids, then all gathers, then the products, so
+    // that each lane keeps its loads in flight together
+    for (int64_t qb = rowptr[i] + g; qb < q1; qb += 4 * kG) {
+      int jj[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) jj[u] = qb + u * kG < q1 ? cols[qb + u * kG] : -1;
+      float bb[4][NP], pj[4][3];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int j = jj[u] < 0 ? (int)i : jj[u];
+        const int64_t q = jj[u] < 0 ? qb : qb + u * kG;
+        const float4 *bp = reinterpret_cast<const float4 *>(blk + NP * q);
+        const float4 b0 = bp[0];
+        bb[u][0] = b0.x; bb[u][1] = b0.y; bb[u][2] = b0.z; bb[u][3] = b0.w;
+        if (DIM == 3) {
+          const float4 b1 = bp[1];
+          bb[u][4] = b1.x; bb[u][5] = b1.y; bb[u][6] = b1.z; bb[u][7] = b1.w;
+        }
+        for (int c = 0; c < DIM; c++) pj[u][c] = fmaf(beta, pold[DIM * j + c], z[DIM * j + c]);
+        if (DIM == 2) pj[u][2] = 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        if (jj[u] < 0) continue;
+        sym_mul<float>(DIM, bb[u], pj[u], tv);
+        for (int c = 0; c < DIM; c++) acc[c] -= tv[c];
+      }
+    }
+  }
+  for (int o = kG / 2; o > 0; o >>= 1)
+    for (int c = 0; c < DIM; c++) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+  float dot = 0.f;
+  if (i < n && g == 0) {
+    const uint8_t fl = flags[i];
+    float pi[3] = {0.f, 0.f, 0.f};
+    for (int c = 0; c < DIM; c++) {
+      pi[c] = fmaf(beta, pold[DIM * i + c], z[DIM * i + c]);
+      pnew[DIM * i + c] = pi[c];
+    }
+    sym_mul<float>(DIM, dblk + NB * i, pi, tv);
+    for (int c = 0; c < DIM; c++) {
+      const float yc = (fl >> c & 1) ? 0.f : acc[c] + tv[c];
+      ap[DIM * i + c] = yc;
+      dot = fmaf(pi[c], yc, dot);
+    }
+  }
+  block_sum_f(dot, pap_part);
+  if (last_block(ticket)) {
+    finish_sums(1, pap_part, pap_total, nullptr, nullptr, ticket);
+    if (threadIdx.x == 0) {
+      const double pap = *pap_total;
+      fs[0] = (float)(pap != 0. ? *rz_cur / pap : 0.);
+    }
+  }
+}
+
+// FP32 form of the second CG launch (see k_cg_update).  Its last block forms
+// beta_k = rz_{k+1} / rz_k for the next first launch.
+template <int DIM>
+__global__ void k_cg32_update(int64_t n, const uint8_t *flags, const float *dblk, const float *p,
+                              const float *ap, float *x, float *r, float *z,
+                              const double *rz_cur, double *rz_part, double *rr_part,
+                              unsigned *ticket, double *rz_next, double *rr_total, float *fs) {
+  const float alpha = fs[0];
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  constexpr int NB = DIM == 2 ? 3 : 6;
+  float drz = 0.f, drr = 0.f;
+  if (i < n) {
+    const uint8_t fl = flags[i];
+    float rv[3] = {0.f, 0.f, 0.f}, zv[3] = {0.f, 0.f, 0.f};
+    for (int c = 0; c < DIM; c++) {
+      const int64_t k = DIM * i + c;
+      x[k] = fmaf(alpha, p[k], x[k]);
+      const float rk = fmaf(-alpha, ap[k], r[k]);
+      r[k] = rk;
+      drr = fmaf(rk, rk, drr);
+      rv[c] = (fl >> c & 1) ? 0.f : rk;
+    }
+    block_jacobi<DIM, float>(dblk + NB * i, fl, rv, zv);
+    for (int c = 0; c < DIM; c++) {
+      z[DIM * i + c] = zv[c];
+      drz = fmaf(rv[c], zv[c], drz);
+    }
+  }
+  block_sum2_f(drz, drr, rz_part, rr_part);
+  if (last_block(ticket)) {
+    finish_sums(2, rz_part, rz_next, rr_part, rr_total, ticket);
+    if (threadIdx.x == 0) {
+      const double rzc = *rz_cur;
+      fs[1] = (float)(rzc != 0. ? *rz_next / rzc : 0.);
+    }
+  }
+}
+
+__global__ void k_cg32_seed(float *fs, float *pold, int64_t m) {
+  // beta = 0 for the first direction (p_0 = z_0); p_{-1} = 0
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k < m) pold[k] = 0.f;
+  if (k == 0) fs[1] = 0.f;
 }
 
 // Bonds of the converged state that exceed the critical strain break.
@@ -508,7 +712,7 @@ cudaError_t qs_dot(const double *a, const double *b, int64_t m, double *part, do
 
 // Preconditioned CG on (-K) dx = r (free dofs).  Scalars: sc[0] = rz_old,
 // sc[1] = pAp, sc[2] = rz_new, sc[3] = r.r (convergence check).
-cudaError_t qs_cg(const StepParams &P, const DevPtrs &D, const QSWork &W, const double *rhs,
+static cudaError_t qs_cg64(const StepParams &P, const DevPtrs &D, const QSWork &W, const double *rhs,
                   double *dx, double tol, int max_iters, int check_every, int *iters,
                   cudaStream_t s) {
   const int dim = P.dim;
@@ -569,6 +773,102 @@ cudaError_t qs_cg(const StepParams &P, const DevPtrs &D, const QSWork &W, const 
   }
   *iters = it;
   return cudaGetLastError();
+}
+
+static cudaError_t qs_cg32(const StepParams &P, const DevPtrs &D, const QSWork &W,
+                           const double *rhs, double *dx, double tol, int max_iters,
+                           int check_every, int *iters, bool *converged, cudaStream_t s) {
+  *converged = true;
+  const int dim = P.dim;
+  const int64_t m = (int64_t)dim * P.n;
+  const unsigned gn = qblk(P.n), gg = grp_blocks(P.n);
+  const int64_t stride = qs_cg_stride(P.n);
+  // partials: pAp (K1 blocks), rz and r.r (K2 blocks); totals on the device:
+  // rz_k in tot[k & 1], pAp in tot[2], r.r in tot[3]
+  double *pap_p = W.cgpart, *rz_p = W.cgpart + stride, *rr_p = W.cgpart + 2 * stride;
+  double *tot = W.cgs;
+  float *fs = reinterpret_cast<float *>(tot + 4);
+  float *pbuf[2] = {W.p32, W.p32b};
+  const int NB = dim == 2 ? 3 : 6;
+  cudaError_t e;
+  // FP32 copies of the tangent and of the right-hand side; x = 0
+  k_blk_to_f32<<<qblk(W.nnz + 1), 256, 0, s>>>(W.nnz + 1, NB, dim == 2 ? 4 : 8, W.blk, W.blk32);
+  k_to_f32<<<qblk((int64_t)NB * P.n), 256, 0, s>>>((int64_t)NB * P.n, W.dblk, W.dblk32);
+  k_to_f32<<<qblk(m), 256, 0, s>>>(m, rhs, W.r32);
+  if ((e = cudaMemsetAsync(W.x32, 0, sizeof(float) * m, s))) return e;
+  // z_0 = M^-1 r_0 and rz_0; beta_{-1} = 0, p_{-1} = 0
+  if (dim == 2)
+    k_qs_precond32<2><<<gn, 256, 0, s>>>(P.n, D.flags, W.dblk32, W.r32, W.z32, rz_p);
+  else
+    k_qs_precond32<3><<<gn, 256, 0, s>>>(P.n, D.flags, W.dblk32, W.r32, W.z32, rz_p);
+  k_qs_sum<<<1, 256, 0, s>>>(rz_p, gn, tot + 0);
+  k_cg32_seed<<<qblk(m), 256, 0, s>>>(fs, pbuf[1], m);
+  double rr0 = 0.;
+  if ((e = qs_dot(rhs, rhs, m, W.part, W.sc + 3, s))) return e;
+  if ((e = cudaMemcpyAsync(&rr0, W.sc + 3, sizeof(double), cudaMemcpyDeviceToHost, s))) return e;
+  if ((e = cudaStreamSynchronize(s))) return e;
+  const double target = tol * tol * rr0;
+  int it = 0;
+  if (rr0 == 0.) {
+    *iters = 0;
+    return cudaMemsetAsync(dx, 0, sizeof(double) * m, s);
+  }
+  while (it < max_iters) {
+    for (int q = 0; q < check_every && it < max_iters; q++, it++) {
+      const int cur = it & 1, prv = cur ^ 1;
+      if (dim == 2) {
+        k_cg32_dir_spmv<2><<<gg, 256, 0, s>>>(P.n, D.flags, D.rowptr, D.cols, W.blk32,
+                                              W.dblk32, W.z32, pbuf[prv], pbuf[cur], W.ap32,
+                                              tot + cur, pap_p, W.ticket, tot + 2, fs);
+        k_cg32_update<2><<<gn, 256, 0, s>>>(P.n, D.flags, W.dblk32, pbuf[cur], W.ap32, W.x32,
+                                            W.r32, W.z32, tot + cur, rz_p, rr_p, W.ticket + 1,
+                                            tot + prv, tot + 3, fs);
+      } else {
+        k_cg32_dir_spmv<3><<<gg, 256, 0, s>>>(P.n, D.flags, D.rowptr, D.cols, W.blk32,
+                                              W.dblk32, W.z32, pbuf[prv], pbuf[cur], W.ap32,
+                                              tot + cur, pap_p, W.ticket, tot + 2, fs);
+        k_cg32_update<3><<<gn, 256, 0, s>>>(P.n, D.flags, W.dblk32, pbuf[cur], W.ap32, W.x32,
+                                            W.r32, W.z32, tot + cur, rz_p, rr_p, W.ticket + 1,
+                                            tot + prv, tot + 3, fs);
+      }
+    }
+    if ((e = cudaGetLastError())) return e;
+    double rr = 0.;
+    if ((e = cudaMemcpyAsync(&rr, tot + 3, sizeof(double), cudaMemcpyDeviceToHost, s))) return e;
+    if ((e = cudaStreamSynchronize(s))) return e;
+    if (!(rr > target)) break;
+  }
+  *converged = it < max_iters;
+  k_to_f64<<<qblk(m), 256, 0, s>>>(m, W.x32, dx);
+  *iters = it;
+  return cudaGetLastError();
+}
+
+// Newton correction (-K) dx = rhs.  The FP32 solve is tried first; when it
+// has not reached the tolerance within kCg32Cap iterations (tangents of
+// fractured states are too ill-conditioned for FP32 recurrences), the FP64
+// solve takes over from scratch and *use64 is set so that the caller keeps
+// FP64 for the rest of the load step.
+constexpr int kCg32Cap = 800;
+
+cudaError_t qs_cg(const StepParams &P, const DevPtrs &D, const QSWork &W, const double *rhs,
+                  double *dx, double tol, int max_iters, int check_every, int *iters,
+                  bool *use64, cudaStream_t s) {
+  int it32 = 0;
+  if (!*use64) {
+    bool conv = false;
+    cudaError_t e = qs_cg32(P, D, W, rhs, dx, tol, std::min(max_iters, kCg32Cap), check_every,
+                            &it32, &conv, s);
+    if (e != cudaSuccess || conv || max_iters <= kCg32Cap) {
+      *iters = it32;
+      return e;
+    }
+    *use64 = true;
+  }
+  int it64 = 0;
+  cudaError_t e = qs_cg64(P, D, W, rhs, dx, tol, max_iters, check_every, &it64, s);
+  *iters = it32 + it64;
+  return e;
 }
 
 // dx = u - u_prev (DIM per node); with fixed_only, 0 on free dofs

@@ -11,13 +11,16 @@ struct QSWork {
   double *r, *z, *p, *ap;  // CG vectors
   double *p2;     // second search-direction buffer (iteration parity)
   double *cgpart; // CG partial sums: 3 arrays of qs_cg_stride(n) entries
-  double *cgs;    // CG totals on the device (4)
+  double *cgs;    // CG totals on the device (4) and two FP32 step lengths
   unsigned *ticket;  // last-block tickets of the two CG launches (start at 0)
   double *part;   // block partial sums
   double *sc;     // device scalars
   double *blk;    // tangent blocks per bond (3 or 6 doubles)
   double *dblk;   // diagonal blocks per node
   double *res0;   // force at the previous converged state
+  // FP32 Krylov solve: tangent copies and CG vectors
+  float *blk32, *dblk32, *r32, *z32, *p32, *p32b, *ap32, *x32;
+  int64_t nnz;
 };
 
 // count != NULL: bonds past the critical strain break during the evaluation
@@ -27,9 +30,10 @@ cudaError_t qs_residual(const StepParams &P, const DevPtrs &D, const double *u, 
                         unsigned long long *count = nullptr);
 cudaError_t qs_dot(const double *a, const double *b, int64_t m, double *part, double *out,
                    cudaStream_t s);
+// use64: in/out, FP64 Krylov solve (set when the FP32 solve did not converge)
 cudaError_t qs_cg(const StepParams &P, const DevPtrs &D, const QSWork &W, const double *rhs,
                   double *dx, double tol, int max_iters, int check_every, int *iters,
-                  cudaStream_t s);
+                  bool *use64, cudaStream_t s);
 // Entries per partial-sum array of the CG (4 arrays live in QSWork::cgpart).
 int64_t qs_cg_stride(int64_t n);
 cudaError_t qs_add(const StepParams &P, const double *du, double *u, cudaStream_t s);

@@ -9,13 +9,12 @@ step k from local features.  The start handed to nlm_qs_load_step is
 where du_{k-1} = u_{k-1} - u_{k-2} is the last increment, s the magnitude of
 the prescribed boundary increment per step and y the network output, so the
 network learns how the increment changes from one step to the next.
-The solver receives two candidate starts, this one and the repeated last
-increment (u_{k-1} + du_{k-1}), judges both by the linear model of the
-residual at the previous converged state and keeps the better one if it
-cuts the linearised residual of the plain start (the previous displacement
-with the new boundary values, QuasiStaticModel::solver,
-QuasiStaticModel.cpp:280-312) at least tenfold; otherwise it starts from the
-plain start.  Newton then runs to the same tolerance either way.
+nlm_qs_load_step judges the start by the linear model of the residual at
+the previous converged state and keeps it if it cuts the linearised
+residual of the plain start (the previous displacement with the new
+boundary values, QuasiStaticModel::solver, QuasiStaticModel.cpp:280-312) at
+least tenfold; otherwise it starts from the plain start.  Newton then runs
+to the same tolerance either way.
 
 Features per node (float32, in this order):
   0, 1  reference position (x - x_min) / W, (y - y_min) / W
@@ -50,7 +49,7 @@ WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "warm
 TARGET_CLIP = 5.0    # targets (units of s) beyond this are clipped for training
 FEATURE_CLIP = 8.0   # increment features (units of s) are clipped to +-8
 DETACHED = 0.999     # nodes with damage above this keep the plain start
-DEADZONE = 0.05      # network outputs below this (units of s) count as zero
+DEADZONE = 0.5       # network outputs below this (units of s) count as zero
 
 
 def _rect_mask(x, b):
@@ -122,10 +121,12 @@ class Features:
 
 
 def run_steps(problem, nsteps, params=None, model=None, record=False, log=None,
-              secant=False, deadzone=DEADZONE):
+              secant=False, deadzone=DEADZONE, start="network"):
     """Run nsteps load steps: plain (no model), with the learned start
-    (model), or with the last increment repeated (secant=True, the ablation
-    of the learned start without its network).
+    (model; start="network": the network's start, "best": the better of the
+    network's start and the repeated last increment by the linearised
+    residual), or with the last increment repeated (secant=True, the
+    ablation of the learned start without its network).
 
     Returns a dict of per-step statistics, wall time, the final state and,
     with record=True, the (features, targets) rows of every step."""
@@ -141,9 +142,11 @@ def run_steps(problem, nsteps, params=None, model=None, record=False, log=None,
     for k in range(nsteps):
         hist = model is not None or record or secant
         F = fb.rows(k, d1, d2, phi) if (model is not None or record) else None
-        if model is not None:
+        if model is not None and start == "best":
             st = q.load_step(candidates=[fb.guess(u_prev, d1, None, phi),
                                          fb.guess(u_prev, d1, model.forward(F), phi, deadzone)])
+        elif model is not None:
+            st = q.load_step(fb.guess(u_prev, d1, model.forward(F), phi, deadzone))
         elif secant:
             st = q.load_step(fb.guess(u_prev, d1, None, phi))
         else:
@@ -178,7 +181,7 @@ def summary(run):
     return {"newton_iters": int(sum(s["newton_iters"] for s in st)),
             "cg_iters": int(sum(s["lin_iters"] for s in st)),
             "guess_used": int(sum(1 for s in st if s["used_guess"])),
-            "network_start_used": int(sum(1 for s in st if s["used_guess"] == 2)),
+
             "wall_s": round(run["wall_s"], 4),
             "solver_ms": round(sum(s["ms"] for s in st), 2),
             "all_steps_converged": bool(tol_ok)}
@@ -240,8 +243,16 @@ def evaluate(model, problems, nsteps, max_newton=500, log=print, deadzone=DEADZO
                        "u_rel_l2_vs_plain": float(du), "broken_bonds_differing": diff,
                        "broken_bonds_plain": int(np.count_nonzero(a["bonds"]))}
         if ablation:
-            c = run_steps(p, nsteps, params, secant=True)
-            res[p.name]["secant_only"] = summary(c)
+            for key, kw in (("secant_only", dict(secant=True)),
+                            ("best_of_two", dict(model=model, deadzone=deadzone, start="best"))):
+                c = run_steps(p, nsteps, params, **kw)
+                sc = summary(c)
+                sc["speedup_wall"] = round(sa["wall_s"] / c["wall_s"], 3)
+                sc["u_rel_l2_vs_plain"] = float(np.linalg.norm(c["u"] - a["u"]) /
+                                                max(np.linalg.norm(a["u"]), 1e-300))
+                sc["broken_bonds_differing"] = int(np.count_nonzero((a["bonds"] != 0) !=
+                                                                    (c["bonds"] != 0)))
+                res[p.name][key] = sc
         log("%s: %s" % (p.name, json.dumps(res[p.name])))
     return res
 

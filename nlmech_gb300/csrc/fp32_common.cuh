@@ -162,9 +162,11 @@ __device__ __forceinline__ void st_pair(float4 *p, int64_t j, const df v[3]) {
   }
 }
 
-// Prescribed (du, dv) of one dof as double-float pairs.
-__device__ __forceinline__ void bc_df(const DevPtrs &D, const BCTable &T, int ref, int c, double t,
-                                      df &u, df &v) {
+// Prescribed (du, dv) of one dof as double-float pairs.  Kept out of line:
+// only nodes with prescribed dofs call it, and inlined, its FP64 time
+// functions were if-converted into the path of every node.
+static __device__ __noinline__ void bc_df(const DevPtrs &D, const BCTable &T, int ref, int c, double t,
+                                   df &u, df &v) {
   double du, dv;
   bc_dof(D, T, ref, c, t, du, dv);
   u = df_from_double(du);
@@ -185,6 +187,11 @@ __device__ __forceinline__ void integrate_node32(const StepParams &P, const Para
     for (int c = 0; c < DIM; c++) f[c] = (float)(fe[c] + (double)fint[c]);
   }
   const int ref = (fl & 7) ? D.bcref[i] : -1;
+  double t_now = 0., t_next = 0.;
+  if (fl & 7) {
+    t_now = t_now_of(A);
+    t_next = t_next_of(A);
+  }
   df un[3], vn[3];
   if (SCHEME == NLM_VELOCITY_VERLET) {
     float vh_[3], vl_[3];
@@ -216,12 +223,12 @@ __device__ __forceinline__ void integrate_node32(const StepParams &P, const Para
       } else {
         df du, dv;
         if (!FIRST) {
-          bc_df(D, T, ref, c, t_now_of(A), du, dv);
+          bc_df(D, T, ref, c, t_now, du, dv);
           vn[c] = dv;
         } else {
           vn[c] = v;
         }
-        bc_df(D, T, ref, c, t_next_of(A), du, dv);
+        bc_df(D, T, ref, c, t_next, du, dv);
         un[c] = du;
       }
     }
@@ -238,7 +245,7 @@ __device__ __forceinline__ void integrate_node32(const StepParams &P, const Para
         un[c] = df_add(u, inc);
         vn[c] = df_mul_c(df_sub(un[c], u), Q.idt_hi, Q.idt_lo);
       } else {
-        bc_df(D, T, ref, c, t_next_of(A), un[c], vn[c]);
+        bc_df(D, T, ref, c, t_next, un[c], vn[c]);
       }
     }
     st_pair<DIM>(D.v32[1 - A.cur], i, vn);

@@ -221,6 +221,10 @@ __global__ void k_scatter_vec(int64_t n, int S, int dim, const int *perm, const 
   const double *p = src + 3 * (int64_t)perm[i];
   for (int d = 0; d < S; d++) dst[S * i + d] = (d < dim && d < 3) ? p[d] : 0.;
 }
+__global__ void k_nonfinite(int64_t m, const double *a, int *flag) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k < m && !isfinite(a[k])) atomicExch(flag, 1);
+}
 __global__ void k_scatter_split(int64_t n, int S, int dim, const int *perm, const double *src,
                                 float4 *dst) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -341,7 +345,8 @@ struct nlm_fd {
   int64_t n_fbc_nodes = 0;
   BCTable FT{};
   // staging
-  double *stage = nullptr;
+  double *stage = nullptr;   // 3 slots of 3n doubles (u, v, f in Point3 layout)
+  int *bad_input = nullptr;  // set by k_nonfinite
   float *dmg_phi = nullptr, *dmg_Z = nullptr;
   unsigned long long *counter = nullptr;
   // CUDA-graph replay of the step loop
@@ -1099,7 +1104,8 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
   }
 
   // ---- state ----
-  TRY(h->alloc(&h->stage, 3 * n));
+  TRY(h->alloc(&h->stage, 9 * n));
+  TRY(h->alloc(&h->bad_input, 1));
   if (h->precision == NLM_PREC_FP64) {
     TRY(h->alloc(&D.u64[0], (size_t)S * n));
     TRY(h->alloc(&D.u64[1], (size_t)S * n));
@@ -1229,33 +1235,34 @@ int nlm_fd_get_state(nlm_fd *h, double *u, double *v, double *f) {
   const int *P = h->D.perm_dev;
   const unsigned g = nblk(n, 256);
   const bool fp32 = h->precision == NLM_PREC_FP32C;
+  // gather each requested field into its own staging slot, copy all out,
+  // synchronise once
+  double *su = h->stage, *sv = h->stage + 3 * n, *sf = h->stage + 6 * n;
   if (u) {
     if (fp32)
-      k_gather_split<<<g, 256, 0, s>>>(n, h->S, P, h->D.u32[h->cur], h->stage);
+      k_gather_split<<<g, 256, 0, s>>>(n, h->S, P, h->D.u32[h->cur], su);
     else
-      k_gather_vec<<<g, 256, 0, s>>>(n, h->S, P, h->D.u64[h->cur], h->stage);
+      k_gather_vec<<<g, 256, 0, s>>>(n, h->S, P, h->D.u64[h->cur], su);
     NLM_CUDA(cudaGetLastError());
-    NLM_CUDA(cudaMemcpyAsync(u, h->stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
-    NLM_CUDA(cudaStreamSynchronize(s));
+    NLM_CUDA(cudaMemcpyAsync(u, su, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
   }
   if (v) {
     if (fp32)
-      k_gather_split<<<g, 256, 0, s>>>(n, h->S, P, h->D.v32[h->vidx()], h->stage);
+      k_gather_split<<<g, 256, 0, s>>>(n, h->S, P, h->D.v32[h->vidx()], sv);
     else
-      k_gather_vec<<<g, 256, 0, s>>>(n, h->S, P, h->D.v[h->vidx()], h->stage);
+      k_gather_vec<<<g, 256, 0, s>>>(n, h->S, P, h->D.v[h->vidx()], sv);
     NLM_CUDA(cudaGetLastError());
-    NLM_CUDA(cudaMemcpyAsync(v, h->stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
-    NLM_CUDA(cudaStreamSynchronize(s));
+    NLM_CUDA(cudaMemcpyAsync(v, sv, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
   }
   if (f) {
     if (fp32)
-      k_gather_f32<<<g, 256, 0, s>>>(n, h->S, P, h->D.f32, h->stage);
+      k_gather_f32<<<g, 256, 0, s>>>(n, h->S, P, h->D.f32, sf);
     else
-      k_gather_vec<<<g, 256, 0, s>>>(n, h->S, P, h->D.f64, h->stage);
+      k_gather_vec<<<g, 256, 0, s>>>(n, h->S, P, h->D.f64, sf);
     NLM_CUDA(cudaGetLastError());
-    NLM_CUDA(cudaMemcpyAsync(f, h->stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
-    NLM_CUDA(cudaStreamSynchronize(s));
+    NLM_CUDA(cudaMemcpyAsync(f, sf, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
   }
+  NLM_CUDA(cudaStreamSynchronize(s));
   return NLM_OK;
 }
 
@@ -1410,29 +1417,32 @@ int nlm_fd_step_host(nlm_fd *h, double *u, double *v, double *f, int64_t nsteps)
     return nlm_fd_get_state(h, u, v, f);
   }
   const int64_t n = h->n;
-  if (!finite_all(u, 3 * n) || !finite_all(v, 3 * n) || !finite_all(f, 3 * n))
-    return fail(NLM_ERR_NONFINITE, "non-finite state");
   cudaStream_t s = h->stream;
   const int *P = h->D.perm_dev;
   const unsigned g = nblk(n, 256);
   const bool fp32 = h->precision == NLM_PREC_FP32C;
-  NLM_CUDA(cudaMemcpyAsync(h->stage, u, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
-  if (fp32)
-    k_scatter_split<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.u32[h->cur]);
-  else
-    k_scatter_vec<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.u64[h->cur]);
+  // upload u, v, f into their staging slots, check them for non-finite
+  // values on the device, and only then replace the state
+  double *su = h->stage, *sv = h->stage + 3 * n, *sf = h->stage + 6 * n;
+  NLM_CUDA(cudaMemsetAsync(h->bad_input, 0, sizeof(int), s));
+  NLM_CUDA(cudaMemcpyAsync(su, u, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  NLM_CUDA(cudaMemcpyAsync(sv, v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  NLM_CUDA(cudaMemcpyAsync(sf, f, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  k_nonfinite<<<nblk(9 * n, 256), 256, 0, s>>>(9 * n, h->stage, h->bad_input);
   NLM_CUDA(cudaGetLastError());
-  NLM_CUDA(cudaMemcpyAsync(h->stage, v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
-  if (fp32)
-    k_scatter_split<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.v32[h->vidx()]);
-  else
-    k_scatter_vec<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.v[h->vidx()]);
-  NLM_CUDA(cudaGetLastError());
-  NLM_CUDA(cudaMemcpyAsync(h->stage, f, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
-  if (fp32)
-    k_scatter_f32<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.f32);
-  else
-    k_scatter_vec<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.f64);
+  int bad = 0;
+  NLM_CUDA(cudaMemcpyAsync(&bad, h->bad_input, sizeof(int), cudaMemcpyDeviceToHost, s));
+  NLM_CUDA(cudaStreamSynchronize(s));
+  if (bad) return fail(NLM_ERR_NONFINITE, "non-finite state");
+  if (fp32) {
+    k_scatter_split<<<g, 256, 0, s>>>(n, h->S, h->dim, P, su, h->D.u32[h->cur]);
+    k_scatter_split<<<g, 256, 0, s>>>(n, h->S, h->dim, P, sv, h->D.v32[h->vidx()]);
+    k_scatter_f32<<<g, 256, 0, s>>>(n, h->S, h->dim, P, sf, h->D.f32);
+  } else {
+    k_scatter_vec<<<g, 256, 0, s>>>(n, h->S, h->dim, P, su, h->D.u64[h->cur]);
+    k_scatter_vec<<<g, 256, 0, s>>>(n, h->S, h->dim, P, sv, h->D.v[h->vidx()]);
+    k_scatter_vec<<<g, 256, 0, s>>>(n, h->S, h->dim, P, sf, h->D.f64);
+  }
   NLM_CUDA(cudaGetLastError());
   cudaError_t e = launch_drift(h->P, h->D, h->T, h->cur, h->time + h->dt, fp32, s);
   if (e != cudaSuccess) return cuda_fail(e, "drift kernel");

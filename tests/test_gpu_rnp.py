@@ -211,6 +211,23 @@ def test_step_host_matches_run(gpu):
             assert rel_max(u, ua) < 1e-12 and rel_max(v, va) < 1e-9
 
 
+def test_step_host_rejects_nonfinite_state(gpu):
+    """A non-finite value in the host state is found on the device before
+    the state is replaced: the call fails and the model is unchanged."""
+    p = configs.rnp_plate(30, 1e-3, 3, 0.008, 0.1, 2e-8, 50, seed=2)
+    m = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_THREAD)
+    u, v, f = np.zeros((p.n, 3)), np.zeros((p.n, 3)), np.zeros((p.n, 3))
+    m.step_host(u, v, f, nsteps=3)
+    t0 = m.time()
+    u0 = m.state()[0].copy()
+    bad = v.copy()
+    bad[7, 1] = np.nan
+    with pytest.raises(gpu.NLMError):
+        m.step_host(u, bad, f, nsteps=1)
+    assert m.time() == t0
+    assert np.array_equal(m.state()[0], u0)
+
+
 def test_runs_are_deterministic(gpu):
     p = configs.config0()
     for prec in (abi.FP64, abi.FP32C):

@@ -249,6 +249,21 @@ int nlm_fd_get_bond_state(nlm_fd *h, uint8_t *broken);
 int nlm_fd_damage(nlm_fd *h, float *phi, float *Z);
 /* Number of broken bonds (directed). */
 int nlm_fd_count_broken(nlm_fd *h, int64_t *count);
+/* Overwrite the bond state (inverse of nlm_fd_get_bond_state). */
+int nlm_fd_set_bond_state(nlm_fd *h, const uint8_t *broken);
+
+/* ---- checkpoint / restart ----------------------------------------------
+ * The reference's restart (fDModel.cpp:102-131, reader.cpp:149-173) reloads
+ * u and v from a VTU file but not the bond state, so a restarted fracture
+ * run heals its cracks.  A checkpoint here holds u, v, f, the bond state
+ * (one byte per bond), the step counter and time in one binary file:
+ *   "NLMCKPT" magic, int32 version, dim, precision, material, started,
+ *   int64 n, nnz, step, double time, dt, then u, v, f (3n doubles each,
+ *   caller's node order) and the bond bytes (nlm_fd_get_bond_state order).
+ * Loading into a handle created from the same description continues the
+ * run as if it had not stopped (bit for bit in FP64 plain). */
+int nlm_fd_save(nlm_fd *h, const char *path);
+int nlm_fd_load(nlm_fd *h, const char *path);
 /* Work decomposition actually used (enum nlm_decomposition). */
 int nlm_fd_decomposition(const nlm_fd *h, int *decomp);
 /* Average device time of the bond-force kernel over the launches since the

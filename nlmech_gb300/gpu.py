@@ -124,6 +124,18 @@ class FDModel:
         v = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
         _check(load().nlm_fd_set_state(self.h, abi.dptr(u), abi.dptr(v)))
 
+    def set_bond_state(self, broken):
+        b = np.ascontiguousarray(broken, dtype=np.uint8)
+        _check(load().nlm_fd_set_bond_state(self.h, abi.ptr(b, C.c_uint8)))
+
+    def save(self, path):
+        """Checkpoint u, v, f, bond state, step and time to a binary file."""
+        _check(load().nlm_fd_save(self.h, str(path).encode()))
+
+    def load(self, path):
+        """Continue from a checkpoint written by save() for the same model."""
+        _check(load().nlm_fd_load(self.h, str(path).encode()))
+
     def step_host(self, u, v, f, nsteps=1):
         """Drop-in step on host arrays u, v, f (3 doubles per node, updated
         in place); passing back the previous call's arrays continues the run."""

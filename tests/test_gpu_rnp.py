@@ -258,3 +258,32 @@ def test_tile_decomposition_rejected_where_unsupported(gpu):
     p = configs.config0()
     with pytest.raises(gpu.NLMError):
         gpu.FDModel(p, precision=abi.FP64, decomposition=abi.DECOMP_TILE)
+
+
+def test_checkpoint_restart_continues_the_run(gpu, tmp_path):
+    """Save after 150 steps of a growing crack, load into a fresh handle,
+    run on: the state, broken bonds and time equal those of the run that
+    never stopped (bit for bit in FP64, FP32C within its split rounding)."""
+    p = configs.rnp_plate(48, 1e-3, 3, 0.012, 0.5, 2e-8, 300, seed=7)
+    for prec in (abi.FP64, abi.FP32C):
+        a = gpu.FDModel(p, precision=prec, decomposition=abi.DECOMP_THREAD)
+        a.run(150)
+        path = tmp_path / ("ckpt_%d.bin" % prec)
+        a.save(path)
+        a.run(150)
+        b = gpu.FDModel(p, precision=prec, decomposition=abi.DECOMP_THREAD)
+        b.load(path)
+        b.run(150)
+        assert b.time() == a.time()
+        assert np.array_equal(b.bond_state(), a.bond_state())
+        assert int(a.bond_state().sum()) > 1000
+        ua, va, fa = a.state()
+        ub, vb, fb = b.state()
+        if prec == abi.FP64:
+            assert np.array_equal(ua, ub) and np.array_equal(va, vb) and np.array_equal(fa, fb)
+        else:
+            assert rel_max(ub, ua) < 1e-12 and rel_max(vb, va) < 1e-9
+    # a checkpoint of another model is refused
+    q = gpu.FDModel(configs.rnp_plate(40, 1e-3, 3, 0.01, 0.5, 2e-8, 10, seed=1))
+    with pytest.raises(gpu.NLMError):
+        q.load(path)

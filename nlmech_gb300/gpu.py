@@ -124,6 +124,23 @@ class FDModel:
         v = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
         _check(load().nlm_fd_set_state(self.h, abi.dptr(u), abi.dptr(v)))
 
+    def write_vtu(self, path, tags=("Displacement", "Velocity", "Force", "Damage_Phi",
+                                    "Damage_Z")):
+        """One output step in the reference's VTU layout (model::Output,
+        src/model/util.cpp:4-191): points at x + u and the requested tags."""
+        from . import vtu
+        u, v, f = self.state()
+        phi = Z = None
+        if "Damage_Phi" in tags or "Damage_Z" in tags:
+            phi, Z = self.damage()
+        t, _ = self.time()
+        vtu.write_vtu(path, self.problem.x, u=u,
+                      v=v if "Velocity" in tags else None,
+                      f=f if ("Force" in tags or "Force_Density" in tags) else None,
+                      volume=self.problem.volume,
+                      phi=phi if "Damage_Phi" in tags else None,
+                      Z=Z if "Damage_Z" in tags else None, time=t)
+
     def set_bond_state(self, broken):
         b = np.ascontiguousarray(broken, dtype=np.uint8)
         _check(load().nlm_fd_set_bond_state(self.h, abi.ptr(b, C.c_uint8)))

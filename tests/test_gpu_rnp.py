@@ -287,3 +287,20 @@ def test_checkpoint_restart_continues_the_run(gpu, tmp_path):
     q = gpu.FDModel(configs.rnp_plate(40, 1e-3, 3, 0.01, 0.5, 2e-8, 10, seed=1))
     with pytest.raises(gpu.NLMError):
         q.load(path)
+
+
+def test_write_vtu_output_step(gpu, tmp_path):
+    from nlmech_gb300 import vtu
+    p = configs.rnp_plate(30, 1e-3, 3, 0.008, 0.3, 2e-8, 50, seed=2)
+    m = gpu.FDModel(p, precision=abi.FP64)
+    m.run(50)
+    path = tmp_path / "output_50.vtu"
+    m.write_vtu(path)
+    d = vtu.read_vtu(str(path))
+    u, v, f = m.state()
+    phi, Z = m.damage()
+    assert np.array_equal(d["Displacement"], u) and np.array_equal(d["Velocity"], v)
+    assert np.array_equal(d["Points"], p.x + u)
+    assert np.array_equal(d["Force"], f * p.volume[:, None])
+    assert np.array_equal(d["Damage_Phi"], phi) and np.array_equal(d["Damage_Z"], Z)
+    assert d["TIME"][0] == m.time()[0]

@@ -249,6 +249,13 @@ int nlm_fd_get_bond_state(nlm_fd *h, uint8_t *broken);
 int nlm_fd_damage(nlm_fd *h, float *phi, float *Z);
 /* Number of broken bonds (directed). */
 int nlm_fd_count_broken(nlm_fd *h, int64_t *count);
+/* Energies of computePostProcFields (fDModel.cpp:651-778), RNPBond, per node
+ * in the caller's order (any may be NULL): strain energy (Strain_Energy),
+ * work done u . f_ext (Work_Done), kinetic energy, and the strain energy of
+ * nodes with Z > 1 (Fracture_Perienergy_Total); totals[4] their sums, in
+ * FP64 (the reference sums the float arrays in float). */
+int nlm_fd_energies(nlm_fd *h, float *strain, float *work, float *kinetic, float *fracture,
+                    double *totals);
 /* Overwrite the bond state (inverse of nlm_fd_get_bond_state). */
 int nlm_fd_set_bond_state(nlm_fd *h, const uint8_t *broken);
 

@@ -176,6 +176,92 @@ __global__ void k_damage(const StepParams P, const DevPtrs D, int cur, bool fp32
   if (Z) Z[i] = (float)z;
 }
 
+// Energies of FDModel::computePostProcFields (fDModel.cpp:651-778), RNPBond:
+// strain energy V_i sum_j E_ij with E_ij the energy of getBondEF
+// (rnpBond.cpp:267-300; a bond past its critical strain counts as broken, the
+// bond state itself is left alone), work done u_i . f_ext_i, kinetic energy
+// rho |v_i|^2 V_i / 2, and the strain energy again where Z_i > 1 - 1e-10
+// (fracture energy).  FP64 in the reference's operation order.
+template <int DIM>
+__global__ void k_energy(const StepParams P, const DevPtrs D, int cur, int vcur, bool fp32,
+                         const double *fext, float *strain, float *work, float *kinetic, float *fracture) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  double xi[3], ui[3], vi[3];
+  ld_node<DIM>(D.pos64, i, xi);
+  if (fp32) {
+    ld_split<DIM>(D.u32[cur], i, ui);
+    ld_split<DIM>(D.v32[vcur], i, vi);
+  } else {
+    ld_node<DIM>(D.u64[cur], i, ui);
+    ld_node<DIM>(D.v[vcur], i, vi);
+  }
+  const uint8_t fl = D.flags[i];
+  const double voli = D.vol64[i];
+  double energy = 0., z = 0.;
+  const int64_t r0 = D.rowptr[i], r1 = D.rowptr[i + 1];
+  for (int64_t k = r0; k < r1; k++) {
+    const int j = D.cols[k];
+    const int kk = (int)(k - r0);
+    bool fs = (D.bits[(int64_t)(kk >> 5) * P.npad + i] >> (kk & 31)) & 1u;
+    double xj[3], uj[3];
+    ld_node<DIM>(D.pos64, j, xj);
+    if (fp32)
+      ld_split<DIM>(D.u32[cur], j, uj);
+    else
+      ld_node<DIM>(D.u64[cur], j, uj);
+    double dx = xj[0] - xi[0], dy = xj[1] - xi[1], dz = DIM == 3 ? xj[2] - xi[2] : 0.;
+    double rr = dx * dx + dy * dy;
+    if (DIM == 3) rr = rr + dz * dz;
+    const double rji = sqrt(rr);
+    double dotp = dx * (uj[0] - ui[0]) + dy * (uj[1] - ui[1]);
+    if (DIM == 3) dotp = dotp + dz * (uj[2] - ui[2]);
+    const double S = dotp / rr;
+    double volj = D.vol64[j];
+    if (dGT(rji, P.check_low)) volj = volj * ((P.check_up - rji) / P.h);
+    const double infl = influence_d(P, rji / P.delta);
+    const bool breakable = !((fl | D.flags[j]) & FLAG_NOFAIL);
+    if (breakable) {
+      if (P.irrev && !fs && dGT(fabs(S), P.fsc * (P.rbar / sqrt(rji)))) fs = true;
+      if (!fs)
+        energy += (infl * P.C * (1. - exp(-P.beta * rji * S * S)) / P.invF) * volj;
+      else
+        energy += infl * P.C / P.invF * volj;
+    } else {
+      energy += (infl * P.C * P.beta * rji * S * S / P.invF) * volj;
+    }
+    double sr = 0.;
+    if (dGT(rji, 1.0E-12)) sr = fabs(S) / (P.rbar / sqrt(rji));
+    if (dLT(z, sr)) z = sr;
+  }
+  if (strain) strain[i] = (float)(energy * voli);
+  if (work) {
+    double fe[3] = {0., 0., 0.};
+    if (fl & FLAG_FBC) ld_node<DIM>(fext, i, fe);
+    double w = ui[0] * fe[0] + ui[1] * fe[1];
+    w = w + ui[2] * fe[2];
+    work[i] = (float)w;
+  }
+  if (kinetic) {
+    double vv = vi[0] * vi[0] + vi[1] * vi[1];
+    vv = vv + vi[2] * vi[2];
+    kinetic[i] = (float)(0.5 * P.rho * vv * voli);
+  }
+  if (fracture) fracture[i] = dGT(z, 1.0 - 1.0E-10) ? (float)(energy * voli) : 0.f;
+}
+
+cudaError_t launch_energy(const StepParams &P, const DevPtrs &D, int cur, int vcur, bool fp32,
+                          const double *fext, float *strain, float *work, float *kinetic,
+                          float *fracture, cudaStream_t s) {
+  if (P.n == 0) return cudaSuccess;
+  const unsigned grid = (unsigned)((P.n + 127) / 128);
+  if (P.dim == 2)
+    k_energy<2><<<grid, 128, 0, s>>>(P, D, cur, vcur, fp32, fext, strain, work, kinetic, fracture);
+  else
+    k_energy<3><<<grid, 128, 0, s>>>(P, D, cur, vcur, fp32, fext, strain, work, kinetic, fracture);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_damage(const StepParams &P, const DevPtrs &D, int cur, bool fp32, bool es,
                           float *phi, float *Z, cudaStream_t s) {
   if (P.n == 0) return cudaSuccess;

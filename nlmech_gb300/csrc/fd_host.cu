@@ -349,6 +349,8 @@ struct nlm_fd {
   double *stage = nullptr;   // 3 slots of 3n doubles (u, v, f in Point3 layout)
   int *bad_input = nullptr;  // set by k_nonfinite
   float *dmg_phi = nullptr, *dmg_Z = nullptr;
+  float *en_buf = nullptr;     // nlm_fd_energies: 4 n floats
+  double *en_fext = nullptr;   // external force at the current time, S n doubles
   unsigned long long *counter = nullptr;
   // CUDA-graph replay of the step loop
   int graph_steps = 0;
@@ -1486,6 +1488,45 @@ int nlm_fd_damage(nlm_fd *h, float *phi, float *Z) {
     if (phi) phi[h->perm[i]] = a[i];
     if (Z) Z[h->perm[i]] = b[i];
   }
+  return NLM_OK;
+}
+
+int nlm_fd_energies(nlm_fd *h, float *strain, float *work, float *kinetic, float *fracture,
+                    double *totals) {
+  if (!h) return fail(NLM_ERR_INVALID, "null handle");
+  if (h->material != NLM_MAT_RNP_BOND) return fail(NLM_ERR_UNSUPPORTED, "energies are for RNPBond");
+  const int64_t n = h->n;
+  cudaStream_t s = h->stream;
+  if (!h->en_buf) {
+    if (h->alloc(&h->en_buf, (size_t)4 * n) != cudaSuccess ||
+        h->alloc(&h->en_fext, (size_t)h->S * n) != cudaSuccess)
+      return fail(NLM_ERR_OOM, "energy buffers");
+  }
+  // f_ext at the current time, as computePostProcFields evaluates it
+  NLM_CUDA(cudaMemsetAsync(h->en_fext, 0, sizeof(double) * h->S * n, s));
+  if (h->n_fbc_nodes > 0) {
+    k_fbc_apply<<<nblk(h->n_fbc_nodes, 128), 128, 0, s>>>(h->n_fbc_nodes, h->S, h->fbc_nodes,
+                                                          h->fbc_iptr, h->fbc_items, h->FT,
+                                                          h->time, h->en_fext);
+    NLM_CUDA(cudaGetLastError());
+  }
+  float *e4 = h->en_buf;
+  cudaError_t e = launch_energy(h->P, h->D, h->cur, h->vidx(), h->precision == NLM_PREC_FP32C,
+                                h->en_fext, e4, e4 + n, e4 + 2 * n, e4 + 3 * n, s);
+  if (e != cudaSuccess) return cuda_fail(e, "energy kernel");
+  std::vector<float> a((size_t)4 * n);
+  NLM_CUDA(cudaMemcpyAsync(a.data(), e4, sizeof(float) * 4 * n, cudaMemcpyDeviceToHost, s));
+  NLM_CUDA(cudaStreamSynchronize(s));
+  float *out[4] = {strain, work, kinetic, fracture};
+  double tot[4] = {0., 0., 0., 0.};
+  for (int q = 0; q < 4; q++)
+    for (int64_t i = 0; i < n; i++) {
+      const float v = a[(size_t)q * n + i];
+      tot[q] += v;
+      if (out[q]) out[q][h->perm[i]] = v;
+    }
+  if (totals)
+    for (int q = 0; q < 4; q++) totals[q] = tot[q];
   return NLM_OK;
 }
 

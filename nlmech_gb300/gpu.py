@@ -194,6 +194,15 @@ class FDModel:
         _check(load().nlm_fd_damage(self.h, abi.ptr(phi, C.c_float), abi.ptr(Z, C.c_float)))
         return phi, Z
 
+    def energies(self):
+        """(strain, work, kinetic, fracture) per node (float32) and their
+        sums, as computePostProcFields (fDModel.cpp:651-778) forms them."""
+        e = np.zeros((4, self.n), dtype=np.float32)
+        tot = np.zeros(4)
+        _check(load().nlm_fd_energies(self.h, *[abi.ptr(e[q], C.c_float) for q in range(4)],
+                  abi.dptr(tot)))
+        return e, tot
+
     def decomposition(self):
         d = C.c_int()
         _check(load().nlm_fd_decomposition(self.h, C.byref(d)))

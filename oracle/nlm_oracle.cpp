@@ -988,6 +988,57 @@ int orc_fd_damage(orc_fd *h, float *phi, float *Z) {
   return NLM_OK;
 }
 
+// FDModel::computePostProcFields energies (fDModel.cpp:651-778), RNPBond:
+// strain energy (sum_j getBondEF energy) V_i with the bond breaking of
+// getBondEF applied to a copy of the state, work done u_i . f_ext(t),
+// kinetic energy rho |v_i|^2 V_i / 2, fracture energy where Z_i > 1 - 1e-10
+// (0 elsewhere).  totals[4]: FP64 sums of the float fields.
+int orc_fd_energies(orc_fd *h, float *strain, float *work, float *kinetic, float *fracture,
+                    double *totals) {
+  Model &m = h->m;
+  if (m.mat.kind != NLM_MAT_RNP_BOND) return NLM_ERR_UNSUPPORTED;
+  std::vector<double> fext(3 * m.n, 0.);
+  apply_fload(m, h->time, fext.data());
+  std::vector<float> e(4 * m.n);
+  const double rho = m.mat.density;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < m.n; i++) {
+    double energy = 0., z = 0.;
+    const double *xi = &m.x[3 * i], *ui = &m.u[3 * i], *vi = &m.v[3 * i];
+    for (int64_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++) {
+      uint8_t fs = m.broken[k];
+      double F[3], en = 0.;
+      rnp_bond(m, m.u.data(), i, k, fs, F, &en, false);
+      energy += en;
+      const int64_t j = m.cols[k];
+      const double *xj = &m.x[3 * j], *uj = &m.u[3 * j];
+      double rji = dist3(xj, xi);
+      double dx[3] = {xj[0] - xi[0], xj[1] - xi[1], xj[2] - xi[2]};
+      double du[3] = {uj[0] - ui[0], uj[1] - ui[1], uj[2] - ui[2]};
+      double Sji = dot3(dx, du) / dot3(dx, dx);
+      double sr = 0.;
+      if (dGT(rji, 1.0E-12)) sr = std::abs(Sji) / (m.rnp.rbar / std::sqrt(rji));
+      if (dLT(z, sr)) z = sr;
+    }
+    const double voli = m.vol[i];
+    const double *fe = &fext[3 * i];
+    e[i] = float(energy * voli);
+    e[m.n + i] = float(ui[0] * fe[0] + ui[1] * fe[1] + ui[2] * fe[2]);
+    e[2 * m.n + i] = float(0.5 * rho * (vi[0] * vi[0] + vi[1] * vi[1] + vi[2] * vi[2]) * voli);
+    e[3 * m.n + i] = dGT(z, 1.0 - 1.0E-10) ? float(energy * voli) : 0.f;
+  }
+  float *out[4] = {strain, work, kinetic, fracture};
+  for (int q = 0; q < 4; q++) {
+    double t = 0.;
+    for (int64_t i = 0; i < m.n; i++) {
+      t += e[q * m.n + i];
+      if (out[q]) out[q][i] = e[q * m.n + i];
+    }
+    if (totals) totals[q] = t;
+  }
+  return NLM_OK;
+}
+
 int orc_fd_es_fields(orc_fd *h, double *omega, double *mw, double *theta) {
   Model &m = h->m;
   if (m.mat.kind != NLM_MAT_ELASTIC_STATE) return fail(NLM_ERR_INVALID, "not ElasticState");

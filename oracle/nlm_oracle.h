@@ -55,6 +55,10 @@ int orc_fd_get_time(const orc_fd *h, double *t, int64_t *n);
 int orc_fd_get_bond_state(const orc_fd *h, uint8_t *broken);
 int orc_fd_set_bond_state(orc_fd *h, const uint8_t *broken);
 int orc_fd_damage(orc_fd *h, float *phi, float *Z);
+/* Energies of computePostProcFields (RNPBond): strain, work done, kinetic,
+ * fracture, per node, and their sums. */
+int orc_fd_energies(orc_fd *h, float *strain, float *work, float *kinetic, float *fracture,
+                    double *totals);
 /* Fixity bits per node as set by ULoading (uLoading.cpp:99-102). */
 int orc_fd_get_fixity(const orc_fd *h, uint8_t *fix);
 /* ElasticState helpers (volumeCorrection.cpp:25-67,

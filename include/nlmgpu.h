@@ -127,7 +127,14 @@ typedef struct nlm_bc_set {
   double spatial_params[2];
 } nlm_bc_set;
 
-/* One pre-crack (inp::EdgeCrack with activation time < 0, or a 3-D plane). */
+/* One crack (inp::EdgeCrack, or a 3-D plane).  timed = 0: a pre-crack, cut
+ * at creation (an EdgeCrack with activation time < 0, fracture.cpp:20-43).
+ * timed = 1: cut by the explicit model after the first step whose end time t
+ * has activation_time definitely less than t (Fracture::addCrack,
+ * fracture.cpp:45-70, called after every step at fDModel.cpp:366-373); at
+ * most one timed crack is cut per step, in array order.  At most 32 timed
+ * cracks per model; the batched and quasi-static models take pre-cracks
+ * only. */
 typedef struct nlm_crack {
   int kind;            /* enum nlm_crack_kind                              */
   int orientation;     /* EdgeCrack d_o: 1 = along x, -1 = along y, 0 = angle */
@@ -135,6 +142,8 @@ typedef struct nlm_crack {
   double theta;        /* EdgeCrack angle for orientation 0               */
   double z0;           /* plane kind: plane height                        */
   double lo[2], hi[2]; /* plane kind: patch [lo0,hi0] x [lo1,hi1]          */
+  int timed;           /* 0: pre-crack; 1: cut at activation_time          */
+  double activation_time; /* EdgeCrack "Activation_Time" (timed = 1)     */
 } nlm_crack;
 
 /* inp::MaterialDeck fields used on the hot path (materialDeck.h). */
@@ -256,6 +265,15 @@ int nlm_fd_count_broken(nlm_fd *h, int64_t *count);
  * FP64 (the reference sums the float arrays in float). */
 int nlm_fd_energies(nlm_fd *h, float *strain, float *work, float *kinetic, float *fracture,
                     double *totals);
+/* Reaction force of FDModel::computeForce (fDModel.cpp:543-580), 2-D RNPBond:
+ * "Reaction_Force" R_i (reaction[3n], caller's order), "Total_Reaction_Force"
+ * |R_i| (total[n]) and the sum of R_i over the nodes (sum[3]); any may be
+ * NULL.  R_i sums V_i F_ij over the bonds that is_reaction_force (:582-605)
+ * selects: node i in max_y - 1.5 delta < y < max_y - delta and the bond
+ * meeting the line y = max_y - delta + 1e-6, with util::geometry's
+ * doLinesIntersect as written (its orientation test truncates the cross
+ * product to an int).  The bounding box is fe::Mesh::computeBBox's. */
+int nlm_fd_reaction_force(nlm_fd *h, double *reaction, double *total, double *sum);
 /* Overwrite the bond state (inverse of nlm_fd_get_bond_state). */
 int nlm_fd_set_bond_state(nlm_fd *h, const uint8_t *broken);
 

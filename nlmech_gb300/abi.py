@@ -68,6 +68,8 @@ class Crack(C.Structure):
         ("z0", C.c_double),
         ("lo", C.c_double * 2),
         ("hi", C.c_double * 2),
+        ("timed", C.c_int),
+        ("activation_time", C.c_double),
     ]
 
 

@@ -250,6 +250,101 @@ __global__ void k_energy(const StepParams P, const DevPtrs D, int cur, int vcur,
   if (fracture) fracture[i] = dGT(z, 1.0 - 1.0E-10) ? (float)(energy * voli) : 0.f;
 }
 
+// util::geometry::direction (utilGeom.cpp:317-326): the orientation of C
+// against the line A-B.  The cross product is stored in an int, so it is
+// truncated toward zero before its sign is taken.
+__device__ int geo_direction(double ax, double ay, double bx, double by, double cx, double cy) {
+  const int val = (int)((by - ay) * (cx - bx) - (bx - ax) * (cy - by));
+  if (val == 0) return 0;
+  return val < 0 ? 2 : 1;
+}
+
+// util::geometry::onLine (utilGeom.cpp:308-315), as written there.
+__device__ bool geo_on_line(double ax, double ay, double bx, double by, double cx, double cy) {
+  return cx <= fmax(ax, bx) && cx <= fmin(ax, bx) && cy <= fmax(ay, by) && cy <= fmin(ay, by);
+}
+
+// util::geometry::doLinesIntersect (utilGeom.cpp:281-306) of A-B and C-D.
+__device__ bool geo_lines_intersect(double ax, double ay, double bx, double by, double cx,
+                                    double cy, double dx, double dy) {
+  const int d1 = geo_direction(ax, ay, bx, by, cx, cy);
+  const int d2 = geo_direction(ax, ay, bx, by, dx, dy);
+  const int d3 = geo_direction(cx, cy, dx, dy, ax, ay);
+  const int d4 = geo_direction(cx, cy, dx, dy, bx, by);
+  if (d1 != d2 && d3 != d4) return true;
+  if (d1 == 0 && geo_on_line(ax, ay, bx, by, cx, cy)) return true;
+  if (d2 == 0 && geo_on_line(ax, ay, bx, by, dx, dy)) return true;
+  if (d3 == 0 && geo_on_line(cx, cy, dx, dy, ax, ay)) return true;
+  if (d4 == 0 && geo_on_line(cx, cy, dx, dy, bx, by)) return true;
+  return false;
+}
+
+// Reaction force of FDModel::computeForce (fDModel.cpp:543-580) with
+// is_reaction_force (:582-605), 2-D RNPBond: for a node i in the layer
+// max_y - 1.5 delta < y_i < max_y - delta, R_i = sum of V_i F_ij over the bonds
+// i-j that meet the line y = max_y - delta + 1e-6 from min_x to max_x (F_ij
+// the getBondEF force, a bond past its critical strain counting as broken);
+// R_i = 0 elsewhere.  R: 2 doubles per node.
+__global__ void k_reaction(const StepParams P, const DevPtrs D, int cur, bool fp32, double min_x,
+                           double max_x, double max_y, double *R) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  double xi[3], ui[3];
+  ld_node<2>(D.pos64, i, xi);
+  double r0 = 0., r1 = 0.;
+  if (xi[1] > max_y - 1.5 * P.delta && xi[1] < max_y - P.delta) {
+    if (fp32)
+      ld_split<2>(D.u32[cur], i, ui);
+    else
+      ld_node<2>(D.u64[cur], i, ui);
+    const double ay = max_y - P.delta + 1e-6;
+    const uint8_t fl = D.flags[i];
+    const double voli = D.vol64[i];
+    const int64_t k0 = D.rowptr[i], k1 = D.rowptr[i + 1];
+    for (int64_t k = k0; k < k1; k++) {
+      const int j = D.cols[k];
+      double xj[3], uj[3], e[3];
+      ld_node<2>(D.pos64, j, xj);
+      if (!geo_lines_intersect(min_x, ay, max_x, ay, xi[0], xi[1], xj[0], xj[1])) continue;
+      if (fp32)
+        ld_split<2>(D.u32[cur], j, uj);
+      else
+        ld_node<2>(D.u64[cur], j, uj);
+      const int kk = (int)(k - k0);
+      bool fs = (D.bits[(int64_t)(kk >> 5) * P.npad + i] >> (kk & 31)) & 1u;
+      const bool breakable = !((fl | D.flags[j]) & FLAG_NOFAIL);
+      double volj = D.vol64[j];
+      const double s = rnp_bond64<2>(P, xi, ui, xj, uj, volj, breakable, fs, e);
+      double f0, f1;
+      if (!fs || !breakable) {
+        f0 = s * e[0];
+        f1 = s * e[1];
+      } else if (P.contact) {
+        const double y0 = (xj[0] + uj[0]) - (xi[0] + ui[0]);
+        const double y1 = (xj[1] + uj[1]) - (xi[1] + ui[1]);
+        const double Rl = sqrt(y0 * y0 + y1 * y1 + 0. * 0.);
+        double sf = P.contact_kn * (voli * volj / (voli + volj)) * (P.contact_rc - Rl) / Rl;
+        if (sf < 0.) sf = 0.;
+        f0 = 0. + -sf * y0;
+        f1 = 0. + -sf * y1;
+      } else {
+        f0 = f1 = 0.;
+      }
+      r0 = r0 + voli * f0;
+      r1 = r1 + voli * f1;
+    }
+  }
+  R[2 * i] = r0;
+  R[2 * i + 1] = r1;
+}
+
+cudaError_t launch_reaction(const StepParams &P, const DevPtrs &D, int cur, bool fp32,
+                            double min_x, double max_x, double max_y, double *R, cudaStream_t s) {
+  if (P.n == 0) return cudaSuccess;
+  k_reaction<<<(unsigned)((P.n + 127) / 128), 128, 0, s>>>(P, D, cur, fp32, min_x, max_x, max_y, R);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_energy(const StepParams &P, const DevPtrs &D, int cur, int vcur, bool fp32,
                           const double *fext, float *strain, float *work, float *kinetic,
                           float *fracture, cudaStream_t s) {

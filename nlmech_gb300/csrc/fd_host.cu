@@ -345,12 +345,17 @@ struct nlm_fd {
   FBCItem *fbc_items = nullptr;
   int64_t n_fbc_nodes = 0;
   BCTable FT{};
+  double bbox_lo[3] = {0., 0., 0.}, bbox_hi[3] = {0., 0., 0.};  // fe::Mesh::computeBBox
+  // timed cracks (Fracture::addCrack): cut after a step, bit c of cracks_on set once cut
+  std::vector<nlm_crack> timed_cracks;
+  uint32_t cracks_on = 0;
   // staging
   double *stage = nullptr;   // 3 slots of 3n doubles (u, v, f in Point3 layout)
   int *bad_input = nullptr;  // set by k_nonfinite
   float *dmg_phi = nullptr, *dmg_Z = nullptr;
   float *en_buf = nullptr;     // nlm_fd_energies: 4 n floats
   double *en_fext = nullptr;   // external force at the current time, S n doubles
+  double *rf_buf = nullptr;    // nlm_fd_reaction_force: 2 n doubles
   unsigned long long *counter = nullptr;
   // CUDA-graph replay of the step loop
   int graph_steps = 0;
@@ -402,13 +407,18 @@ bool finite_all(const double *a, int64_t n) {
 // :146-185): a node is not interior when it lies within tol of the mesh
 // bounding box.  fe::Mesh::computeBBox (mesh.cpp:311-324) starts both corners
 // at the origin and only widens them, so the box always contains the origin.
-void nofail_flags(const double *x, int64_t n, double tol, std::vector<uint8_t> &interior) {
-  double lo[3] = {0., 0., 0.}, hi[3] = {0., 0., 0.};
+void mesh_bbox(const double *x, int64_t n, double lo[3], double hi[3]) {
+  for (int dd = 0; dd < 3; dd++) lo[dd] = hi[dd] = 0.;
   for (int64_t i = 0; i < n; i++)
     for (int dd = 0; dd < 3; dd++) {
       if (hLT(x[3 * i + dd], lo[dd])) lo[dd] = x[3 * i + dd];
       if (hLT(hi[dd], x[3 * i + dd])) hi[dd] = x[3 * i + dd];
     }
+}
+
+void nofail_flags(const double *x, int64_t n, double tol, std::vector<uint8_t> &interior) {
+  double lo[3], hi[3];
+  mesh_bbox(x, n, lo, hi);
   for (int64_t i = 0; i < n; i++) {
     const double *p = x + 3 * i;
     interior[i] = !(hLT(p[0], lo[0] + tol) || hLT(p[1], lo[1] + tol) ||
@@ -716,6 +726,51 @@ int capture_graph(nlm_fd *h, int c0) {
   return NLM_OK;
 }
 
+// Fracture::addCrack (fracture.cpp:45-70) for the step that ended at h->time:
+// the first timed crack not yet cut whose activation time is definitely less
+// than that time is cut into the bond state; one crack per call.  The
+// reference calls it after the step's output (fDModel.cpp:352-373); here it
+// runs just before the next step's launch, which is the same point for the
+// dynamics and leaves the state read between run calls equal to the one the
+// reference's output of that step sees.
+int add_crack(nlm_fd *h) {
+  for (size_t c = 0; c < h->timed_cracks.size(); c++) {
+    if (h->cracks_on >> c & 1u) continue;
+    if (!dLT(h->timed_cracks[c].activation_time, h->time)) continue;
+    NLM_CUDA(apply_precrack(h->n, h->S, h->D.pos64, h->D.rowptr, h->D.cols, h->timed_cracks[c],
+                            h->P.npad, h->D.bits, h->stream));
+    h->cracks_on |= 1u << c;
+    return NLM_OK;
+  }
+  return NLM_OK;
+}
+
+// True if a timed crack would be cut before one of the next nsteps steps
+// (checked at the times h->time, h->time + dt, ..., accumulated as in do_run).
+bool crack_due(const nlm_fd *h, int64_t nsteps) {
+  if ((uint64_t)h->cracks_on + 1 == (1ull << h->timed_cracks.size())) return false;
+  double t = h->time;
+  for (int64_t k = 1; k < nsteps; k++) t = t + h->dt;
+  for (size_t c = 0; c < h->timed_cracks.size(); c++)
+    if (!(h->cracks_on >> c & 1u) && dLT(h->timed_cracks[c].activation_time, t)) return true;
+  return false;
+}
+
+int single_steps(nlm_fd *h, int64_t nsteps) {
+  for (int64_t s = 0; s < nsteps; s++) {
+    int rc;
+    if (!h->timed_cracks.empty() && h->step > 0 && (rc = add_crack(h))) return rc;
+    const double tm = h->time + h->dt;
+    h->cur = 1 - h->cur;
+    if ((rc = apply_fbc(h, tm))) return rc;
+    StepArgs a{h->cur, false, tm, tm + h->dt, nullptr, 0, h->n};
+    if ((rc = launch_step(h, a))) return rc;
+    h->time = tm;
+    h->step++;
+  }
+  return NLM_OK;
+}
+
 int do_run(nlm_fd *h, int64_t nsteps) {
   if (!h->started) {
     int rc = apply_bc(h, h->time);
@@ -727,6 +782,13 @@ int do_run(nlm_fd *h, int64_t nsteps) {
   }
   const int G = h->graph_steps;
   while (G > 0 && nsteps >= G) {
+    if (!h->timed_cracks.empty() && crack_due(h, G)) {
+      // a crack is cut within this chunk: its steps run one by one
+      int rc = single_steps(h, G);
+      if (rc) return rc;
+      nsteps -= G;
+      continue;
+    }
     if (!h->gexec[h->cur]) {
       int rc = capture_graph(h, h->cur);
       if (rc) return rc;
@@ -746,17 +808,7 @@ int do_run(nlm_fd *h, int64_t nsteps) {
     h->step += G;
     nsteps -= G;
   }
-  for (int64_t s = 0; s < nsteps; s++) {
-    const double tm = h->time + h->dt;
-    h->cur = 1 - h->cur;
-    int rc = apply_fbc(h, tm);
-    if (rc) return rc;
-    StepArgs a{h->cur, false, tm, tm + h->dt, nullptr, 0, h->n};
-    if ((rc = launch_step(h, a))) return rc;
-    h->time = tm;
-    h->step++;
-  }
-  return NLM_OK;
+  return single_steps(h, nsteps);
 }
 
 }  // namespace
@@ -973,6 +1025,11 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
   for (int c = 0; c < d->n_cracks; c++) {
     if (d->cracks[c].kind == NLM_CRACK_EDGE && d->dim != 2)
       return bail(fail(NLM_ERR_INVALID, "edge pre-cracks are 2-D only (input.cpp:298-307)"));
+    if (d->cracks[c].timed) {
+      if (h->timed_cracks.size() >= 32) return bail(fail(NLM_ERR_INVALID, "more than 32 timed cracks"));
+      h->timed_cracks.push_back(d->cracks[c]);
+      continue;
+    }
     TRY(apply_precrack(n, S, nb.pos, nb.rowptr, nb.cols, d->cracks[c], P.npad, bits, s));
   }
 
@@ -999,6 +1056,7 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
   }
   h->T.nsets = d->n_ubc;
   if (d->no_fail != NLM_NOFAIL_OFF) nofail_flags(d->x, n, d->no_fail_tol, interior);
+  mesh_bbox(d->x, n, h->bbox_lo, h->bbox_hi);
   // force BC items per node, in set order
   std::vector<std::vector<FBCItem>> fitems(n);
   for (int sidx = 0; sidx < d->n_fbc; sidx++) {
@@ -1388,7 +1446,8 @@ int nlm_fd_set_bond_state(nlm_fd *h, const uint8_t *broken) {
 namespace {
 struct CkptHeader {
   char magic[8];
-  int32_t version, dim, precision, material, started, pad;
+  int32_t version, dim, precision, material, started;
+  uint32_t cracks_on;  // timed cracks already cut (bit c = crack c)
   int64_t n, nnz, step;
   double time, dt;
 };
@@ -1410,6 +1469,7 @@ int nlm_fd_save(nlm_fd *h, const char *path) {
   hd.precision = h->precision;
   hd.material = h->material;
   hd.started = h->started ? 1 : 0;
+  hd.cracks_on = h->cracks_on;
   hd.n = n;
   hd.nnz = h->nnz;
   hd.step = h->step;
@@ -1435,9 +1495,11 @@ int nlm_fd_load(nlm_fd *h, const char *path) {
   std::vector<uint8_t> b((size_t)h->nnz);
   bool ok = std::fread(&hd, sizeof(hd), 1, fp) == 1 && std::memcmp(hd.magic, kCkptMagic, 8) == 0;
   if (ok && (hd.version != 1 || hd.n != n || hd.nnz != h->nnz || hd.dim != h->dim ||
-             hd.material != h->material || hd.dt != h->dt)) {
+             hd.material != h->material || hd.dt != h->dt ||
+             (uint64_t)hd.cracks_on >= (1ull << h->timed_cracks.size()))) {
     std::fclose(fp);
-    return fail(NLM_ERR_INVALID, "checkpoint does not match this model (n, bonds, dim, material, dt)");
+    return fail(NLM_ERR_INVALID,
+                "checkpoint does not match this model (n, bonds, dim, material, dt, timed cracks)");
   }
   ok = ok && std::fread(st.data(), sizeof(double), st.size(), fp) == st.size() &&
        std::fread(b.data(), 1, b.size(), fp) == b.size();
@@ -1447,6 +1509,7 @@ int nlm_fd_load(nlm_fd *h, const char *path) {
   if (rc) return rc;
   h->time = hd.time;
   h->step = hd.step;
+  h->cracks_on = hd.cracks_on;
   if (!hd.started) {
     h->started = false;
     return nlm_fd_set_state(h, st.data(), st.data() + 3 * n);
@@ -1527,6 +1590,38 @@ int nlm_fd_energies(nlm_fd *h, float *strain, float *work, float *kinetic, float
     }
   if (totals)
     for (int q = 0; q < 4; q++) totals[q] = tot[q];
+  return NLM_OK;
+}
+
+int nlm_fd_reaction_force(nlm_fd *h, double *reaction, double *total, double *sum) {
+  if (!h) return fail(NLM_ERR_INVALID, "null handle");
+  if (h->material != NLM_MAT_RNP_BOND || h->dim != 2)
+    return fail(NLM_ERR_UNSUPPORTED, "the reaction force is for 2-D RNPBond");
+  const int64_t n = h->n;
+  cudaStream_t s = h->stream;
+  if (!h->rf_buf && h->alloc(&h->rf_buf, (size_t)2 * n) != cudaSuccess)
+    return fail(NLM_ERR_OOM, "reaction-force buffer");
+  cudaError_t e = launch_reaction(h->P, h->D, h->cur, h->precision == NLM_PREC_FP32C,
+                                  h->bbox_lo[0], h->bbox_hi[0], h->bbox_hi[1], h->rf_buf, s);
+  if (e != cudaSuccess) return cuda_fail(e, "reaction-force kernel");
+  std::vector<double> a((size_t)2 * n);
+  NLM_CUDA(cudaMemcpyAsync(a.data(), h->rf_buf, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, s));
+  NLM_CUDA(cudaStreamSynchronize(s));
+  double tot[3] = {0., 0., 0.};
+  for (int64_t i = 0; i < n; i++) {
+    const double rx = a[2 * i], ry = a[2 * i + 1];
+    const int64_t o = h->perm[i];
+    if (reaction) {
+      reaction[3 * o] = rx;
+      reaction[3 * o + 1] = ry;
+      reaction[3 * o + 2] = 0.;
+    }
+    if (total) total[o] = std::sqrt(rx * rx + ry * ry + 0. * 0.);
+    tot[0] += rx;
+    tot[1] += ry;
+  }
+  if (sum)
+    for (int c = 0; c < 3; c++) sum[c] = tot[c];
   return NLM_OK;
 }
 
@@ -2020,6 +2115,8 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
     for (int c = 0; c < d.n_cracks; c++) {
       if (d.cracks[c].kind == NLM_CRACK_EDGE && d.dim != 2)
         return bail(fail(NLM_ERR_INVALID, "edge pre-cracks are 2-D only"));
+      if (d.cracks[c].timed)
+        return bail(fail(NLM_ERR_UNSUPPORTED, "the batched model takes pre-cracks only"));
       BTRY(apply_precrack(d.n_nodes, S, pos64, rowptr, cols, d.cracks[c], N, bits, st, b->off[s]));
     }
     const int set0 = (int)bct.size();
@@ -2456,6 +2553,9 @@ int nlm_qs_create(const nlm_fd_desc *desc, const nlm_qs_params *prm, nlm_qs **ou
     return fail(NLM_ERR_UNSUPPORTED, "the GPU quasi-static solver is for RNPBond");
   if (desc->material.apply_contact)
     return fail(NLM_ERR_UNSUPPORTED, "the quasi-static solver has no contact term");
+  for (int c = 0; c < desc->n_cracks; c++)
+    if (desc->cracks && desc->cracks[c].timed)
+      return fail(NLM_ERR_UNSUPPORTED, "the quasi-static solver takes pre-cracks only");
   if (prm->max_newton < 1 || !(prm->tol > 0.) || prm->lin_max_iters < 1 || !(prm->lin_tol > 0.))
     return fail(NLM_ERR_INVALID, "bad solver parameters");
   nlm_fd_desc d = *desc;

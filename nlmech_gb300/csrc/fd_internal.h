@@ -88,6 +88,8 @@ cudaError_t launch_drift32(const StepParams &P, const DevPtrs &D, const BCTable 
 cudaError_t launch_es_setup(const StepParams &P, const DevPtrs &D, double *mw, cudaStream_t s);
 cudaError_t launch_damage(const StepParams &P, const DevPtrs &D, int cur, bool fp32,
                           bool es, float *phi, float *Z, cudaStream_t s);
+cudaError_t launch_reaction(const StepParams &P, const DevPtrs &D, int cur, bool fp32,
+                            double min_x, double max_x, double max_y, double *R, cudaStream_t s);
 cudaError_t launch_energy(const StepParams &P, const DevPtrs &D, int cur, int vcur, bool fp32,
                           const double *fext, float *strain, float *work, float *kinetic,
                           float *fracture, cudaStream_t s);

@@ -55,7 +55,9 @@ class BC:
 
 @dataclass
 class Crack:
-    """A pre-crack: inp::EdgeCrack (2-D) or a planar patch (3-D)."""
+    """A crack: inp::EdgeCrack (2-D) or a planar patch (3-D).
+    activation_time < 0 (the default, as in fractureDeck.h:103): a pre-crack;
+    >= 0: "Activation_Time", cut by the explicit model during the run."""
     kind: str = "edge"
     orientation: int = 1
     pb: tuple = (0.0, 0.0)
@@ -64,6 +66,7 @@ class Crack:
     z0: float = 0.0
     lo: tuple = (0.0, 0.0)
     hi: tuple = (0.0, 0.0)
+    activation_time: float = -1.0
 
     def to_c(self):
         c = abi.Crack()
@@ -75,6 +78,8 @@ class Crack:
         c.z0 = float(self.z0)
         c.lo[0], c.lo[1] = self.lo
         c.hi[0], c.hi[1] = self.hi
+        c.timed = int(self.activation_time >= 0.)
+        c.activation_time = float(self.activation_time)
         return c
 
 

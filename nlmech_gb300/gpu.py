@@ -203,6 +203,15 @@ class FDModel:
                   abi.dptr(tot)))
         return e, tot
 
+    def reaction_force(self):
+        """Reaction_Force (n, 3), Total_Reaction_Force (n,) and the sum (3,)
+        of FDModel::computeForce (fDModel.cpp:543-605)."""
+        R = np.zeros((self.n, 3))
+        t = np.zeros(self.n)
+        s = np.zeros(3)
+        _check(load().nlm_fd_reaction_force(self.h, abi.dptr(R), abi.dptr(t), abi.dptr(s)))
+        return R, t, s
+
     def decomposition(self):
         d = C.c_int()
         _check(load().nlm_fd_decomposition(self.h, C.byref(d)))

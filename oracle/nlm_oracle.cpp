@@ -431,6 +431,8 @@ struct Model {
   std::vector<int64_t> rowptr;
   std::vector<int32_t> cols;
   std::vector<uint8_t> broken;  // one byte per CSR entry
+  std::vector<nlm_crack> timed; // timed cracks (Activation_Time >= 0)
+  uint32_t cracks_on = 0;       // bit c: timed crack c has been cut
   std::vector<uint8_t> fix;     // bit d = dof d fixed
   std::vector<uint8_t> interior;
   std::vector<nlm_bc_set> ubc, fbc;
@@ -439,6 +441,43 @@ struct Model {
   // ElasticState fields
   std::vector<double> omega, mw, theta;
 };
+
+// Fracture::computeFracturedBondFd (fracture.cpp:74-160) over every node:
+// bonds that cross the crack are marked broken.
+void cut_crack(Model &m, const nlm_crack &ck) {
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < m.n; i++) {
+    const double *xi = &m.x[3 * i];
+    if (ck.kind == NLM_CRACK_PLANE) {
+      for (int64_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++)
+        if (plane_cuts(ck, xi, &m.x[3 * int64_t(m.cols[k])])) m.broken[k] = 1;
+      continue;
+    }
+    if (crack_pt_outside(ck, xi)) continue;
+    bool left = crack_left(ck, xi);
+    for (int64_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++) {
+      const double *xj = &m.x[3 * int64_t(m.cols[k])];
+      bool modify = !crack_pt_outside(ck, xj);
+      bool other = left ? !crack_left(ck, xj) : crack_left(ck, xj);
+      if (other && modify) m.broken[k] = 1;
+    }
+  }
+}
+
+// Fracture::addCrack (fracture.cpp:45-70) for a step that ended at time: the
+// first timed crack not yet cut whose activation time is definitely less than
+// time is cut; at most one per call.  Called before the next step rather than
+// after the step's output (fDModel.cpp:352-373): the same point for the
+// dynamics.
+void add_crack(Model &m, double time) {
+  for (size_t c = 0; c < m.timed.size(); c++) {
+    if (m.cracks_on >> c & 1u) continue;
+    if (!dLT(m.timed[c].activation_time, time)) continue;
+    cut_crack(m, m.timed[c]);
+    m.cracks_on |= 1u << c;
+    return;
+  }
+}
 
 int setup_model(const nlm_fd_desc *d, bool grid, Model &m) {
   if (!d || d->n_nodes < 0 || d->dim < 1 || d->dim > 3 || (d->n_nodes > 0 && (!d->x || !d->volume)))
@@ -469,27 +508,15 @@ int setup_model(const nlm_fd_desc *d, bool grid, Model &m) {
   for (int64_t i = 0; i < m.n; i++)
     std::copy(rows[i].begin(), rows[i].end(), m.cols.begin() + m.rowptr[i]);
   // pre-cracks (Fracture ctor, fracture.cpp:20-43: every crack with
-  // activation time < 0 is applied at construction)
+  // activation time < 0 is applied at construction); timed cracks wait for
+  // Fracture::addCrack
   m.broken.assign(m.cols.size(), 0);
   for (int c = 0; c < d->n_cracks; c++) {
-    const nlm_crack &ck = d->cracks[c];
-#pragma omp parallel for schedule(dynamic, 256)
-    for (int64_t i = 0; i < m.n; i++) {
-      const double *xi = &m.x[3 * i];
-      if (ck.kind == NLM_CRACK_PLANE) {
-        for (int64_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++)
-          if (plane_cuts(ck, xi, &m.x[3 * int64_t(m.cols[k])])) m.broken[k] = 1;
-        continue;
-      }
-      if (crack_pt_outside(ck, xi)) continue;
-      bool left = crack_left(ck, xi);
-      for (int64_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++) {
-        const double *xj = &m.x[3 * int64_t(m.cols[k])];
-        bool modify = !crack_pt_outside(ck, xj);
-        bool other = left ? !crack_left(ck, xj) : crack_left(ck, xj);
-        if (other && modify) m.broken[k] = 1;
-      }
-    }
+    if (d->cracks[c].timed) {
+      if (m.timed.size() >= 32) return fail(NLM_ERR_INVALID, "more than 32 timed cracks");
+      m.timed.push_back(d->cracks[c]);
+    } else
+      cut_crack(m, d->cracks[c]);
   }
   // interior flags (interiorFlags.cpp:27-100, 121-191)
   m.interior.assign(m.n, 1);
@@ -859,7 +886,8 @@ int orc_fd_get_neighbors(const orc_fd *h, int64_t *rowptr, int32_t *cols) {
 }
 
 // FDModel::integrate (fDModel.cpp:317-374) with integrateVerlet (:445-525)
-// or integrateCD (:376-443).  Output I/O and timed cracks are not part of it.
+// or integrateCD (:376-443), after the timed-crack check of the step before.
+// Output I/O is not part of it.
 int orc_fd_run(orc_fd *h, int64_t nsteps) {
   Model &m = h->m;
   double *u = m.u.data(), *v = m.v.data(), *f = m.f.data();
@@ -873,6 +901,7 @@ int orc_fd_run(orc_fd *h, int64_t nsteps) {
   }
   double rho = m.mat.density;
   for (int64_t s = 0; s < nsteps; s++) {
+    if (h->step > 0) add_crack(m, h->time);  // fDModel.cpp:366-373
     if (h->scheme == NLM_VELOCITY_VERLET) {
       double fact = 0.5 * h->dt / rho;
 #pragma omp parallel for schedule(static)
@@ -1036,6 +1065,68 @@ int orc_fd_energies(orc_fd *h, float *strain, float *work, float *kinetic, float
     }
     if (totals) totals[q] = t;
   }
+  return NLM_OK;
+}
+
+// util::geometry::direction / onLine / doLinesIntersect (utilGeom.cpp:281-326)
+// as written there: the orientation's cross product is stored in an int.
+int geo_direction(const double *A, const double *B, const double *C) {
+  int val = (int)((B[1] - A[1]) * (C[0] - B[0]) - (B[0] - A[0]) * (C[1] - B[1]));
+  if (val == 0) return 0;
+  return val < 0 ? 2 : 1;
+}
+bool geo_on_line(const double *A, const double *B, const double *C) {
+  return C[0] <= std::max(A[0], B[0]) && C[0] <= std::min(A[0], B[0]) &&
+         C[1] <= std::max(A[1], B[1]) && C[1] <= std::min(A[1], B[1]);
+}
+bool geo_lines_intersect(const double *A, const double *B, const double *C, const double *D) {
+  int d1 = geo_direction(A, B, C), d2 = geo_direction(A, B, D);
+  int d3 = geo_direction(C, D, A), d4 = geo_direction(C, D, B);
+  if (d1 != d2 && d3 != d4) return true;
+  if (d1 == 0 && geo_on_line(A, B, C)) return true;
+  if (d2 == 0 && geo_on_line(A, B, D)) return true;
+  if (d3 == 0 && geo_on_line(C, D, A)) return true;
+  if (d4 == 0 && geo_on_line(C, D, B)) return true;
+  return false;
+}
+
+// FDModel::computeForce reaction force (fDModel.cpp:543-605), 2-D RNPBond:
+// R[3n] per node, |R| per node, their sum.
+int orc_fd_reaction_force(orc_fd *h, double *R, double *total, double *sum) {
+  Model &m = h->m;
+  if (m.mat.kind != NLM_MAT_RNP_BOND || m.dim != 2) return NLM_ERR_UNSUPPORTED;
+  double lo[3] = {0., 0., 0.}, hi[3] = {0., 0., 0.};  // fe::Mesh::computeBBox
+  for (int64_t i = 0; i < m.n; i++)
+    for (int c = 0; c < 3; c++) {
+      if (dLT(m.x[3 * i + c], lo[c])) lo[c] = m.x[3 * i + c];
+      if (dLT(hi[c], m.x[3 * i + c])) hi[c] = m.x[3 * i + c];
+    }
+  const double delta = m.delta, eps = 1e-6;
+  const double A[2] = {lo[0], hi[1] - delta + eps}, B[2] = {hi[0], hi[1] - delta + eps};
+  std::vector<double> r(3 * m.n, 0.);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < m.n; i++) {
+    const double *xi = &m.x[3 * i];
+    if (!(xi[1] > hi[1] - 1.5 * delta && xi[1] < hi[1] - delta)) continue;
+    for (int64_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++) {
+      const double *xj = &m.x[3 * int64_t(m.cols[k])];
+      if (!geo_lines_intersect(A, B, xi, xj)) continue;
+      uint8_t fs = m.broken[k];
+      double F[3];
+      rnp_bond(m, m.u.data(), i, k, fs, F, nullptr, false);
+      for (int c = 0; c < 3; c++) r[3 * i + c] += m.vol[i] * F[c];
+    }
+  }
+  double s[3] = {0., 0., 0.};
+  for (int64_t i = 0; i < m.n; i++) {
+    const double *q = &r[3 * i];
+    if (R)
+      for (int c = 0; c < 3; c++) R[3 * i + c] = q[c];
+    if (total) total[i] = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+    for (int c = 0; c < 3; c++) s[c] += q[c];
+  }
+  if (sum)
+    for (int c = 0; c < 3; c++) sum[c] = s[c];
   return NLM_OK;
 }
 

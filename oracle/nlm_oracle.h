@@ -59,6 +59,8 @@ int orc_fd_damage(orc_fd *h, float *phi, float *Z);
  * fracture, per node, and their sums. */
 int orc_fd_energies(orc_fd *h, float *strain, float *work, float *kinetic, float *fracture,
                     double *totals);
+/* Reaction force of FDModel::computeForce (2-D RNPBond). */
+int orc_fd_reaction_force(orc_fd *h, double *R, double *total, double *sum);
 /* Fixity bits per node as set by ULoading (uLoading.cpp:99-102). */
 int orc_fd_get_fixity(const orc_fd *h, uint8_t *fix);
 /* ElasticState helpers (volumeCorrection.cpp:25-67,

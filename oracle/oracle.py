@@ -167,6 +167,15 @@ class OracleFD:
                   abi.dptr(tot)))
         return e, tot
 
+    def reaction_force(self):
+        """Reaction_Force (n, 3), Total_Reaction_Force (n,) and the sum (3,)
+        of FDModel::computeForce (fDModel.cpp:543-605)."""
+        R = np.zeros((self.n, 3))
+        t = np.zeros(self.n)
+        s = np.zeros(3)
+        _check(lib().orc_fd_reaction_force(self.h, abi.dptr(R), abi.dptr(t), abi.dptr(s)))
+        return R, t, s
+
     def es_fields(self):
         om = np.zeros(self.nnz())
         m = np.zeros(self.n)
@@ -356,3 +365,10 @@ class RefRNP:
         v = C.c_double()
         self._chk(ref_lib().ref_rnp_sc(self.h, C.c_double(r), C.byref(v)))
         return v.value
+
+    def energies(self):
+        """(strain, work, kinetic, fracture) per node from the reference's
+        getBondEF, FLoading::apply and computePostProcFields formulas."""
+        e = np.zeros((4, self.n), dtype=np.float32)
+        self._chk(ref_lib().ref_rnp_energies(self.h, *[abi.ptr(e[q], C.c_float) for q in range(4)]))
+        return e

@@ -161,6 +161,8 @@ struct ref_rnp {
   // FDModel::integrateVerlet (fDModel.cpp:445-525)
   void verlet() {
     const long long n = (long long)u.size();
+    // timed cracks of the step before (fDModel.cpp:366-373), after its output
+    if (step > 0) frac->addCrack(time, mesh->getNodesP(), neigh->getNeighborsListP());
     const double fact = 0.5 * dt / mat->getDensity();
 #pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; i++) {
@@ -252,6 +254,7 @@ int ref_rnp_create(const nlm_fd_desc *d, ref_rnp **out) {
       e.d_oldPb = e.d_initPb = e.d_pb;
       e.d_oldPt = e.d_initPt = e.d_pt;
       e.d_theta = c.theta;
+      if (c.timed) e.d_activationTime = c.activation_time;
       h->fdeck.d_cracks.push_back(e);
     }
     h->frac = new geometry::Fracture(&h->fdeck, h->mesh->getNodesP(),
@@ -378,6 +381,43 @@ int ref_rnp_get_state(const ref_rnp *h, double *u, double *v, double *f) {
 int ref_rnp_get_time(const ref_rnp *h, double *t, int64_t *n) {
   *t = h->time;
   *n = h->step;
+  return 0;
+}
+
+// FDModel::computePostProcFields energies (fDModel.cpp:651-778): strain
+// energy (sum of getBondEF energies) V_i, work done u_i . f_ext(t), kinetic
+// energy, and the strain energy where Z_i > 1 - 1e-10 (0 elsewhere).
+int ref_rnp_energies(ref_rnp *h, float *strain, float *work, float *kinetic, float *fracture) {
+  try {
+    const long long n = (long long)h->u.size();
+    std::vector<util::Point3> f_ext(n, util::Point3());
+    h->fload->apply(h->time, &f_ext, h->mesh);
+    for (long long i = 0; i < n; i++) {
+      double energy_i = 0., z = 0.;
+      auto xi = h->mesh->getNode(i);
+      auto ui = h->u[i];
+      const auto &row = h->neigh->getNeighbors((size_t)i);
+      for (size_t j = 0; j < row.size(); j++) {
+        energy_i += h->mat->getBondEF((size_t)i, j).second;
+        auto xj = h->mesh->getNode(row[j]);
+        auto uj = h->u[row[j]];
+        auto rji = xj.dist(xi);
+        auto Sji = h->mat->getS(xj - xi, uj - ui);
+        double sr = 0.;
+        if (util::compare::definitelyGreaterThan(rji, 1.0E-12))
+          sr = std::abs(Sji) / h->mat->getSc(rji);
+        if (util::compare::definitelyLessThan(z, sr)) z = sr;
+      }
+      const double voli = h->mesh->getNodalVolume(i);
+      strain[i] = float(energy_i * voli);
+      work[i] = float(ui.dot(f_ext[i]));
+      kinetic[i] = float(0.5 * h->mat->getDensity() * h->v[i].dot(h->v[i]) * voli);
+      fracture[i] = util::compare::definitelyGreaterThan(z, 1.0 - 1.0E-10)
+                        ? float(energy_i * voli) : 0.f;
+    }
+  } catch (const std::exception &e) {
+    return fail(e.what());
+  }
   return 0;
 }
 

@@ -30,9 +30,12 @@ def main():
         r.run(steps)
         u, v, f = r.state()
         t, n = r.time()
+        broken = r.bond_state()
+        energies = r.energies()  # strain, work, kinetic, fracture (computePostProcFields)
         out = os.path.join(HERE, "rnp_ref_%s.npz" % name)
         np.savez_compressed(out, u=u, v=v, f=f, rowptr=rowptr, cols=cols, precrack=pre,
-                            broken=r.bond_state(), fixity=r.fixity(), time=t, steps=n)
+                            broken=broken, fixity=r.fixity(), time=t, steps=n,
+                            energies=energies)
         print(out, os.path.getsize(out), "bytes,", int(r.bond_state().sum()), "broken")
 
 

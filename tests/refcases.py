@@ -2,7 +2,7 @@
 import numpy as np
 
 from nlmech_gb300 import abi, configs
-from nlmech_gb300.decks import BC
+from nlmech_gb300.decks import BC, Crack
 
 
 def fracture_plate():
@@ -60,6 +60,23 @@ def contact_plate():
     return p
 
 
+def timed_crack_plate():
+    """40 x 40 plate with a pre-crack and three timed cracks (Activation_Time):
+    one at t = 0 (cut after the first step), two at 3e-7 s (the first cut
+    after step 16, the second one step later: one crack per step)."""
+    p = configs.rnp_plate(40, 1e-3, 3, 0.008, 0.3, 2e-8, 200, seed=5)
+    W = 0.04
+    p.cracks += [
+        Crack(kind="edge", orientation=1, pb=(0.004, 0.3 * W), pt=(0.016, 0.3 * W),
+              activation_time=3e-7),
+        Crack(kind="edge", orientation=-1, pb=(0.7 * W, 0.006), pt=(0.7 * W, 0.018),
+              activation_time=3e-7),
+        Crack(kind="edge", orientation=1, pb=(0.022, 0.75 * W), pt=(0.034, 0.75 * W),
+              activation_time=0.0),
+    ]
+    return p
+
+
 # name -> (problem, Verlet steps) of the committed reference outputs
 # (tests/golden/rnp_ref_<name>.npz)
 GOLDEN_CASES = {
@@ -67,4 +84,5 @@ GOLDEN_CASES = {
     "loads_nofail_plate": (loads_nofail_plate, 200),
     "cube3d": (cube3d, 100),
     "contact_plate": (contact_plate, 300),
+    "timed_crack_plate": (timed_crack_plate, 200),
 }

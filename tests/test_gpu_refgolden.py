@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 RTOL = {"fracture_plate": 1e-12, "loads_nofail_plate": 1e-11, "cube3d": 1e-12,
-        "contact_plate": 1e-12}
+        "contact_plate": 1e-12, "timed_crack_plate": 1e-12}
 
 
 def _pairs(rowptr, cols, b):
@@ -44,6 +44,13 @@ def test_fp64_matches_reference_golden(gpu, name):
         assert _rel_max(a, z[k]) <= RTOL[name], (k, _rel_max(a, z[k]))
     assert _pairs(rowptr, cols, m.bond_state()) == _pairs(rowptr, cols, z["broken"])
     assert m.time() == (float(z["time"]), int(z["steps"]))
+    # computePostProcFields energies, float per node (1e-6 of each field's scale)
+    e = m.energies()[0]
+    for q in range(4):
+        if np.abs(z["energies"][q]).max() == 0:
+            assert np.abs(e[q]).max() == 0
+        else:
+            assert _rel_max(e[q], z["energies"][q]) <= 1e-6, q
 
 
 def test_fp32c_matches_reference_golden(gpu):

@@ -304,3 +304,64 @@ def test_write_vtu_output_step(gpu, tmp_path):
     assert np.array_equal(d["Force"], f * p.volume[:, None])
     assert np.array_equal(d["Damage_Phi"], phi) and np.array_equal(d["Damage_Z"], Z)
     assert d["TIME"][0] == m.time()[0]
+
+
+def test_timed_cracks_with_graph_replay(gpu, oracle):
+    """Timed cracks (Fracture::addCrack after every step) with and without
+    CUDA-graph replay: a graph chunk in which a crack falls due runs step by
+    step, so the broken bonds and u equal the oracle's at every check."""
+    import refcases
+    p = refcases.timed_crack_plate()
+    o = oracle.OracleFD(p)
+    rowptr, cols = o.neighbors()
+    runs = []
+    for prec, graph, dec in ((abi.FP64, 0, abi.DECOMP_THREAD), (abi.FP64, 8, abi.DECOMP_THREAD),
+                             (abi.FP32C, 8, abi.DECOMP_TILE)):
+        m = gpu.FDModel(p, precision=prec, decomposition=dec)
+        m.set_graph(graph)
+        runs.append((prec, m))
+    for n in (1, 15, 1, 1, 22, 160):
+        o.run(n)
+        ref = bonds_as_pairs(rowptr, cols, o.bond_state())
+        uo = o.state()[0]
+        for prec, m in runs:
+            m.run(n)
+            assert m.time() == o.time()
+            got = bonds_as_pairs(rowptr, cols, m.bond_state())
+            if prec == abi.FP64:
+                assert got == ref
+                assert rel_max(m.state()[0], uo) <= FP64_RTOL
+            else:
+                assert len(got ^ ref) <= FP32_BROKEN * len(ref)
+                assert rel_l2(m.state()[0], uo) <= FP32_L2
+
+
+def test_timed_crack_checkpoint_between_activations(gpu, tmp_path):
+    """A checkpoint taken after step 17 (one of the two cracks due at 3e-7 s
+    cut) restarts with the second still pending: it is cut before step 18."""
+    import refcases
+    p = refcases.timed_crack_plate()
+    a = gpu.FDModel(p, precision=abi.FP64)
+    a.run(17)
+    path = tmp_path / "timed.bin"
+    a.save(path)
+    n17 = int(a.bond_state().sum())
+    a.run(24)
+    b = gpu.FDModel(p, precision=abi.FP64)
+    b.load(path)
+    b.run(1)
+    assert int(b.bond_state().sum()) > n17 + 200  # the pending crack
+    b.run(23)
+    assert np.array_equal(a.bond_state(), b.bond_state())
+    assert np.array_equal(a.state()[0], b.state()[0])
+
+
+def test_timed_cracks_rejected_by_batch_and_qs(gpu):
+    import refcases
+    p = refcases.timed_crack_plate()
+    with pytest.raises(gpu.NLMError):
+        gpu.Batch([p])
+    q = configs.qs_plate(nx=40)
+    q.cracks[0].activation_time = 1.0
+    with pytest.raises(gpu.NLMError):
+        gpu.QSModel(q, gpu.qs_params())

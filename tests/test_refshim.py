@@ -14,7 +14,8 @@ import pytest
 from nlmech_gb300 import configs
 from oracle import oracle as orc
 
-from refcases import GOLDEN_CASES, contact_plate, cube3d, fracture_plate, loads_nofail_plate
+from refcases import (GOLDEN_CASES, contact_plate, cube3d, fracture_plate, loads_nofail_plate,
+                      timed_crack_plate)
 
 needs_ref = pytest.mark.skipif(not orc.refshim_available(),
                                reason="reference source tree not present")
@@ -68,6 +69,41 @@ def test_refshim_contact_bit_exact():
 
 
 @needs_ref
+def test_refshim_timed_cracks_bit_exact():
+    """Fracture::addCrack after every step's output: the crack at t = 0 is
+    cut before step 2, the two at 3e-7 s before steps 17 and 18 (one per
+    step)."""
+    p = timed_crack_plate()
+    r = orc.RefRNP(p)
+    o = orc.OracleFD(p)
+    counts = [int(r.bond_state().sum())]
+    for n in (1, 14, 1, 1, 1, 182):
+        r.run(n)
+        o.run(n)
+        assert np.array_equal(r.bond_state(), o.bond_state())
+        for a, b in zip(r.state(), o.state()):
+            assert np.array_equal(a, b)
+        counts.append(int(r.bond_state().sum()))
+    d = np.diff(counts)  # after steps 1, 15, 16, 17, 18, 200
+    assert d[0] < 50 and d[1] > 200 and d[2] < 50 and d[3] > 200 and d[4] > 200, counts
+
+
+@needs_ref
+@pytest.mark.parametrize("make,steps", [(loads_nofail_plate, 200), (fracture_plate, 300),
+                                        (cube3d, 50)])
+def test_refshim_energies_bit_exact(make, steps):
+    """computePostProcFields energies from the reference's getBondEF and
+    FLoading against the oracle's restatement."""
+    r = orc.RefRNP(make())
+    o = orc.OracleFD(make())
+    r.run(steps)
+    o.run(steps)
+    eo, tot = o.energies()
+    assert np.array_equal(r.energies(), eo)
+    assert np.allclose(tot, eo.astype(np.float64).sum(axis=1), rtol=1e-12, atol=0)
+
+
+@needs_ref
 def test_refshim_critical_stretch():
     p = configs.config0()
     r = orc.RefRNP(p)
@@ -97,3 +133,4 @@ def test_oracle_matches_reference_golden(name):
         assert np.array_equal(a, z[k]), k
     assert np.array_equal(o.bond_state(), z["broken"])
     assert o.time() == (float(z["time"]), int(z["steps"]))
+    assert np.array_equal(o.energies()[0], z["energies"])

@@ -258,6 +258,10 @@ int nlm_fd_get_bond_state(nlm_fd *h, uint8_t *broken);
 int nlm_fd_damage(nlm_fd *h, float *phi, float *Z);
 /* Number of broken bonds (directed). */
 int nlm_fd_count_broken(nlm_fd *h, int64_t *count);
+/* Fixity bits per node in the caller's order (bit d: dof d is prescribed by
+ * a Displacement_BC; fe::Mesh::getFixity as ULoading sets it,
+ * uLoading.cpp:99-102). */
+int nlm_fd_get_fixity(nlm_fd *h, uint8_t *fixity);
 /* Energies of computePostProcFields (fDModel.cpp:651-778), RNPBond, per node
  * in the caller's order (any may be NULL): strain energy (Strain_Energy),
  * work done u . f_ext (Work_Done), kinetic energy, and the strain energy of

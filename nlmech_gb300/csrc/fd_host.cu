@@ -1520,6 +1520,16 @@ int nlm_fd_load(nlm_fd *h, const char *path) {
   return nlm_fd_step_host(h, st.data(), st.data() + 3 * n, st.data() + 6 * n, 0);
 }
 
+int nlm_fd_get_fixity(nlm_fd *h, uint8_t *fixity) {
+  if (!h || !fixity) return fail(NLM_ERR_INVALID, "null argument");
+  std::vector<uint8_t> fl(h->n);
+  if (h->n)
+    NLM_CUDA(cudaMemcpyAsync(fl.data(), h->D.flags, h->n, cudaMemcpyDeviceToHost, h->stream));
+  NLM_CUDA(cudaStreamSynchronize(h->stream));
+  for (int64_t i = 0; i < h->n; i++) fixity[h->perm[i]] = fl[i] & 7u;
+  return NLM_OK;
+}
+
 int nlm_fd_count_broken(nlm_fd *h, int64_t *count) {
   if (!h || !count) return fail(NLM_ERR_INVALID, "null argument");
   NLM_CUDA(cudaMemsetAsync(h->counter, 0, sizeof(unsigned long long), h->stream));

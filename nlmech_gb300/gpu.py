@@ -194,6 +194,11 @@ class FDModel:
         _check(load().nlm_fd_damage(self.h, abi.ptr(phi, C.c_float), abi.ptr(Z, C.c_float)))
         return phi, Z
 
+    def fixity(self):
+        fx = np.zeros(self.n, dtype=np.uint8)
+        _check(load().nlm_fd_get_fixity(self.h, abi.ptr(fx, C.c_uint8)))
+        return fx
+
     def energies(self):
         """(strain, work, kinetic, fracture) per node (float32) and their
         sums, as computePostProcFields (fDModel.cpp:651-778) forms them."""

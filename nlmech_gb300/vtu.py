@@ -19,8 +19,10 @@ import zlib
 import numpy as np
 
 _VTK_TYPE = {np.dtype("<f8"): "Float64", np.dtype("<f4"): "Float32",
-             np.dtype("<i8"): "Int64", np.dtype("uint8"): "UInt8", np.dtype("<i4"): "Int32"}
-_NP_TYPE = {"Float64": "<f8", "Float32": "<f4", "Int64": "<i8", "UInt8": "u1", "Int32": "<i4"}
+             np.dtype("<i8"): "Int64", np.dtype("uint8"): "UInt8", np.dtype("<i4"): "Int32",
+             np.dtype("<u8"): "UInt64"}
+_NP_TYPE = {"Float64": "<f8", "Float32": "<f4", "Int64": "<i8", "UInt8": "u1", "Int32": "<i4",
+            "UInt64": "<u8"}
 _BLOCK = 1 << 15
 
 
@@ -41,7 +43,6 @@ def write_vtu(path, x, u=None, v=None, f=None, volume=None, phi=None, Z=None, fi
     times the nodal volume, as "Force"); phi, Z: damage fields; fixity:
     uint8 bits per node; extra: {name: array} more point data."""
     x = np.asarray(x, dtype=np.float64).reshape(-1, 3)
-    n = x.shape[0]
     pts = x + (np.asarray(u, dtype=np.float64).reshape(-1, 3) if u is not None else 0.)
     point_data = []
     if u is not None:
@@ -64,6 +65,16 @@ def write_vtu(path, x, u=None, v=None, f=None, volume=None, phi=None, Z=None, fi
     for name, a in (extra or {}).items():
         point_data.append((name, np.asarray(a)))
 
+    write_points(path, pts, point_data,
+                 [] if time is None else [("TIME", np.array([time], dtype=np.float64))])
+
+
+def write_points(path, points, point_data, field_data=()):
+    """Write a VTU of vertex cells at points (n, 3) with point_data and
+    field_data given as ordered [(name, array)] lists (model::Output's
+    appendPointData / appendFieldData, in the caller's order)."""
+    pts = np.asarray(points, dtype=np.float64).reshape(-1, 3)
+    n = pts.shape[0]
     chunks, off = [], [0]
 
     def add(arr):
@@ -85,9 +96,11 @@ def write_vtu(path, x, u=None, v=None, f=None, volume=None, phi=None, Z=None, fi
              '<VTKFile type="UnstructuredGrid" version="1.0" byte_order="LittleEndian" '
              'header_type="UInt32" compressor="vtkZLibDataCompressor">',
              '  <UnstructuredGrid>']
-    if time is not None:
-        lines += ['    <FieldData>', '      ' + tag("TIME", np.array([time], dtype=np.float64), 1),
-                  '    </FieldData>']
+    if field_data:
+        lines.append('    <FieldData>')
+        lines += ['      ' + tag(name, np.atleast_1d(np.asarray(a, dtype=np.float64)),
+                                 np.atleast_1d(a).size) for name, a in field_data]
+        lines.append('    </FieldData>')
     lines.append('    <Piece NumberOfPoints="%d" NumberOfCells="%d">' % (n, n))
     lines.append('      <PointData>')
     lines += ['        ' + tag(name, a) for name, a in point_data]

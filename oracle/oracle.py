@@ -372,3 +372,10 @@ class RefRNP:
         e = np.zeros((4, self.n), dtype=np.float32)
         self._chk(ref_lib().ref_rnp_energies(self.h, *[abi.ptr(e[q], C.c_float) for q in range(4)]))
         return e
+
+    def reaction_force(self):
+        """Reaction_Force (n, 3) from the reference's getBondEF and
+        util::geometry::doLinesIntersect."""
+        R = np.zeros((self.n, 3))
+        self._chk(ref_lib().ref_rnp_reaction_force(self.h, abi.dptr(R)))
+        return R

@@ -43,6 +43,7 @@
 #include "loading/fLoading.h"
 #include "loading/uLoading.h"
 #include "material/pd/rnpBond.h"
+#include "util/utilGeom.h"
 
 namespace {
 
@@ -414,6 +415,40 @@ int ref_rnp_energies(ref_rnp *h, float *strain, float *work, float *kinetic, flo
       kinetic[i] = float(0.5 * h->mat->getDensity() * h->v[i].dot(h->v[i]) * voli);
       fracture[i] = util::compare::definitelyGreaterThan(z, 1.0 - 1.0E-10)
                         ? float(energy_i * voli) : 0.f;
+    }
+  } catch (const std::exception &e) {
+    return fail(e.what());
+  }
+  return 0;
+}
+
+// Reaction force of FDModel::computeForce (fDModel.cpp:543-580): for the
+// bonds FDModel::is_reaction_force (:582-605) selects, V_i times the getBondEF
+// force, with the reference's util::geometry::doLinesIntersect and bounding box.
+int ref_rnp_reaction_force(ref_rnp *h, double *R) {
+  try {
+    const size_t n = h->u.size();
+    const auto bb = h->mesh->getBoundingBox();
+    const double delta = h->mdeck.d_horizon, eps = 1e-6;
+    const double min_x = bb.first[0], max_x = bb.second[0];
+    const double max_y = bb.second[1];
+    for (size_t i = 0; i < n; i++) {
+      auto r = util::Point3();
+      auto xi = h->mesh->getNode(i);
+      const auto &row = h->neigh->getNeighbors(i);
+      for (size_t j = 0; j < row.size(); j++) {
+        auto fe = h->mat->getBondEF(i, j);
+        auto xj = h->mesh->getNode(row[j]);
+        if (xi.d_y > max_y - 1.5 * delta && xi.d_y < max_y - delta) {
+          util::Point3 A = util::Point3(min_x, max_y - delta + eps, 0.);
+          util::Point3 B = util::Point3(max_x, max_y - delta + eps, 0.);
+          if (util::geometry::doLinesIntersect(A, B, xi, xj))
+            r += (h->mesh->getNodalVolume(i) * fe.first);
+        }
+      }
+      R[3 * i] = r.d_x;
+      R[3 * i + 1] = r.d_y;
+      R[3 * i + 2] = r.d_z;
     }
   } catch (const std::exception &e) {
     return fail(e.what());

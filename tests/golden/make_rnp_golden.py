@@ -32,10 +32,11 @@ def main():
         t, n = r.time()
         broken = r.bond_state()
         energies = r.energies()  # strain, work, kinetic, fracture (computePostProcFields)
+        extra = {"reaction": r.reaction_force()} if p.dim == 2 else {}
         out = os.path.join(HERE, "rnp_ref_%s.npz" % name)
         np.savez_compressed(out, u=u, v=v, f=f, rowptr=rowptr, cols=cols, precrack=pre,
                             broken=broken, fixity=r.fixity(), time=t, steps=n,
-                            energies=energies)
+                            energies=energies, **extra)
         print(out, os.path.getsize(out), "bytes,", int(r.bond_state().sum()), "broken")
 
 

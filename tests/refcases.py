@@ -77,6 +77,14 @@ def timed_crack_plate():
     return p
 
 
+def reaction_plate():
+    """40 x 40 plate at h = 1 m (horizon 3 m), pulled at 1e-4 m/s: the
+    reaction-force layer below the top boundary carries bond forces, and at
+    this scale the orientation test of the reference's doLinesIntersect
+    (an int-truncated cross product) separates the two sides of the line."""
+    return configs.rnp_plate(40, 1.0, 3, 8.0, 1e-4, 2e-5, 200, seed=2)
+
+
 # name -> (problem, Verlet steps) of the committed reference outputs
 # (tests/golden/rnp_ref_<name>.npz)
 GOLDEN_CASES = {
@@ -85,4 +93,5 @@ GOLDEN_CASES = {
     "cube3d": (cube3d, 100),
     "contact_plate": (contact_plate, 300),
     "timed_crack_plate": (timed_crack_plate, 200),
+    "reaction_plate": (reaction_plate, 200),
 }

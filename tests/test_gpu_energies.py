@@ -1,4 +1,5 @@
-"""Post-processing energies (nlm_fd_energies) against the oracle's
+"""Post-processing energies (nlm_fd_energies) and reaction force
+(nlm_fd_reaction_force) against the oracle's
 restatement of FDModel::computePostProcFields (fDModel.cpp:651-778).
 
 FP64 plain mode follows the reference's operation order, so per-node fields
@@ -88,3 +89,20 @@ def test_energies_unsupported_for_elastic_state(gpu):
     m = gpu.FDModel(configs.elastic_state_cube(8, 1e-3), precision=abi.FP64)
     with pytest.raises(gpu.NLMError):
         m.energies()
+
+
+def test_reaction_force_fp32c_and_limits(gpu):
+    """Reaction_Force in FP32C against the reference's golden output (1e-3
+    relative L2: the FP32C state's own bar is 1e-5 on u, and the bond forces
+    difference it), and the 3-D model refuses the 2-D layer definition."""
+    import os
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                             "rnp_ref_reaction_plate.npz"))
+    m = gpu.FDModel(refcases.reaction_plate(), precision=abi.FP32C)
+    m.run(int(z["steps"]))
+    R, tot, s = m.reaction_force()
+    assert np.linalg.norm(R - z["reaction"]) <= 1e-3 * np.linalg.norm(z["reaction"])
+    assert np.array_equal(np.abs(R).sum(axis=1) > 0, np.abs(z["reaction"]).sum(axis=1) > 0)
+    m3 = gpu.FDModel(refcases.cube3d(8), precision=abi.FP64)
+    with pytest.raises(gpu.NLMError):
+        m3.reaction_force()

@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 RTOL = {"fracture_plate": 1e-12, "loads_nofail_plate": 1e-11, "cube3d": 1e-12,
-        "contact_plate": 1e-12, "timed_crack_plate": 1e-12}
+        "contact_plate": 1e-12, "timed_crack_plate": 1e-12, "reaction_plate": 1e-12}
 
 
 def _pairs(rowptr, cols, b):
@@ -51,6 +51,13 @@ def test_fp64_matches_reference_golden(gpu, name):
             assert np.abs(e[q]).max() == 0
         else:
             assert _rel_max(e[q], z["energies"][q]) <= 1e-6, q
+    if "reaction" in z.files:
+        R, tot, s = m.reaction_force()
+        if np.abs(z["reaction"]).max() == 0:
+            assert np.abs(R).max() == 0
+        else:
+            assert _rel_max(R, z["reaction"]) <= RTOL[name]
+            assert np.allclose(s, z["reaction"].sum(axis=0), rtol=1e-9)
 
 
 def test_fp32c_matches_reference_golden(gpu):

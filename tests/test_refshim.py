@@ -15,7 +15,7 @@ from nlmech_gb300 import configs
 from oracle import oracle as orc
 
 from refcases import (GOLDEN_CASES, contact_plate, cube3d, fracture_plate, loads_nofail_plate,
-                      timed_crack_plate)
+                      reaction_plate, timed_crack_plate)
 
 needs_ref = pytest.mark.skipif(not orc.refshim_available(),
                                reason="reference source tree not present")
@@ -104,6 +104,22 @@ def test_refshim_energies_bit_exact(make, steps):
 
 
 @needs_ref
+def test_refshim_reaction_force_bit_exact():
+    """Reaction_Force of FDModel::computeForce from the reference's getBondEF
+    and doLinesIntersect against the oracle: non-zero on the 1 m plate, zero
+    on the 1 mm plate (the truncated orientation test)."""
+    for make, steps, nonzero in ((reaction_plate, 200, True), (fracture_plate, 300, False)):
+        r = orc.RefRNP(make())
+        o = orc.OracleFD(make())
+        r.run(steps)
+        o.run(steps)
+        R, tot, s = o.reaction_force()
+        assert np.array_equal(r.reaction_force(), R)
+        assert np.array_equal(tot, np.sqrt((R * R).sum(axis=1)))
+        assert (np.abs(R).sum() > 0) == nonzero
+
+
+@needs_ref
 def test_refshim_critical_stretch():
     p = configs.config0()
     r = orc.RefRNP(p)
@@ -134,3 +150,5 @@ def test_oracle_matches_reference_golden(name):
     assert np.array_equal(o.bond_state(), z["broken"])
     assert o.time() == (float(z["time"]), int(z["steps"]))
     assert np.array_equal(o.energies()[0], z["energies"])
+    if "reaction" in z.files:
+        assert np.array_equal(o.reaction_force()[0], z["reaction"])

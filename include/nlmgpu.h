@@ -397,6 +397,41 @@ int nlm_qs_get_bond_state(nlm_qs *q, uint8_t *broken);
 int nlm_qs_damage(nlm_qs *q, float *phi, float *Z);
 int nlm_qs_num_bonds(const nlm_qs *q, int64_t *nnz);
 
+/* ---- quasi-static ElasticState (the reference's QuasiStaticModel) -------
+ * QuasiStaticModel<ElasticState> (src/model/quasistatic/QuasiStaticModel.cpp,
+ * the reference's only quasi-static instantiation, :648): per load step n the
+ * force loading is added to the body force at time n dt, the displacement
+ * loading is applied, and Newton iterates while ||f + b|| >= tol (free dofs)
+ * and fewer than max_iters iterations ran (solver, :526-594).  The Jacobian is
+ * assembly_jacobian_matrix_part's (:361-454): central differences of f_i with
+ * u_j moved by +-perturbation * mesh size, for j = i and its neighbours,
+ * keeping the (i, r; j, r) entries (jacobian = 0, as the reference) or whole
+ * blocks (jacobian = 1).  The linear solve is BiCGSTAB to lin_tol relative
+ * (the reference asks BlazeIterative for a CG solve, :486-489).  Differences:
+ * the first residual of a load step uses the force at the new boundary
+ * values, and a node with only some components prescribed keeps rows for its
+ * free ones.  dim 1, 2 or 3 (desc->dim); 1-D needs material.E. */
+typedef struct nlm_esqs nlm_esqs;
+typedef struct nlm_esqs_params {
+  int jacobian;        /* 0: (i, r; j, r) entries (reference); 1: full blocks */
+  int max_iters;       /* Newton iterations per load step (Solver.Max_Iteration) */
+  double tol;          /* Solver.Tolerance on ||f + b||                     */
+  int tol_relative;    /* 1: ||r|| / ||r_0|| < tol instead                   */
+  double perturbation; /* Solver.Perturbation                               */
+  int lin_max_iters;   /* BiCGSTAB iteration cap                            */
+  double lin_tol;      /* BiCGSTAB relative residual                        */
+  double dt;           /* load-step time increment (Final_Time / Time_Steps) */
+} nlm_esqs_params;
+int nlm_esqs_create(const nlm_fd_desc *desc, const nlm_esqs_params *params, nlm_esqs **out);
+int nlm_esqs_destroy(nlm_esqs *q);
+/* nsteps load steps; newton_iters[k], lin_iters[k] per step (may be NULL);
+ * final_res = ||f + b|| after the last one. */
+int nlm_esqs_solve(nlm_esqs *q, int nsteps, int *newton_iters, int *lin_iters,
+                   double *final_res);
+/* u (3 per node) and the output's "Force" f_i V_i (3 per node), caller's
+ * order; either may be NULL. */
+int nlm_esqs_get_state(nlm_esqs *q, double *u, double *force);
+
 /* ---- learned warm start of the quasi-static solver --------------------
  * No counterpart in the reference (its QuasiStaticModel starts every load
  * step from the previous displacement).  A per-node MLP

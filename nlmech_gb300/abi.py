@@ -146,6 +146,20 @@ class QSParams(C.Structure):
     ]
 
 
+class ESQSParams(C.Structure):
+    """nlm_esqs_params: the quasi-static ElasticState solver (Solver deck)."""
+    _fields_ = [
+        ("jacobian", C.c_int),
+        ("max_iters", C.c_int),
+        ("tol", C.c_double),
+        ("tol_relative", C.c_int),
+        ("perturbation", C.c_double),
+        ("lin_max_iters", C.c_int),
+        ("lin_tol", C.c_double),
+        ("dt", C.c_double),
+    ]
+
+
 class QSStats(C.Structure):
     _fields_ = [
         ("newton_iters", C.c_int),

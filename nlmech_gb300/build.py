@@ -31,6 +31,7 @@ UNITS = {
     "qs.cu": [],
     "noalloc.cu": ["--fmad=false"],
     "mlp.cu": [],
+    "esqs.cu": ["--fmad=false"],
 }
 
 

@@ -373,6 +373,52 @@ class QSModel:
         return phi, Z
 
 
+def esqs_params(max_iters=200, tol=1e-6, perturbation=1e-7, jacobian=0, tol_relative=False,
+                lin_max_iters=5000, lin_tol=1e-12, dt=1.0):
+    """Solver deck of QuasiStaticModel (Max_Iteration, Tolerance,
+    Perturbation) plus the BiCGSTAB cap and tolerance."""
+    return abi.ESQSParams(jacobian=int(jacobian), max_iters=int(max_iters), tol=float(tol),
+                          tol_relative=int(bool(tol_relative)), perturbation=float(perturbation),
+                          lin_max_iters=int(lin_max_iters), lin_tol=float(lin_tol), dt=float(dt))
+
+
+class ESQSModel:
+    """QuasiStaticModel<ElasticState> on the GPU (nlm_esqs_*)."""
+
+    def __init__(self, problem, params=None):
+        self.problem = problem
+        self.params = params if params is not None else esqs_params()
+        d, self._keep = problem.desc(precision=abi.FP64)
+        h = C.c_void_p()
+        _check(load().nlm_esqs_create(C.byref(d), C.byref(self.params), C.byref(h)))
+        self.h = h
+        self.n = problem.n
+
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.nlm_esqs_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def solve(self, nsteps=1):
+        """nsteps load steps: (Newton iterations per step, BiCGSTAB
+        iterations per step, final residual norm)."""
+        it = (C.c_int * max(1, nsteps))()
+        li = (C.c_int * max(1, nsteps))()
+        res = C.c_double()
+        _check(load().nlm_esqs_solve(self.h, C.c_int(int(nsteps)), it, li, C.byref(res)))
+        return list(it)[:nsteps], list(li)[:nsteps], res.value
+
+    def get(self):
+        """u (n, 3) and the output's "Force" f_i V_i (n, 3)."""
+        u = np.zeros((self.n, 3))
+        f = np.zeros((self.n, 3))
+        _check(load().nlm_esqs_get_state(self.h, abi.dptr(u), abi.dptr(f)))
+        return u, f
+
+
 def mlp_layout(n_in, n_hidden, n_layers, n_out):
     """[(d_in, d_out, w_offset, b_offset)] of the nlm_mlp parameter vector."""
     r16 = lambda v: (v + 15) // 16 * 16

@@ -54,6 +54,8 @@ int main(void) {
          sizeof(nlm_material), sizeof(nlm_fd_desc));
   printf("%zu %zu %zu %zu %zu\n", offsetof(nlm_fd_desc, material), offsetof(nlm_fd_desc, ubc),
          offsetof(nlm_fd_desc, dt), offsetof(nlm_fd_desc, u0), offsetof(nlm_material, es_sc));
+  printf("%zu %zu %zu\n", sizeof(nlm_esqs_params), offsetof(nlm_esqs_params, lin_tol),
+         offsetof(nlm_esqs_params, dt));
   return 0;
 }
 """
@@ -66,7 +68,8 @@ int main(void) {
     sizes = [C.sizeof(abi.BCSet), C.sizeof(abi.Crack), C.sizeof(abi.Material), C.sizeof(abi.FDDesc)]
     offs = [abi.FDDesc.material.offset, abi.FDDesc.ubc.offset, abi.FDDesc.dt.offset,
             abi.FDDesc.u0.offset, abi.Material.es_sc.offset]
-    assert [int(v) for v in out] == sizes + offs
+    esqs = [C.sizeof(abi.ESQSParams), abi.ESQSParams.lin_tol.offset, abi.ESQSParams.dt.offset]
+    assert [int(v) for v in out] == sizes + offs + esqs
 
 
 def test_invalid_arguments_are_status_codes(lib):

@@ -146,6 +146,17 @@ typedef struct nlm_crack {
   double activation_time; /* EdgeCrack "Activation_Time" (timed = 1)     */
 } nlm_crack;
 
+/* One No_Fail_Region "Region_k" (interiorFlagsDeck.h:38, interiorFlags.cpp:
+ * 76-90): a node inside it is not interior, so its bonds never break.
+ * Circle: params = centre x, y, z and radius r, inside when
+ * |x - c| < r (definitelyLessThan).  Rectangle: params = x1, y1, x2, y2,
+ * inside by util::geometry::isPointInsideRectangle.  Used when no_fail is on. */
+enum nlm_nofail_region_kind { NLM_NOFAIL_CIRCLE = 0, NLM_NOFAIL_RECTANGLE = 1 };
+typedef struct nlm_nofail_region {
+  int kind;          /* enum nlm_nofail_region_kind */
+  double params[4];
+} nlm_nofail_region;
+
 /* inp::MaterialDeck fields used on the hot path (materialDeck.h). */
 typedef struct nlm_material {
   int kind;                 /* enum nlm_material_kind                      */
@@ -188,6 +199,8 @@ typedef struct nlm_fd_desc {
   int decomposition;        /* enum nlm_decomposition                      */
   const double *u0;         /* optional 3*n initial displacement (or NULL) */
   const double *v0;         /* optional 3*n initial velocity (or NULL)     */
+  int n_nofail_regions;     /* No_Fail_Region.Num_Regions                  */
+  const nlm_nofail_region *nofail_regions;
 } nlm_fd_desc;
 
 /* ---- library ---------------------------------------------------------- */

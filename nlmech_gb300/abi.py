@@ -73,6 +73,14 @@ class Crack(C.Structure):
     ]
 
 
+class NoFailRegion(C.Structure):
+    _fields_ = [("kind", C.c_int), ("params", C.c_double * 4)]
+
+
+NOFAIL_CIRCLE = 0
+NOFAIL_RECTANGLE = 1
+
+
 class Material(C.Structure):
     _fields_ = [
         ("kind", C.c_int),
@@ -116,6 +124,8 @@ class FDDesc(C.Structure):
         ("decomposition", C.c_int),
         ("u0", C.POINTER(C.c_double)),
         ("v0", C.POINTER(C.c_double)),
+        ("n_nofail_regions", C.c_int),
+        ("nofail_regions", C.POINTER(NoFailRegion)),
     ]
 
 

@@ -417,14 +417,38 @@ void mesh_bbox(const double *x, int64_t n, double lo[3], double hi[3]) {
     }
 }
 
-void nofail_flags(const double *x, int64_t n, double tol, std::vector<uint8_t> &interior) {
+// The No_Fail_Region list (:76-90): circles |x - c| < r and rectangles
+// (isPointInsideRectangle, utilGeom.cpp:43-50) are not interior either.
+void nofail_flags(const double *x, int64_t n, double tol, int nreg, const nlm_nofail_region *reg,
+                  std::vector<uint8_t> &interior) {
   double lo[3], hi[3];
   mesh_bbox(x, n, lo, hi);
   for (int64_t i = 0; i < n; i++) {
     const double *p = x + 3 * i;
-    interior[i] = !(hLT(p[0], lo[0] + tol) || hLT(p[1], lo[1] + tol) ||
-                    hGT(p[0], hi[0] - tol) || hGT(p[1], hi[1] - tol));
+    bool in = !(hLT(p[0], lo[0] + tol) || hLT(p[1], lo[1] + tol) ||
+                hGT(p[0], hi[0] - tol) || hGT(p[1], hi[1] - tol));
+    for (int r = 0; r < nreg && in; r++) {
+      const double *q = reg[r].params;
+      if (reg[r].kind == NLM_NOFAIL_CIRCLE) {
+        const double d0 = p[0] - q[0], d1 = p[1] - q[1], d2 = p[2] - q[2];
+        if (hLT(std::sqrt(d0 * d0 + d1 * d1 + d2 * d2), q[3])) in = false;
+      } else if (!(hLT(p[0], q[0] - 1.0E-12) || hLT(p[1], q[1] - 1.0E-12) ||
+                   hGT(p[0], q[2] + 1.0E-12) || hGT(p[1], q[3] + 1.0E-12))) {
+        in = false;
+      }
+    }
+    interior[i] = in;
   }
+}
+
+int check_nofail_regions(const nlm_fd_desc &d) {
+  if (d.n_nofail_regions < 0 || (d.n_nofail_regions > 0 && !d.nofail_regions))
+    return fail(NLM_ERR_INVALID, "bad no-fail region list");
+  for (int r = 0; r < d.n_nofail_regions; r++)
+    if (d.nofail_regions[r].kind != NLM_NOFAIL_CIRCLE &&
+        d.nofail_regions[r].kind != NLM_NOFAIL_RECTANGLE)
+      return fail(NLM_ERR_INVALID, "no-fail region kind must be circle or rectangle");
+  return NLM_OK;
 }
 
 // RNPBond constants (rnpBond.cpp:23-97, computeParameters :99-189) and the
@@ -895,6 +919,7 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
     return fail(NLM_ERR_INVALID, "too many BC sets");
   if ((d->n_ubc && !d->ubc) || (d->n_fbc && !d->fbc) || (d->n_cracks && !d->cracks))
     return fail(NLM_ERR_INVALID, "null BC / crack array");
+  if (int rc0 = check_nofail_regions(*d)) return rc0;
   if (d->precision != NLM_PREC_FP64 && d->precision != NLM_PREC_FP32C)
     return fail(NLM_ERR_INVALID, "unknown precision");
   if (d->scheme != NLM_VELOCITY_VERLET && d->scheme != NLM_CENTRAL_DIFFERENCE)
@@ -1056,7 +1081,8 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
     for (int k = 0; k < 4; k++) h->T.t[sidx].p[k] = bc.time_params[k];
   }
   h->T.nsets = d->n_ubc;
-  if (d->no_fail != NLM_NOFAIL_OFF) nofail_flags(d->x, n, d->no_fail_tol, interior);
+  if (d->no_fail != NLM_NOFAIL_OFF)
+    nofail_flags(d->x, n, d->no_fail_tol, d->n_nofail_regions, d->nofail_regions, interior);
   mesh_bbox(d->x, n, h->bbox_lo, h->bbox_hi);
   // force BC items per node, in set order
   std::vector<std::vector<FBCItem>> fitems(n);
@@ -1956,6 +1982,7 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
       return fail(NLM_ERR_INVALID, "horizon, mesh size, dt and density must be positive");
     if (d.n_ubc < 0 || d.n_ubc > kMaxBCSets || (d.n_ubc && !d.ubc) || (d.n_cracks && !d.cracks))
       return fail(NLM_ERR_INVALID, "bad BC / crack arrays");
+    if (int rc0 = check_nofail_regions(d)) return rc0;
     if (!finite_all(d.x, 3 * d.n_nodes) || !finite_all(d.volume, d.n_nodes))
       return fail(NLM_ERR_NONFINITE, "non-finite coordinate or volume");
     total_sets += d.n_ubc;
@@ -2152,7 +2179,8 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
             wumax[3 * i + dd] = um;
           }
       }
-    if (d.no_fail != NLM_NOFAIL_OFF) nofail_flags(d.x, d.n_nodes, d.no_fail_tol, interior);
+    if (d.no_fail != NLM_NOFAIL_OFF)
+      nofail_flags(d.x, d.n_nodes, d.no_fail_tol, d.n_nofail_regions, d.nofail_regions, interior);
     for (int64_t i = 0; i < d.n_nodes; i++) {
       const int64_t g = b->off[s] + i;
       const int o = b->perm[s][i];

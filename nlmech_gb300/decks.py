@@ -146,6 +146,9 @@ class Problem:
     u0: Optional[np.ndarray] = None
     v0: Optional[np.ndarray] = None
     name: str = ""
+    # No_Fail_Region.Region_k: ("Circle", [cx, cy, cz, r]) or
+    # ("Rectangle", [x1, y1, x2, y2]) (interiorFlags.cpp:76-90)
+    nofail_regions: List[tuple] = field(default_factory=list)
 
     @property
     def n(self):
@@ -173,6 +176,16 @@ class Problem:
         d.n_cracks, d.cracks = len(self.cracks), ck
         d.no_fail = self.no_fail
         d.no_fail_tol = self.no_fail_tol
+        if self.nofail_regions:
+            regs = (abi.NoFailRegion * len(self.nofail_regions))()
+            for k, (kind, prm) in enumerate(self.nofail_regions):
+                if kind not in ("Circle", "Rectangle"):
+                    raise ValueError("no-fail region type must be Circle or Rectangle")
+                regs[k].kind = abi.NOFAIL_CIRCLE if kind == "Circle" else abi.NOFAIL_RECTANGLE
+                for q, v in enumerate(list(prm)[:4]):
+                    regs[k].params[q] = float(v)
+            keep.append(regs)
+            d.n_nofail_regions, d.nofail_regions = len(self.nofail_regions), regs
         d.dt = self.dt
         d.scheme = self.scheme if scheme is None else scheme
         d.precision = self.precision if precision is None else precision

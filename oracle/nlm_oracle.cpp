@@ -535,6 +535,17 @@ int setup_model(const nlm_fd_desc *d, bool grid, Model &m) {
       const double *p = &m.x[3 * i];
       bool in = !(dLT(p[0], lo[0] + tol) || dLT(p[1], lo[1] + tol) ||
                   dGT(p[0], hi[0] - tol) || dGT(p[1], hi[1] - tol));
+      // No_Fail_Region list (:76-90)
+      for (int r = 0; r < d->n_nofail_regions && d->nofail_regions; r++) {
+        const double *q = d->nofail_regions[r].params;
+        if (d->nofail_regions[r].kind == NLM_NOFAIL_CIRCLE) {
+          const double c[3] = {q[0], q[1], q[2]};
+          if (dLT(dist3(c, p), q[3])) in = false;
+        } else if (!(dLT(p[0], q[0] - 1.0E-12) || dLT(p[1], q[1] - 1.0E-12) ||
+                     dGT(p[0], q[2] + 1.0E-12) || dGT(p[1], q[3] + 1.0E-12))) {
+          in = false;
+        }
+      }
       m.interior[i] = in ? 1 : 0;
     }
   }

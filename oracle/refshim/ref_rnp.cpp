@@ -264,6 +264,12 @@ int ref_rnp_create(const nlm_fd_desc *d, ref_rnp **out) {
     h->ideck.d_noFailActive = d->no_fail != NLM_NOFAIL_OFF;
     h->ideck.d_computeAndNotStoreFlag = d->no_fail == NLM_NOFAIL_COMPUTE;
     h->ideck.d_noFailTol = d->no_fail_tol;
+    for (int r = 0; r < d->n_nofail_regions; r++) {
+      const nlm_nofail_region &g = d->nofail_regions[r];
+      h->ideck.d_noFailRegions.emplace_back(
+          g.kind == NLM_NOFAIL_CIRCLE ? "Circle" : "Rectangle",
+          std::vector<double>(g.params, g.params + 4));
+    }
     h->iflags = new geometry::InteriorFlags(&h->ideck, h->mesh->getNodesP(),
                                             h->mesh->getBoundingBox());
 

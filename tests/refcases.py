@@ -85,6 +85,18 @@ def reaction_plate():
     return configs.rnp_plate(40, 1.0, 3, 8.0, 1e-4, 2e-5, 200, seed=2)
 
 
+def nofail_regions_plate():
+    """The growing-crack plate with a stored no-fail layer and the
+    No_Fail_Region list: a circle around the right crack tip and a rectangle
+    across the left one, whose bonds never break."""
+    p = fracture_plate()
+    p.no_fail = abi.NOFAIL_DATA
+    p.no_fail_tol = 1.5e-3
+    p.nofail_regions = [("Circle", [0.03, 0.024, 0.0, 4e-3]),
+                        ("Rectangle", [0.006, 0.02, 0.014, 0.028])]
+    return p
+
+
 # name -> (problem, Verlet steps) of the committed reference outputs
 # (tests/golden/rnp_ref_<name>.npz)
 GOLDEN_CASES = {
@@ -94,4 +106,5 @@ GOLDEN_CASES = {
     "contact_plate": (contact_plate, 300),
     "timed_crack_plate": (timed_crack_plate, 200),
     "reaction_plate": (reaction_plate, 200),
+    "nofail_regions_plate": (nofail_regions_plate, 300),
 }

@@ -91,14 +91,20 @@ enum nlm_time_fn { /* uLoading.cpp:210-236 */
   NLM_TFN_LINEAR_SLOW_FAST = 5
 };
 
-enum nlm_spatial_fn { /* uLoading.cpp:186-208 */
+enum nlm_spatial_fn { /* uLoading.cpp:186-208, fLoading.cpp:124-238 */
   NLM_SFN_CONSTANT = 0,
   NLM_SFN_SIN_X = 1,
   NLM_SFN_SIN_Y = 2,
   NLM_SFN_SIN_Z = 3,
   NLM_SFN_LINEAR_X = 4,
   NLM_SFN_LINEAR_Y = 5,
-  NLM_SFN_LINEAR_Z = 6
+  NLM_SFN_LINEAR_Z = 6,
+  /* Force_BC only (a Displacement_BC ignores them, as ULoading does): */
+  NLM_SFN_HAT_X = 7,      /* p0 * hat(x; x1, x2), util::function::hatFunction */
+  NLM_SFN_HAT_Y = 8,      /* p0 * hat(y; y1, y2)                            */
+  NLM_SFN_HAT_Z = 9,      /* p0 * hat(z; z1, z2)                            */
+  NLM_SFN_LINE_LOAD = 10  /* per direction d: floor((x_d - min)/h) / floor(|max - min|/h),
+                             from max when p0 == -1 (fLoading.cpp:171-232) */
 };
 
 enum nlm_crack_kind {

@@ -35,7 +35,8 @@ REGION = {"rectangle": 0, "line": 1, "circle": 2, "torus": 3, "cuboid": 4}
 TIME_FN = {"constant": 0, "linear": 1, "quadratic": 2, "sin": 3,
            "linear_step": 4, "linear_slow_fast": 5}
 SPATIAL_FN = {"constant": 0, "sin_x": 1, "sin_y": 2, "sin_z": 3,
-              "linear_x": 4, "linear_y": 5, "linear_z": 6}
+              "linear_x": 4, "linear_y": 5, "linear_z": 6,
+              "hat_x": 7, "hat_y": 8, "hat_z": 9, "line_load": 10}
 CRACK_EDGE = 0
 CRACK_PLANE = 1
 NOFAIL_OFF = 0

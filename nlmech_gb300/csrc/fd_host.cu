@@ -95,15 +95,56 @@ static double uload_umax(const nlm_bc_set &bc, const double *x) {
     case NLM_SFN_LINEAR_X: { const double a = sp[0]; umax = umax * a * x[0]; } break;
     case NLM_SFN_LINEAR_Y: { const double a = sp[0]; umax = umax * a * x[1]; } break;
     case NLM_SFN_LINEAR_Z: { const double a = sp[0]; umax = umax * a * x[2]; } break;
-    default: { const double a = sp[0]; umax = umax * a; } break;
+    case NLM_SFN_CONSTANT: { const double a = sp[0]; umax = umax * a; } break;
+    default: break;  // a Force_BC-only function: no spatial factor
   }
   return umax;
 }
 
+// util::function::hatFunction (utilFunction.cpp:14-30).
+static double hat_function(double x, double x_min, double x_max) {
+  if (hGT(x, x_min - 1.0E-12) && hLT(x, x_max + 1.0E-12)) {
+    const double x_mid = 0.5 * (x_min + x_max);
+    const double l = x_mid - x_min;
+    if (l < 1.0E-12) return 1.0;
+    return hLT(x, x_mid) ? (x - x_min) / l : (x_max - x) / l;
+  }
+  return 0.0;
+}
+
+// size_t(v) of a non-negative double (truncation); values below zero give 0,
+// which is what a truncation of the (-1, 0) values a node inside its region
+// can produce gives.
+static double trunc_count(double v) {
+  return v > 0. ? (v < 1.8e19 ? (double)(uint64_t)v : v) : 0.;
+}
+
+// "line_load" (fLoading.cpp:171-232): for each direction d of the set,
+// fmax *= pos / nodes with nodes = size_t(|max - min| / h) and
+// pos = size_t((x_d - min) / h), or size_t((max - x_d) / h) when p0 == -1.
+static double line_load(const nlm_bc_set &bc, const double *x, double h) {
+  double fmax = 1.0;
+  const double lo[3] = {bc.x1, bc.y1, bc.z1}, hi[3] = {bc.x2, bc.y2, bc.z2};
+  for (int d = 0; d < 3; d++) {
+    if (!(bc.dir_mask >> d & 1)) continue;
+    const double length = std::abs(hi[d] - lo[d]);
+    const double nodes = trunc_count(length / h);
+    const double scale = 1. / nodes;
+    double pos = trunc_count((x[d] - lo[d]) / h);
+    if (bc.spatial_params[0] == -1) pos = trunc_count((hi[d] - x[d]) / h);
+    fmax *= pos * scale;
+  }
+  return fmax;
+}
+
 // Spatial part of FLoading::apply (fLoading.cpp:124-152).
-static double fload_spatial(const nlm_bc_set &bc, const double *x) {
+static double fload_spatial(const nlm_bc_set &bc, const double *x, double h) {
   const double *sp = bc.spatial_params;
   switch (bc.spatial_fn) {
+    case NLM_SFN_HAT_X: return sp[0] * hat_function(x[0], bc.x1, bc.x2);
+    case NLM_SFN_HAT_Y: return sp[0] * hat_function(x[1], bc.y1, bc.y2);
+    case NLM_SFN_HAT_Z: return sp[0] * hat_function(x[2], bc.z1, bc.z2);
+    case NLM_SFN_LINE_LOAD: return line_load(bc, x, h);
     case NLM_SFN_SIN_X: { const double a = M_PI * sp[0]; return sp[0] * std::sin(a * x[0]); }
     case NLM_SFN_SIN_Y: { const double a = M_PI * sp[0]; return sp[0] * std::sin(a * x[1]); }
     case NLM_SFN_SIN_Z: { const double a = M_PI * sp[0]; return sp[0] * std::sin(a * x[2]); }
@@ -439,6 +480,27 @@ void nofail_flags(const double *x, int64_t n, double tol, int nreg, const nlm_no
     }
     interior[i] = in;
   }
+}
+
+// The function names ULoading and FLoading accept (uLoading.cpp:35-53,
+// fLoading.cpp:33-52); the reference exits on any other.
+int check_bc_functions(const nlm_fd_desc &d) {
+  for (int k = 0; k < d.n_ubc; k++) {
+    const nlm_bc_set &b = d.ubc[k];
+    if (b.spatial_fn < NLM_SFN_CONSTANT || b.spatial_fn > NLM_SFN_LINEAR_Z)
+      return fail(NLM_ERR_INVALID, "Displacement_BC spatial function not recognised");
+    if (b.time_fn < NLM_TFN_CONSTANT || b.time_fn > NLM_TFN_LINEAR_SLOW_FAST)
+      return fail(NLM_ERR_INVALID, "Displacement_BC time function not recognised");
+  }
+  for (int k = 0; k < d.n_fbc; k++) {
+    const nlm_bc_set &b = d.fbc[k];
+    if (b.spatial_fn < NLM_SFN_CONSTANT || b.spatial_fn > NLM_SFN_LINE_LOAD)
+      return fail(NLM_ERR_INVALID, "Force_BC spatial function not recognised");
+    if (b.time_fn < NLM_TFN_CONSTANT || b.time_fn > NLM_TFN_LINEAR_SLOW_FAST ||
+        b.time_fn == NLM_TFN_QUADRATIC)
+      return fail(NLM_ERR_INVALID, "Force_BC time function not recognised");
+  }
+  return NLM_OK;
 }
 
 int check_nofail_regions(const nlm_fd_desc &d) {
@@ -920,6 +982,7 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
   if ((d->n_ubc && !d->ubc) || (d->n_fbc && !d->fbc) || (d->n_cracks && !d->cracks))
     return fail(NLM_ERR_INVALID, "null BC / crack array");
   if (int rc0 = check_nofail_regions(*d)) return rc0;
+  if (int rc0 = check_bc_functions(*d)) return rc0;
   if (d->precision != NLM_PREC_FP64 && d->precision != NLM_PREC_FP32C)
     return fail(NLM_ERR_INVALID, "unknown precision");
   if (d->scheme != NLM_VELOCITY_VERLET && d->scheme != NLM_CENTRAL_DIFFERENCE)
@@ -1090,7 +1153,7 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
     const nlm_bc_set &bc = d->fbc[sidx];
     for (int64_t i = 0; i < n; i++)
       if (in_region(bc, d->x + 3 * i, d->dim))
-        fitems[i].push_back(FBCItem{sidx, bc.dir_mask & 7, fload_spatial(bc, d->x + 3 * i)});
+        fitems[i].push_back(FBCItem{sidx, bc.dir_mask & 7, fload_spatial(bc, d->x + 3 * i, d->mesh_size)});
     h->FT.t[sidx].fn = bc.time_fn;
     for (int k = 0; k < 4; k++) h->FT.t[sidx].p[k] = bc.time_params[k];
   }

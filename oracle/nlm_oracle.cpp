@@ -358,7 +358,8 @@ void uload_value(const nlm_bc_set &bc, const double *x, double time, double &du,
     case NLM_SFN_LINEAR_X: { double a = sp[0]; umax = umax * a * x[0]; } break;
     case NLM_SFN_LINEAR_Y: { double a = sp[0]; umax = umax * a * x[1]; } break;
     case NLM_SFN_LINEAR_Z: { double a = sp[0]; umax = umax * a * x[2]; } break;
-    default: { double a = sp[0]; umax = umax * a; } break;
+    case NLM_SFN_CONSTANT: { double a = sp[0]; umax = umax * a; } break;
+    default: break;  // ULoading knows no other spatial function
   }
   du = 0.;
   dv = 0.;
@@ -392,10 +393,41 @@ void uload_value(const nlm_bc_set &bc, const double *x, double time, double &du,
 }
 
 // FLoading::apply value for one node (fLoading.cpp:117-277, no hat/line_load).
-double fload_value(const nlm_bc_set &bc, const double *x, double time) {
+// util::function::hatFunction (utilFunction.cpp:14-30).
+double hat_function(double x, double x_min, double x_max) {
+  if (dGT(x, x_min - 1.0E-12) && dLT(x, x_max + 1.0E-12)) {
+    double x_mid = 0.5 * (x_min + x_max);
+    double l = x_mid - x_min;
+    if (l < 1.0E-12) return 1.0;
+    if (dLT(x, x_mid)) return (x - x_min) / l;
+    return (x_max - x) / l;
+  }
+  return 0.0;
+}
+
+// size_t conversion (truncation) of a count; negative values give 0.
+double to_count(double v) { return v > 0. ? (v < 1.8e19 ? double(uint64_t(v)) : v) : 0.; }
+
+double fload_value(const nlm_bc_set &bc, const double *x, double time, double h) {
   double fmax = 1.0;
   const double *sp = bc.spatial_params;
   switch (bc.spatial_fn) {
+    case NLM_SFN_HAT_X: fmax = sp[0] * hat_function(x[0], bc.x1, bc.x2); break;
+    case NLM_SFN_HAT_Y: fmax = sp[0] * hat_function(x[1], bc.y1, bc.y2); break;
+    case NLM_SFN_HAT_Z: fmax = sp[0] * hat_function(x[2], bc.z1, bc.z2); break;
+    case NLM_SFN_LINE_LOAD: {
+      // fLoading.cpp:171-232 (the -1 branch's inner min/max are unused there)
+      const double lo[3] = {bc.x1, bc.y1, bc.z1}, hi[3] = {bc.x2, bc.y2, bc.z2};
+      for (int d = 0; d < 3; d++) {
+        if (!(bc.dir_mask >> d & 1)) continue;
+        double length = std::abs(hi[d] - lo[d]);
+        double nodes = to_count(length / h);
+        double scale = 1. / nodes;
+        double pos = to_count((x[d] - lo[d]) / h);
+        if (sp[0] == -1) pos = to_count((hi[d] - x[d]) / h);
+        fmax *= pos * scale;
+      }
+    } break;
     case NLM_SFN_SIN_X: { double a = M_PI * sp[0]; fmax = sp[0] * std::sin(a * x[0]); } break;
     case NLM_SFN_SIN_Y: { double a = M_PI * sp[0]; fmax = sp[0] * std::sin(a * x[1]); } break;
     case NLM_SFN_SIN_Z: { double a = M_PI * sp[0]; fmax = sp[0] * std::sin(a * x[2]); } break;
@@ -615,7 +647,7 @@ void apply_fload(Model &m, double time, double *f) {
   for (size_t s = 0; s < m.fbc.size(); s++) {
     const nlm_bc_set &bc = m.fbc[s];
     for (int64_t i : m.fbc_nodes[s]) {
-      double fm = fload_value(bc, &m.x[3 * i], time);
+      double fm = fload_value(bc, &m.x[3 * i], time, m.h);
       for (int d = 0; d < 3; d++)
         if (bc.dir_mask & (1 << d)) f[3 * i + d] += fm;
     }

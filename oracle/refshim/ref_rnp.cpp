@@ -84,6 +84,10 @@ const char *spatial_name(int s) {
     case NLM_SFN_LINEAR_X: return "linear_x";
     case NLM_SFN_LINEAR_Y: return "linear_y";
     case NLM_SFN_LINEAR_Z: return "linear_z";
+    case NLM_SFN_HAT_X: return "hat_x";
+    case NLM_SFN_HAT_Y: return "hat_y";
+    case NLM_SFN_HAT_Z: return "hat_z";
+    case NLM_SFN_LINE_LOAD: return "line_load";
   }
   return "";
 }

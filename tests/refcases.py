@@ -97,6 +97,24 @@ def nofail_regions_plate():
     return p
 
 
+def force_functions_plate():
+    """Force_BC spatial functions hat_x, hat_y and line_load (from either
+    end) on a 40 x 40 plate."""
+    p = configs.rnp_plate(40, 1e-3, 3, 0.01, 0.2, 2e-8, 200, seed=13)
+    lin = dict(time_fn="linear", time_params=[1.0])
+    p.fbc = [BC(region="rectangle", x1=0.005, x2=0.035, y1=0.030, y2=0.036, direction=[2],
+                spatial_fn="hat_x", spatial_params=[4e13], **lin),
+             BC(region="rectangle", x1=0.0, x2=0.004, y1=0.004, y2=0.036, direction=[1],
+                spatial_fn="hat_y", spatial_params=[-3e13], **lin),
+             BC(region="rectangle", x1=0.036, x2=0.04, y1=0.004, y2=0.036, direction=[1],
+                spatial_fn="line_load", spatial_params=[1.0], time_fn="linear",
+                time_params=[2e13]),
+             BC(region="rectangle", x1=0.005, x2=0.035, y1=0.004, y2=0.01, direction=[2],
+                spatial_fn="line_load", spatial_params=[-1.0], time_fn="linear",
+                time_params=[-2e13])]
+    return p
+
+
 # name -> (problem, Verlet steps) of the committed reference outputs
 # (tests/golden/rnp_ref_<name>.npz)
 GOLDEN_CASES = {
@@ -107,4 +125,5 @@ GOLDEN_CASES = {
     "timed_crack_plate": (timed_crack_plate, 200),
     "reaction_plate": (reaction_plate, 200),
     "nofail_regions_plate": (nofail_regions_plate, 300),
+    "force_functions_plate": (force_functions_plate, 200),
 }

@@ -365,3 +365,18 @@ def test_timed_cracks_rejected_by_batch_and_qs(gpu):
     q.cracks[0].activation_time = 1.0
     with pytest.raises(gpu.NLMError):
         gpu.QSModel(q, gpu.qs_params())
+
+
+def test_bc_function_names_checked_like_the_reference(gpu):
+    """ULoading accepts only constant / sin_* / linear_* spatial functions and
+    FLoading no quadratic time function (uLoading.cpp:35-53,
+    fLoading.cpp:33-52): such decks are refused, not run."""
+    p = configs.rnp_plate(20, 1e-3, 3, 0.0, 0.1, 2e-8, 10)
+    p.ubc[0].spatial_fn = "hat_x"
+    with pytest.raises(gpu.NLMError):
+        gpu.FDModel(p)
+    p = configs.rnp_plate(20, 1e-3, 3, 0.0, 0.1, 2e-8, 10)
+    p.fbc = [BC(region="rectangle", x1=0.0, x2=0.02, y1=0.0, y2=0.02, direction=[1],
+                time_fn="quadratic", time_params=[1.0, 1.0])]
+    with pytest.raises(gpu.NLMError):
+        gpu.FDModel(p)

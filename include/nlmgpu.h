@@ -79,7 +79,10 @@ enum nlm_region {
   NLM_REGION_LINE = 1,      /* x1 < x < x2 (1-D)                          */
   NLM_REGION_CIRCLE = 2,    /* |x - (x1,y1)| < r1                          */
   NLM_REGION_TORUS = 3,     /* r2 <= |x - (x1,y1)| < r1                    */
-  NLM_REGION_CUBOID = 4     /* 3-D box [x1,x2]x[y1,y2]x[z1,z2] (extension) */
+  NLM_REGION_CUBOID = 4,    /* box [x1,x2]x[y1,y2]x[z1,z2] (Force_BC; a
+                               Displacement_BC cuboid is an extension)     */
+  NLM_REGION_ANGLED_RECTANGLE = 5 /* rectangle from (x1,y1) to (x2,y2) in axes
+                               turned by theta (utilGeom.cpp:60-95)        */
 };
 
 enum nlm_time_fn { /* uLoading.cpp:210-236 */
@@ -131,6 +134,7 @@ typedef struct nlm_bc_set {
   double time_params[4];
   int spatial_fn;        /* enum nlm_spatial_fn                          */
   double spatial_params[2];
+  double theta;          /* NLM_REGION_ANGLED_RECTANGLE: Location.Angle   */
 } nlm_bc_set;
 
 /* One crack (inp::EdgeCrack, or a 3-D plane).  timed = 0: a pre-crack, cut

@@ -31,7 +31,8 @@ DECOMP_WARP = 2
 DECOMP_THREAD1 = 3
 DECOMP_TILE = 4
 # regions
-REGION = {"rectangle": 0, "line": 1, "circle": 2, "torus": 3, "cuboid": 4}
+REGION = {"rectangle": 0, "line": 1, "circle": 2, "torus": 3, "cuboid": 4,
+          "angled_rectangle": 5}
 TIME_FN = {"constant": 0, "linear": 1, "quadratic": 2, "sin": 3,
            "linear_step": 4, "linear_slow_fast": 5}
 SPATIAL_FN = {"constant": 0, "sin_x": 1, "sin_y": 2, "sin_z": 3,
@@ -56,6 +57,7 @@ class BCSet(C.Structure):
         ("time_params", C.c_double * 4),
         ("spatial_fn", C.c_int),
         ("spatial_params", C.c_double * 2),
+        ("theta", C.c_double),
     ]
 
 

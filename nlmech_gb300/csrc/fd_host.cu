@@ -74,12 +74,20 @@ static bool in_region(const nlm_bc_set &bc, const double *p, int dim) {
       return l <= bc.r1 && !(l <= bc.r2);
     }
     case NLM_REGION_CUBOID:
-      if (dim < 3)
-        return !(hLT(p[0], bc.x1 - 1.0E-12) || hLT(p[1], bc.y1 - 1.0E-12) ||
-                 hGT(p[0], bc.x2 + 1.0E-12) || hGT(p[1], bc.y2 + 1.0E-12));
+      // isPointInsideCuboid(3, ...) as FLoading calls it (fLoading.cpp:104-107)
       return !(hLT(p[0], bc.x1 - 1.0E-12) || hLT(p[1], bc.y1 - 1.0E-12) ||
                hLT(p[2], bc.z1 - 1.0E-12) || hGT(p[0], bc.x2 + 1.0E-12) ||
                hGT(p[1], bc.y2 + 1.0E-12) || hGT(p[2], bc.z2 + 1.0E-12));
+    case NLM_REGION_ANGLED_RECTANGLE: {
+      // isPointInsideAngledRectangle with rotateCW2D (transformation.cpp:20-24)
+      const double c = std::cos(bc.theta), s = std::sin(bc.theta);
+      const double a0 = bc.x2 - bc.x1, a1 = bc.y2 - bc.y1;
+      const double lam0 = a0 * c + a1 * s, lam1 = -a0 * s + a1 * c;
+      const double b0 = p[0] - bc.x1, b1 = p[1] - bc.y1;
+      const double m0 = b0 * c + b1 * s, m1 = -b0 * s + b1 * c;
+      return !(hLT(m0, -1.0E-12) || hLT(m1, -1.0E-12) || hGT(m0, lam0 + 1.0E-12) ||
+               hGT(m1, lam1 + 1.0E-12));
+    }
   }
   return false;
 }
@@ -487,6 +495,8 @@ void nofail_flags(const double *x, int64_t n, double tol, int nreg, const nlm_no
 int check_bc_functions(const nlm_fd_desc &d) {
   for (int k = 0; k < d.n_ubc; k++) {
     const nlm_bc_set &b = d.ubc[k];
+    if (b.region < NLM_REGION_RECTANGLE || b.region > NLM_REGION_ANGLED_RECTANGLE)
+      return fail(NLM_ERR_INVALID, "Displacement_BC region type not recognised");
     if (b.spatial_fn < NLM_SFN_CONSTANT || b.spatial_fn > NLM_SFN_LINEAR_Z)
       return fail(NLM_ERR_INVALID, "Displacement_BC spatial function not recognised");
     if (b.time_fn < NLM_TFN_CONSTANT || b.time_fn > NLM_TFN_LINEAR_SLOW_FAST)
@@ -494,6 +504,9 @@ int check_bc_functions(const nlm_fd_desc &d) {
   }
   for (int k = 0; k < d.n_fbc; k++) {
     const nlm_bc_set &b = d.fbc[k];
+    if (b.region != NLM_REGION_RECTANGLE && b.region != NLM_REGION_LINE &&
+        b.region != NLM_REGION_ANGLED_RECTANGLE && b.region != NLM_REGION_CUBOID)
+      return fail(NLM_ERR_INVALID, "Force_BC region type not recognised (fLoading.cpp:24-31)");
     if (b.spatial_fn < NLM_SFN_CONSTANT || b.spatial_fn > NLM_SFN_LINE_LOAD)
       return fail(NLM_ERR_INVALID, "Force_BC spatial function not recognised");
     if (b.time_fn < NLM_TFN_CONSTANT || b.time_fn > NLM_TFN_LINEAR_SLOW_FAST ||

@@ -32,11 +32,12 @@ class BC:
     time_params: List[float] = field(default_factory=lambda: [0.0])
     spatial_fn: str = "constant"
     spatial_params: List[float] = field(default_factory=lambda: [1.0])
+    theta: float = 0.0  # angled_rectangle: Location.Angle
 
     def to_c(self):
         s = abi.BCSet()
         s.region = abi.REGION[self.region]
-        for k in ("x1", "x2", "y1", "y2", "z1", "z2", "r1", "r2"):
+        for k in ("x1", "x2", "y1", "y2", "z1", "z2", "r1", "r2", "theta"):
             setattr(s, k, float(getattr(self, k)))
         mask = 0
         for d in self.direction:

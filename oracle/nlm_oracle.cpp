@@ -324,13 +324,18 @@ bool in_region(const nlm_bc_set &bc, const double *p, int dim) {
       double d[3] = {p[0] - bc.x1, p[1] - bc.y1, p[2]};
       return len3(d) <= bc.r1 && !(len3(d) <= bc.r2);
     }
-    case NLM_REGION_CUBOID:  // utilGeom.cpp:97-115
-      if (dim < 3)
-        return !(dLT(p[0], bc.x1 - 1.0E-12) || dLT(p[1], bc.y1 - 1.0E-12) ||
-                 dGT(p[0], bc.x2 + 1.0E-12) || dGT(p[1], bc.y2 + 1.0E-12));
+    case NLM_REGION_CUBOID:  // utilGeom.cpp:97-115 with dim 3 (fLoading.cpp:104-107)
       return !(dLT(p[0], bc.x1 - 1.0E-12) || dLT(p[1], bc.y1 - 1.0E-12) ||
                dLT(p[2], bc.z1 - 1.0E-12) || dGT(p[0], bc.x2 + 1.0E-12) ||
                dGT(p[1], bc.y2 + 1.0E-12) || dGT(p[2], bc.z2 + 1.0E-12));
+    case NLM_REGION_ANGLED_RECTANGLE: {  // utilGeom.cpp:60-95, transformation.cpp:20-24
+      double lam[2] = {(bc.x2 - bc.x1) * std::cos(bc.theta) + (bc.y2 - bc.y1) * std::sin(bc.theta),
+                       -(bc.x2 - bc.x1) * std::sin(bc.theta) + (bc.y2 - bc.y1) * std::cos(bc.theta)};
+      double xm[2] = {(p[0] - bc.x1) * std::cos(bc.theta) + (p[1] - bc.y1) * std::sin(bc.theta),
+                      -(p[0] - bc.x1) * std::sin(bc.theta) + (p[1] - bc.y1) * std::cos(bc.theta)};
+      return !(dLT(xm[0], -1.0E-12) || dLT(xm[1], -1.0E-12) || dGT(xm[0], lam[0] + 1.0E-12) ||
+               dGT(xm[1], lam[1] + 1.0E-12));
+    }
   }
   return false;
 }

@@ -61,6 +61,7 @@ const char *region_name(int r) {
     case NLM_REGION_CIRCLE: return "circle";
     case NLM_REGION_TORUS: return "torus";
     case NLM_REGION_CUBOID: return "cuboid";
+    case NLM_REGION_ANGLED_RECTANGLE: return "angled_rectangle";
   }
   return "";
 }
@@ -105,6 +106,7 @@ inp::BCData to_bc(const nlm_bc_set &b) {
   d.d_z2 = b.z2;
   d.d_r1 = b.r1;
   d.d_r2 = b.r2;
+  d.d_theta = b.theta;
   for (int k = 0; k < 3; k++)
     if (b.dir_mask >> k & 1) d.d_direction.push_back((size_t)k + 1);
   // the deck parser keeps as many parameters as the function takes; the

@@ -115,6 +115,21 @@ def force_functions_plate():
     return p
 
 
+def angled_regions_plate():
+    """Angled_Rectangle regions: a Displacement_BC strip turned by 0.3 rad
+    and a Force_BC patch turned by -0.2 rad, plus a Force_BC cuboid (a 3-D
+    box test on a 2-D mesh, z = 0 inside)."""
+    p = configs.rnp_plate(40, 1e-3, 3, 0.01, 0.2, 2e-8, 200, seed=17)
+    p.ubc.append(BC(region="angled_rectangle", x1=0.002, y1=0.012, x2=0.012, y2=0.020,
+                    theta=0.3, direction=[1], time_fn="linear", time_params=[-0.05]))
+    p.fbc = [BC(region="angled_rectangle", x1=0.025, y1=0.012, x2=0.036, y2=0.016, theta=-0.2,
+                direction=[1, 2], time_fn="linear", time_params=[1.0],
+                spatial_params=[3e13]),
+             BC(region="cuboid", x1=0.015, y1=0.004, z1=-1.0, x2=0.025, y2=0.008, z2=1.0,
+                direction=[2], time_fn="sin", time_params=[2e13, 3e4])]
+    return p
+
+
 # name -> (problem, Verlet steps) of the committed reference outputs
 # (tests/golden/rnp_ref_<name>.npz)
 GOLDEN_CASES = {
@@ -126,4 +141,5 @@ GOLDEN_CASES = {
     "reaction_plate": (reaction_plate, 200),
     "nofail_regions_plate": (nofail_regions_plate, 300),
     "force_functions_plate": (force_functions_plate, 200),
+    "angled_regions_plate": (angled_regions_plate, 200),
 }

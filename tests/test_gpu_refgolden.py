@@ -18,7 +18,8 @@ pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 RTOL = {"fracture_plate": 1e-12, "loads_nofail_plate": 1e-11, "cube3d": 1e-12,
         "contact_plate": 1e-12, "timed_crack_plate": 1e-12, "reaction_plate": 1e-12,
-        "nofail_regions_plate": 1e-12, "force_functions_plate": 1e-12}
+        "nofail_regions_plate": 1e-12, "force_functions_plate": 1e-12,
+        "angled_regions_plate": 1e-11}
 
 
 def _pairs(rowptr, cols, b):

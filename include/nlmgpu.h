@@ -301,6 +301,11 @@ int nlm_fd_energies(nlm_fd *h, float *strain, float *work, float *kinetic, float
  * doLinesIntersect as written (its orientation test truncates the cross
  * product to an int).  The bounding box is fe::Mesh::computeBBox's. */
 int nlm_fd_reaction_force(nlm_fd *h, double *reaction, double *total, double *sum);
+/* Start the run at this step and time (FDModel::restart sets
+ * d_n = Restart.Step and d_time = d_n dt, fDModel.cpp:102-131); only before
+ * the first step (NLM_ERR_STATE afterwards).  With nlm_fd_set_state this is
+ * the reference's restart from a VTU file (which restores u and v only). */
+int nlm_fd_set_time(nlm_fd *h, double time, int64_t step);
 /* Overwrite the bond state (inverse of nlm_fd_get_bond_state). */
 int nlm_fd_set_bond_state(nlm_fd *h, const uint8_t *broken);
 

@@ -1623,6 +1623,14 @@ int nlm_fd_load(nlm_fd *h, const char *path) {
   return nlm_fd_step_host(h, st.data(), st.data() + 3 * n, st.data() + 6 * n, 0);
 }
 
+int nlm_fd_set_time(nlm_fd *h, double time, int64_t step) {
+  if (!h || step < 0 || !std::isfinite(time)) return fail(NLM_ERR_INVALID, "bad arguments");
+  if (h->started) return fail(NLM_ERR_STATE, "the run has started");
+  h->time = time;
+  h->step = step;
+  return NLM_OK;
+}
+
 int nlm_fd_get_fixity(nlm_fd *h, uint8_t *fixity) {
   if (!h || !fixity) return fail(NLM_ERR_INVALID, "null argument");
   std::vector<uint8_t> fl(h->n);

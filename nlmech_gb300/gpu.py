@@ -194,6 +194,10 @@ class FDModel:
         _check(load().nlm_fd_damage(self.h, abi.ptr(phi, C.c_float), abi.ptr(Z, C.c_float)))
         return phi, Z
 
+    def set_time(self, time, step):
+        """Start at this step and time (a restart); before the first step."""
+        _check(load().nlm_fd_set_time(self.h, C.c_double(float(time)), C.c_int64(int(step))))
+
     def fixity(self):
         fx = np.zeros(self.n, dtype=np.uint8)
         _check(load().nlm_fd_get_fixity(self.h, abi.ptr(fx, C.c_uint8)))

@@ -221,12 +221,22 @@ def integrate(model, deck, nsteps, on_output=None):
         return nsteps, []
     os.makedirs(deck.path, exist_ok=True)
     t0, n0 = model.time()
+    files = []
+    Z = np.zeros(model.n, dtype=np.float32)
+    if n0 == 0:
+        # the output at the beginning (fDModel.cpp:335-339): loads and forces
+        # at t = 0, then output_0
+        model.run(0)
+        post = post_process(model, deck) if deck.post_processing else None
+        if post is not None:
+            Z = post["damage"][1]
+        files.append(write_output(model, deck, 0, crit.dt_out_criteria, post))
+        if on_output is not None:
+            on_output(0, files[-1])
     pending = [c for c in model.problem.cracks if c.activation_time >= 0]
     t = t0
     n = n0
     n_end = n0 + nsteps
-    files = []
-    Z = np.zeros(model.n, dtype=np.float32)
     x = model.problem.x
     while n < n_end:
         # next step at which output or a check may act (a crack's check is

@@ -23,6 +23,11 @@ def _naive_integrate(model, deck, nsteps):
     pending = [c for c in model.problem.cracks if c.activation_time >= 0]
     files, Z = [], np.zeros(model.n, dtype=np.float32)
     n0 = model.time()[1]
+    if n0 == 0:  # output at the beginning (fDModel.cpp:335-339)
+        model.run(0)
+        post = output.post_process(model, deck)
+        Z = post["damage"][1]
+        files.append(output.write_output(model, deck, 0, crit.dt_out_criteria, post))
     for _ in range(nsteps):
         model.run(1)
         t, n = model.time()
@@ -49,8 +54,8 @@ def test_output_schedule_and_files(tmp_path):
             "Fracture_Perienergy_Total", "Neighbors"]
     deck = output.OutputDeck(path=str(tmp_path) + "/", tags=tags, dt_out=50)
     steps, files = output.integrate(m, deck, 120)
-    assert steps == 120 and [os.path.basename(f) for f in files] == ["output_1.vtu",
-                                                                     "output_2.vtu"]
+    assert steps == 120 and [os.path.basename(f) for f in files] == [
+        "output_0.vtu", "output_1.vtu", "output_2.vtu"]
     d = vtu.read_vtu(files[-1])
     o = orc.OracleFD(p)
     o.run(100)

@@ -102,7 +102,7 @@ enum nlm_spatial_fn { /* uLoading.cpp:186-208, fLoading.cpp:124-238 */
   NLM_SFN_LINEAR_X = 4,
   NLM_SFN_LINEAR_Y = 5,
   NLM_SFN_LINEAR_Z = 6,
-  /* Force_BC only (a Displacement_BC ignores them, as ULoading does): */
+  /* Force_BC only (refused in a Displacement_BC, as ULoading refuses them): */
   NLM_SFN_HAT_X = 7,      /* p0 * hat(x; x1, x2), util::function::hatFunction */
   NLM_SFN_HAT_Y = 8,      /* p0 * hat(y; y1, y2)                            */
   NLM_SFN_HAT_Z = 9,      /* p0 * hat(z; z1, z2)                            */
@@ -347,7 +347,9 @@ int nlm_fd_run_timed(nlm_fd *h, int64_t nsteps, double *ms);
 
 /* Replay the step loop from CUDA graphs of steps_per_graph steps (even,
  * >= 2; 0 = plain launches).  The step-0 evaluation and any remainder run as
- * plain launches.  Not available with Force_BC sets (returns UNSUPPORTED). */
+ * plain launches, and so does a chunk in which a timed crack falls due.  A
+ * graph step evaluates the Force_BC loads at its own time, which its launches
+ * read from a device array. */
 int nlm_fd_set_graph(nlm_fd *h, int steps_per_graph);
 
 /* ---- batched specimens -------------------------------------------------

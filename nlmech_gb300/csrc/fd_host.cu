@@ -190,10 +190,13 @@ struct FBCItem {
   double spatial;
 };
 
+// time: the load time, or tdev[0] when tdev is set (graph replay).
 __global__ void k_fbc_apply(int64_t nf, int S, const int *nodes, const int *iptr,
-                            const FBCItem *items, BCTable T, double time, double *fext) {
+                            const FBCItem *items, BCTable T, double time, double *fext,
+                            const double *tdev = nullptr) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= nf) return;
+  if (tdev) time = tdev[0];
   double fe[3] = {0., 0., 0.};
   for (int k = iptr[t]; k < iptr[t + 1]; k++) {
     const FBCItem it = items[k];
@@ -810,8 +813,16 @@ int capture_graph(nlm_fd *h, int c0) {
   int c = c0, rc = NLM_OK;
   for (int k = 0; k < h->graph_steps && rc == NLM_OK; k++) {
     c = 1 - c;
+    if (h->n_fbc_nodes > 0) {
+      // FLoading::apply at the step's time, read from the time array
+      k_fbc_apply<<<nblk(h->n_fbc_nodes, 128), 128, 0, h->stream>>>(
+          h->n_fbc_nodes, h->S, h->fbc_nodes, h->fbc_iptr, h->fbc_items, h->FT, 0.,
+          const_cast<double *>(h->D.fext), h->d_times + k);
+      const cudaError_t ef = cudaGetLastError();
+      if (ef != cudaSuccess) rc = cuda_fail(ef, "force-load kernel");
+    }
     StepArgs a{c, false, 0., 0., h->d_times + k, 0, h->n};
-    rc = launch_step(h, a);
+    if (rc == NLM_OK) rc = launch_step(h, a);
   }
   e = cudaStreamEndCapture(h->stream, &g);
   h->capturing = false;
@@ -1825,8 +1836,6 @@ int nlm_fd_step_host(nlm_fd *h, double *u, double *v, double *f, int64_t nsteps)
 int nlm_fd_set_graph(nlm_fd *h, int steps_per_graph) {
   if (!h || steps_per_graph < 0 || (steps_per_graph % 2) || steps_per_graph == 1)
     return fail(NLM_ERR_INVALID, "steps_per_graph must be 0 or an even number >= 2");
-  if (steps_per_graph > 0 && h->n_fbc_nodes > 0)
-    return fail(NLM_ERR_UNSUPPORTED, "graph replay with Force_BC sets");
   NLM_CUDA(cudaStreamSynchronize(h->stream));
   for (auto &g : h->gexec)
     if (g) {

@@ -380,3 +380,18 @@ def test_bc_function_names_checked_like_the_reference(gpu):
                 time_fn="quadratic", time_params=[1.0, 1.0])]
     with pytest.raises(gpu.NLMError):
         gpu.FDModel(p)
+
+
+def test_graph_replay_with_force_loads(gpu):
+    """Force_BC loads evaluated inside the graph at each step's time: the same
+    state as plain launches, bit for bit (FP64)."""
+    import refcases
+    runs = []
+    for graph in (0, 8):
+        m = gpu.FDModel(refcases.loads_nofail_plate(), precision=abi.FP64)
+        m.set_graph(graph)
+        m.run(3)
+        m.run(61)
+        runs.append(m.state())
+    for a, b in zip(*runs):
+        assert np.array_equal(a, b)

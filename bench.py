@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--qs-steps", type=int, default=100,
                     help="quasi-static load steps of the learned vs plain warm-start comparison "
                          "(200 x 200 plate); 0 skips it")
-    ap.add_argument("--decomp", default="auto", choices=["auto", "thread", "thread1", "warp", "tile"])
+    ap.add_argument("--decomp", default="auto", choices=["auto", "thread", "thread1", "warp", "tile", "tilel"])
     ap.add_argument("--workload", default="plate", choices=["plate", "ensemble"],
                     help="plate: 1000x1000 RNPBond plate (headline); ensemble: 256 plates "
                          "of 5k-200k nodes batched, against sequential single-plate runs")
@@ -225,12 +225,15 @@ def run_ours(a):
 
     # ---- FP32-compensated (headline) ----
     dmap = {"auto": abi.DECOMP_AUTO, "thread": abi.DECOMP_THREAD,
-            "thread1": abi.DECOMP_THREAD1, "warp": abi.DECOMP_WARP, "tile": abi.DECOMP_TILE}
+            "thread1": abi.DECOMP_THREAD1, "warp": abi.DECOMP_WARP, "tile": abi.DECOMP_TILE,
+               "tilel": abi.DECOMP_TILE_LOCAL}
     m = gpu.FDModel(p, precision=abi.FP32C, decomposition=dmap[a.decomp])
     nnz = m.nnz()
     decomp = {1: "thread-per-node, 4-bond groups", 2: "warp-per-node",
               3: "thread-per-node, 1 bond/iteration",
-              4: "256-node tiles staged in shared memory"}.get(m.decomposition(), "?")
+              4: "256-node tiles staged in shared memory",
+              5: "256-node tiles staged in shared memory, tile-frame FP32 bond data"
+              }.get(m.decomposition(), "?")
     m.run(a.warmup)
     barrier_sync()
     with ClockSampler(local) as cs:

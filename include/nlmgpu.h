@@ -69,8 +69,11 @@ enum nlm_decomposition {
                              four at a time                                */
   NLM_DECOMP_WARP = 2,    /* one warp per node, CSR bond storage           */
   NLM_DECOMP_THREAD1 = 3, /* one thread per node, one bond per iteration   */
-  NLM_DECOMP_TILE = 4     /* FP32C 2-D: 256-node tiles with their halo staged
+  NLM_DECOMP_TILE = 4,    /* FP32C 2-D: 256-node tiles with their halo staged
                              in shared memory, 16-bit tile-local bond ids  */
+  NLM_DECOMP_TILE_LOCAL = 5 /* as TILE with the staged positions and
+                             displacements in the tile's frame, one FP32
+                             value per component                          */
 };
 
 /* Displacement_BC / Force_BC region types (loading/uLoading.cpp:38-46). */

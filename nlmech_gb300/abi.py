@@ -30,6 +30,7 @@ DECOMP_THREAD = 1
 DECOMP_WARP = 2
 DECOMP_THREAD1 = 3
 DECOMP_TILE = 4
+DECOMP_TILE_LOCAL = 5
 # regions
 REGION = {"rectangle": 0, "line": 1, "circle": 2, "torus": 3, "cuboid": 4,
           "angled_rectangle": 5}

@@ -35,23 +35,18 @@ enum : int {
 // as the node itself: xi = eta = 0 gives S = 0, s = 0 and no break.
 // The volume correction min(1, (delta + h/2 - r) / h) equals the reference's
 // "if r > delta - h/2" factor away from its 1e-5 relative comparison band.
-template <int DIM, int OPT>
-__device__ __forceinline__ float rnp_bond32(const Params32 &Q, const Node32<DIM> &ni,
-                                            const float uih[3], const float uil[3],
-                                            const Node32<DIM> &nj, const float ujh[3],
-                                            const float ujl[3], bool breakable, bool &fs,
-                                            float d[3]) {
-  const float2 dl = __half22float2(__hsub2(nj.lxy, ni.lxy));
-  d[0] = fmaf(dl.x, Q.inv_lo, nj.xh[0] - ni.xh[0]);
-  d[1] = fmaf(dl.y, Q.inv_lo, nj.xh[1] - ni.xh[1]);
-  const float e0 = (ujh[0] - uih[0]) + (ujl[0] - uil[0]);
-  const float e1 = (ujh[1] - uih[1]) + (ujl[1] - uil[1]);
+// The bond force from the bond vector d (= xi) and eta's components e (same
+// arithmetic for every kernel): returns s with F = s * d and updates fs.
+// On a broken bond with contact, d becomes the deformed bond y = xi + eta.
+// KVOL: volj is already K1 * V_j (the same product formed here otherwise;
+// only without the contact term, which needs V_j itself).
+template <int DIM, int OPT, bool KVOL = false>
+__device__ __forceinline__ float rnp_bond32_core(const Params32 &Q, float d[3], float e0,
+                                                 float e1, float e2, float volj, float voli,
+                                                 bool breakable, bool &fs) {
   float r2 = d[0] * d[0] + d[1] * d[1];
   float de = d[0] * e0 + d[1] * e1;
   if (DIM == 3) {
-    const float2 dz = __half22float2(__hsub2(nj.lz, ni.lz));
-    d[2] = fmaf(dz.x, Q.inv_lo, nj.xh[2] - ni.xh[2]);
-    const float e2 = (ujh[2] - uih[2]) + (ujl[2] - uil[2]);
     r2 = fmaf(d[2], d[2], r2);
     de = fmaf(d[2], e2, de);
   }
@@ -59,7 +54,7 @@ __device__ __forceinline__ float rnp_bond32(const Params32 &Q, const Node32<DIM>
   const float rinv = rsqrt_approx(r2);
   const float r = r2 * rinv;
   const float S = de * (rinv * rinv);
-  float k = Q.K1 * nj.vol * fminf(1.f, (Q.check_up - r) * Q.inv_h);
+  float k = (KVOL ? volj : Q.K1 * volj) * fminf(1.f, (Q.check_up - r) * Q.inv_h);
   if (!(OPT & OPT_CONSTJ) && Q.infl_type != 0) {  // type 0: J folded into K1
     const float rr = r * Q.inv_delta;
     k *= Q.infl_type == 1 ? Q.a0 + Q.a1 * rr
@@ -75,18 +70,38 @@ __device__ __forceinline__ float rnp_bond32(const Params32 &Q, const Node32<DIM>
     const float y0 = d[0] + e0, y1 = d[1] + e1;
     float yy = y0 * y0 + y1 * y1;
     if (DIM == 3) {
-      d[2] = d[2] + ((ujh[2] - uih[2]) + (ujl[2] - uil[2]));
+      d[2] = d[2] + e2;
       yy = fmaf(d[2], d[2], yy);
     }
     d[0] = y0;
     d[1] = y1;
     const float R = sqrtf(yy);
-    const float vj = nj.vol * fminf(1.f, (Q.check_up - r) * Q.inv_h);
-    const float sf = Q.kn * (ni.vol * vj / (ni.vol + vj)) * (Q.rc - R) / R;
+    const float vj = volj * fminf(1.f, (Q.check_up - r) * Q.inv_h);
+    const float sf = Q.kn * (voli * vj / (voli + vj)) * (Q.rc - R) / R;
     return -fmaxf(sf, 0.f);
   }
   const float s1 = fs ? 0.f : s0 * ex2_approx(Q.nbl2e * bs2);
   return brk ? s1 : s0;
+}
+
+template <int DIM, int OPT>
+__device__ __forceinline__ float rnp_bond32(const Params32 &Q, const Node32<DIM> &ni,
+                                            const float uih[3], const float uil[3],
+                                            const Node32<DIM> &nj, const float ujh[3],
+                                            const float ujl[3], bool breakable, bool &fs,
+                                            float d[3]) {
+  const float2 dl = __half22float2(__hsub2(nj.lxy, ni.lxy));
+  d[0] = fmaf(dl.x, Q.inv_lo, nj.xh[0] - ni.xh[0]);
+  d[1] = fmaf(dl.y, Q.inv_lo, nj.xh[1] - ni.xh[1]);
+  const float e0 = (ujh[0] - uih[0]) + (ujl[0] - uil[0]);
+  const float e1 = (ujh[1] - uih[1]) + (ujl[1] - uil[1]);
+  float e2 = 0.f;
+  if (DIM == 3) {
+    const float2 dz = __half22float2(__hsub2(nj.lz, ni.lz));
+    d[2] = fmaf(dz.x, Q.inv_lo, nj.xh[2] - ni.xh[2]);
+    e2 = (ujh[2] - uih[2]) + (ujl[2] - uil[2]);
+  }
+  return rnp_bond32_core<DIM, OPT>(Q, d, e0, e1, e2, nj.vol, ni.vol, breakable, fs);
 }
 
 // Thread-per-node, sliced-ELL bond store.  NW1: every row fits one bit word.
@@ -344,6 +359,99 @@ __global__ void __launch_bounds__(kTileNodes, 3)
   integrate_node32<2, SCHEME>(P, Q, D, T, A, i, fl, uih, uil, fi);
 }
 
+// Tile kernel with the bond data in the tile's own frame (2-D): staging
+// writes, per staged node, x - x_o and u - u_o rounded once to FP32 (x_o, u_o
+// of the tile's first node, both differences formed in the split
+// representation), so a bond needs one 16-byte shared-memory read and two
+// subtractions per component for xi and eta.  xi and eta then carry the
+// FP32 rounding of the tile-frame coordinates (~2^-24 of the tile span)
+// instead of ~2^-24 of themselves; the node's own update stays on the
+// (hi, lo) pairs.
+template <int SCHEME, bool NW1, int OPT>
+__global__ void __launch_bounds__(kTileNodes, 4)
+    k_rnp32_tilel(const StepParams P, const Params32 Q, const DevPtrs D, const BCTable T,
+                  const StepArgs A) {
+  __shared__ float4 s_xu[kTileMaxLocal];  // x - x_o, y - y_o, ux - ux_o, uy - uy_o
+  __shared__ float s_vol[kTileMaxLocal];  // K1 V (V with the contact term)
+  constexpr bool KV = !(OPT & OPT_CONTACT);
+  __shared__ uint8_t s_fl[(OPT & OPT_NOFAIL) ? kTileMaxLocal : 1];
+  const int64_t t0 = (int64_t)blockIdx.x * kTileNodes;
+  const int h0 = D.tile_hptr[blockIdx.x];
+  const int nh = D.tile_hptr[blockIdx.x + 1] - h0;
+  const int nt = (int)min((int64_t)kTileNodes, P.n - t0);
+  const float4 *ucur = D.u32[A.cur];
+  const float4 po = __ldg(D.pos32 + t0);
+  const float2 plo = __half22float2(*reinterpret_cast<const __half2 *>(&po.w));
+  const float4 uo = ucur[t0];
+  for (int e = threadIdx.x; e < kTileNodes + nh; e += blockDim.x) {
+    if (e < kTileNodes && e >= nt) continue;
+    const int64_t g = e < kTileNodes ? t0 + e : (int64_t)D.tile_halo[h0 + e - kTileNodes];
+    const float4 a = __ldg(D.pos32 + g);
+    const float2 lo = __half22float2(*reinterpret_cast<const __half2 *>(&a.w));
+    const float4 u = ucur[g];
+    s_xu[e] = make_float4(fmaf(lo.x - plo.x, Q.inv_lo, a.x - po.x),
+                          fmaf(lo.y - plo.y, Q.inv_lo, a.y - po.y),
+                          (u.x - uo.x) + (u.z - uo.z), (u.y - uo.y) + (u.w - uo.w));
+    s_vol[e] = KV ? Q.K1 * a.z : a.z;
+    if (OPT & OPT_NOFAIL) s_fl[e] = D.flags[g];
+  }
+  __syncthreads();
+  const int il = threadIdx.x;
+  if (il >= nt) return;
+  const int64_t i = t0 + il;
+  const float4 xi = s_xu[il];
+  const float voli = s_vol[il];  // used by the contact term only (raw V there)
+  float uih[3], uil[3];
+  {
+    const float4 a = ucur[i];
+    uih[0] = a.x; uih[1] = a.y; uih[2] = 0.f;
+    uil[0] = a.z; uil[1] = a.w; uil[2] = 0.f;
+  }
+  const uint8_t fl = D.flags[i];
+  const bool brk_i = !(fl & FLAG_NOFAIL);
+  const int len = D.rowlen[i];
+  const int ng = (len + 3) >> 2;
+  const uint2 *lp = reinterpret_cast<const uint2 *>(D.tile_lidx + D.sell_ptr[i >> 5]) + (i & 31);
+  float fi[3] = {0.f, 0.f, 0.f};
+  uint32_t word = NW1 ? D.bits[i] : 0u;
+  uint32_t nw = 0;
+  uint2 nxt = ng > 0 ? __ldg(lp) : make_uint2(0u, 0u);
+  for (int g = 0; g < ng; g++) {
+    const uint2 cur = nxt;
+    if (g + 1 < ng) nxt = __ldg(lp + 32 * (g + 1));
+    if (!NW1 && (g & 7) == 0) {
+      if (nw) D.bits[(int64_t)((g >> 3) - 1) * P.npad + i] = word | nw;
+      word = D.bits[(int64_t)(g >> 3) * P.npad + i];
+      nw = 0;
+    }
+    const int jl[4] = {(int)(cur.x & 0xffffu), (int)(cur.x >> 16), (int)(cur.y & 0xffffu),
+                       (int)(cur.y >> 16)};
+    float4 xj[4];
+    float vj[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      xj[q] = s_xu[jl[q]];
+      vj[q] = s_vol[jl[q]];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int k = 4 * g + q;
+      float dv[3] = {xj[q].x - xi.x, xj[q].y - xi.y, 0.f};
+      const bool was = (word >> (k & 31)) & 1u;
+      bool fs = was;
+      bool breakable = true;
+      if (OPT & OPT_NOFAIL) breakable = brk_i && !(s_fl[jl[q]] & FLAG_NOFAIL);
+      const float sc = rnp_bond32_core<2, OPT, KV>(Q, dv, xj[q].z - xi.z, xj[q].w - xi.w, 0.f,
+                                                   vj[q], voli, breakable, fs);
+      nw |= (uint32_t)(fs && !was) << (k & 31);
+      fi[0] = fmaf(sc, dv[0], fi[0]);
+      fi[1] = fmaf(sc, dv[1], fi[1]);
+    }
+  }
+  if (nw) D.bits[NW1 ? i : (int64_t)((len - 1) >> 5) * P.npad + i] = word | nw;
+  integrate_node32<2, SCHEME>(P, Q, D, T, A, i, fl, uih, uil, fi);
+}
+
 template <int DIM, int SCHEME, int OPT, bool BATCH>
 static void launch_opt(const StepParams &P, const Params32 &Q, const DevPtrs &D,
                        const BCTable &T, const StepArgs &a, int decomp, cudaStream_t s) {
@@ -356,6 +464,14 @@ static void launch_opt(const StepParams &P, const Params32 &Q, const DevPtrs &D,
       k_rnp32_tile<SCHEME, true, OPT><<<grid, kTileNodes, 0, s>>>(P, Q, D, T, a);
     else
       k_rnp32_tile<SCHEME, false, OPT><<<grid, kTileNodes, 0, s>>>(P, Q, D, T, a);
+    return;
+  }
+  if (DIM == 2 && !BATCH && decomp == NLM_DECOMP_TILE_LOCAL) {
+    const unsigned grid = (unsigned)((P.n + kTileNodes - 1) / kTileNodes);
+    if (P.nw1)
+      k_rnp32_tilel<SCHEME, true, OPT><<<grid, kTileNodes, 0, s>>>(P, Q, D, T, a);
+    else
+      k_rnp32_tilel<SCHEME, false, OPT><<<grid, kTileNodes, 0, s>>>(P, Q, D, T, a);
     return;
   }
   if (decomp == NLM_DECOMP_WARP) {

@@ -751,7 +751,10 @@ int autotune(nlm_fd *h) {
   D.f32 = sf;
   D.bits = sb;
   std::vector<int> cands = {NLM_DECOMP_THREAD, NLM_DECOMP_THREAD1, NLM_DECOMP_WARP};
-  if (h->tile_ok) cands.push_back(NLM_DECOMP_TILE);
+  if (h->tile_ok) {
+    cands.push_back(NLM_DECOMP_TILE);
+    cands.push_back(NLM_DECOMP_TILE_LOCAL);
+  }
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
@@ -1065,11 +1068,12 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
   }
   h->decomp = d->decomposition == NLM_DECOMP_AUTO ? NLM_DECOMP_THREAD : d->decomposition;
   if (h->decomp != NLM_DECOMP_THREAD && h->decomp != NLM_DECOMP_WARP &&
-      h->decomp != NLM_DECOMP_THREAD1 && h->decomp != NLM_DECOMP_TILE)
+      h->decomp != NLM_DECOMP_THREAD1 && h->decomp != NLM_DECOMP_TILE &&
+      h->decomp != NLM_DECOMP_TILE_LOCAL)
     return bail(fail(NLM_ERR_INVALID, "unknown decomposition"));
   const bool tile_able = d->precision == NLM_PREC_FP32C && d->material.kind == NLM_MAT_RNP_BOND &&
                          d->dim == 2;
-  if (h->decomp == NLM_DECOMP_TILE && !tile_able)
+  if ((h->decomp == NLM_DECOMP_TILE || h->decomp == NLM_DECOMP_TILE_LOCAL) && !tile_able)
     return bail(fail(NLM_ERR_UNSUPPORTED, "the tile decomposition is for FP32C 2-D RNPBond"));
   const bool want_tune = d->decomposition == NLM_DECOMP_AUTO &&
                          d->precision == NLM_PREC_FP32C && d->material.kind == NLM_MAT_RNP_BOND;
@@ -1129,10 +1133,11 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
   TRY(h->alloc(&bits, (size_t)P.nwords * P.npad));
   TRY(cudaMemsetAsync(bits, 0, sizeof(uint32_t) * P.nwords * P.npad, s));
   D.bits = bits;
-  if (tile_able && (h->decomp == NLM_DECOMP_TILE || want_tune)) {
+  if (tile_able &&
+      (h->decomp == NLM_DECOMP_TILE || h->decomp == NLM_DECOMP_TILE_LOCAL || want_tune)) {
     int rc_t = build_tiles(h, st.ptr);
     if (rc_t) return bail(rc_t);
-    if (h->decomp == NLM_DECOMP_TILE && !h->tile_ok)
+    if ((h->decomp == NLM_DECOMP_TILE || h->decomp == NLM_DECOMP_TILE_LOCAL) && !h->tile_ok)
       return bail(fail(NLM_ERR_UNSUPPORTED, "a tile's halo exceeds the tile store limit"));
   }
   for (int c = 0; c < d->n_cracks; c++) {

@@ -66,7 +66,7 @@ def test_fp32c_matches_reference_golden(gpu):
     make, steps = GOLDEN_CASES["fracture_plate"]
     z = np.load(os.path.join(GOLDEN, "rnp_ref_fracture_plate.npz"))
     ref = _pairs(z["rowptr"], z["cols"], z["broken"])
-    for dec in (abi.DECOMP_THREAD, abi.DECOMP_WARP, abi.DECOMP_TILE):
+    for dec in (abi.DECOMP_THREAD, abi.DECOMP_WARP, abi.DECOMP_TILE, abi.DECOMP_TILE_LOCAL):
         m = gpu.FDModel(make(), precision=abi.FP32C, decomposition=dec)
         m.run(steps)
         u, v, f = m.state()

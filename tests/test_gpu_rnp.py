@@ -179,6 +179,7 @@ def test_fp32c_config0_error(gpu, oracle):
     rowptr, cols = o.neighbors()
     bo = bonds_as_pairs(rowptr, cols, o.bond_state())
     for dec in (abi.DECOMP_THREAD, abi.DECOMP_THREAD1, abi.DECOMP_WARP, abi.DECOMP_TILE,
+                abi.DECOMP_TILE_LOCAL,
                 abi.DECOMP_AUTO):
         m = gpu.FDModel(p, precision=abi.FP32C, decomposition=dec)
         m.run(1000)
@@ -256,8 +257,9 @@ def test_tile_decomposition_bit_identical_to_thread(gpu):
 
 def test_tile_decomposition_rejected_where_unsupported(gpu):
     p = configs.config0()
-    with pytest.raises(gpu.NLMError):
-        gpu.FDModel(p, precision=abi.FP64, decomposition=abi.DECOMP_TILE)
+    for dec in (abi.DECOMP_TILE, abi.DECOMP_TILE_LOCAL):
+        with pytest.raises(gpu.NLMError):
+            gpu.FDModel(p, precision=abi.FP64, decomposition=dec)
 
 
 def test_checkpoint_restart_continues_the_run(gpu, tmp_path):

@@ -383,6 +383,26 @@ __global__ void __launch_bounds__(kTileNodes, 4)
   const float4 po = __ldg(D.pos32 + t0);
   const float2 plo = __half22float2(*reinterpret_cast<const __half2 *>(&po.w));
   const float4 uo = ucur[t0];
+  // the node's own loads go out before the staging loop, so their latency
+  // overlaps it
+  const int il = threadIdx.x;
+  const int64_t i = t0 + il;
+  const bool own = il < nt;
+  const uint8_t fl = own ? D.flags[i] : 0;
+  const int len = own ? D.rowlen[i] : 0;
+  const int ng = (len + 3) >> 2;
+  const uint2 *lp = reinterpret_cast<const uint2 *>(D.tile_lidx + (own ? D.sell_ptr[i >> 5] : 0)) +
+                    (i & 31);
+  uint32_t word = (NW1 && own) ? D.bits[i] : 0u;
+  uint2 nxt = ng > 0 ? __ldg(lp) : make_uint2(0u, 0u);
+  float4 ui4 = own ? ucur[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  if (own) {
+    // the integrator's velocity and force reads, brought into L1 early
+    const float4 *vp = D.v32[SCHEME == NLM_VELOCITY_VERLET ? 0 : A.cur] + i;
+    const float2 *fp = reinterpret_cast<const float2 *>(D.f32) + i;
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(vp));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(fp));
+  }
   for (int e = threadIdx.x; e < kTileNodes + nh; e += blockDim.x) {
     if (e < kTileNodes && e >= nt) continue;
     const int64_t g = e < kTileNodes ? t0 + e : (int64_t)D.tile_halo[h0 + e - kTileNodes];
@@ -396,26 +416,13 @@ __global__ void __launch_bounds__(kTileNodes, 4)
     if (OPT & OPT_NOFAIL) s_fl[e] = D.flags[g];
   }
   __syncthreads();
-  const int il = threadIdx.x;
-  if (il >= nt) return;
-  const int64_t i = t0 + il;
+  if (!own) return;
   const float4 xi = s_xu[il];
   const float voli = s_vol[il];  // used by the contact term only (raw V there)
-  float uih[3], uil[3];
-  {
-    const float4 a = ucur[i];
-    uih[0] = a.x; uih[1] = a.y; uih[2] = 0.f;
-    uil[0] = a.z; uil[1] = a.w; uil[2] = 0.f;
-  }
-  const uint8_t fl = D.flags[i];
+  float uih[3] = {ui4.x, ui4.y, 0.f}, uil[3] = {ui4.z, ui4.w, 0.f};
   const bool brk_i = !(fl & FLAG_NOFAIL);
-  const int len = D.rowlen[i];
-  const int ng = (len + 3) >> 2;
-  const uint2 *lp = reinterpret_cast<const uint2 *>(D.tile_lidx + D.sell_ptr[i >> 5]) + (i & 31);
   float fi[3] = {0.f, 0.f, 0.f};
-  uint32_t word = NW1 ? D.bits[i] : 0u;
   uint32_t nw = 0;
-  uint2 nxt = ng > 0 ? __ldg(lp) : make_uint2(0u, 0u);
   for (int g = 0; g < ng; g++) {
     const uint2 cur = nxt;
     if (g + 1 < ng) nxt = __ldg(lp + 32 * (g + 1));

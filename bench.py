@@ -140,9 +140,18 @@ def measured_peaks():
         return None
 
 
-def profiled_traffic():
+KERNELS = {1: ("k_rnp32_thread", "rnp_fp32_step_plate1000.md"),
+           2: ("k_rnp32_warp", None), 3: ("k_rnp32_thread1", None),
+           4: ("k_rnp32_tile", None),
+           5: ("k_rnp32_tilel", "rnp_fp32_tilel_step_plate1000.md")}
+
+
+def profiled_traffic(decomp=1):
     """dram bytes per launch of the step kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "rnp_fp32_step_plate1000.md")
+    name = KERNELS.get(decomp, (None, None))[1]
+    if name is None:
+        return None
+    p = os.path.join(ROOT, "profiles", name)
     try:
         for ln in open(p):
             if ln.startswith("traffic_bytes_per_launch:"):
@@ -229,6 +238,7 @@ def run_ours(a):
                "tilel": abi.DECOMP_TILE_LOCAL}
     m = gpu.FDModel(p, precision=abi.FP32C, decomposition=dmap[a.decomp])
     nnz = m.nnz()
+    dcode = m.decomposition()
     decomp = {1: "thread-per-node, 4-bond groups", 2: "warp-per-node",
               3: "thread-per-node, 1 bond/iteration",
               4: "256-node tiles staged in shared memory",
@@ -309,7 +319,7 @@ def run_ours(a):
     else:
         peak, peak_src = 6800.0, "fallback"
     achieved = bytes_per_launch / (kms * 1e-3) / 1e9 if kms > 0 else None
-    traffic = profiled_traffic()
+    traffic = profiled_traffic(dcode)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
@@ -332,7 +342,8 @@ def run_ours(a):
         "gpu_launches": a.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                     "peak_source": peak_src, "kernel": "k_rnp32_thread",
+                     "peak_source": peak_src,
+                     "kernel": KERNELS.get(dcode, ("?", None))[0],
                      "kernel_ms": kms, "bytes_per_launch": bytes_per_launch},
         "clocks": clocks,
     }

@@ -344,6 +344,13 @@ int nlm_fd_sync(nlm_fd *h);
  * exactly as nlm_fd_run would. */
 int nlm_fd_step_host(nlm_fd *h, double *u, double *v, double *f,
                      int64_t nsteps);
+/* How the last nlm_fd_step_host moved the arrays: 1 = read and written in
+ * place by kernels (each of u, v, f lies inside one page-locked allocation
+ * the device maps at the same address, e.g. from cudaHostAlloc or
+ * cudaHostRegister), 0 = copied through device staging buffers.  In 2-D the
+ * z entries of u and v are left as the caller had them either way (the
+ * reference's 2-D integrator never writes them) and f's z is written as 0. */
+int nlm_fd_host_io(const nlm_fd *h, int *mode);
 /* nlm_fd_run bracketed by CUDA events on the handle's stream; *ms is the
  * device time of the whole run (the stream is synchronized). */
 int nlm_fd_run_timed(nlm_fd *h, int64_t nsteps, double *ms);

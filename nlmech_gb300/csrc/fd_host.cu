@@ -275,6 +275,108 @@ __global__ void k_scatter_vec(int64_t n, int S, int dim, const int *perm, const 
   const double *p = src + 3 * (int64_t)perm[i];
   for (int d = 0; d < S; d++) dst[S * i + d] = (d < dim && d < 3) ? p[d] : 0.;
 }
+__global__ void k_invert_perm(int64_t n, const int *perm, int *iperm) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) iperm[perm[i]] = (int)i;
+}
+
+// Pinned caller arrays read in place.  The caller's arrays are taken as flat
+// sequences of 3n doubles, two per thread with 16-byte loads, so every byte
+// crosses the host link once in full lines.  Value k is component k % 3 of
+// caller node k / 3; it goes into a staging copy of the state array in the
+// internal order (FP32C: its (hi, lo) floats), or, for a component the model
+// does not hold (z in 2-D), into zkeep in the caller's order.
+template <bool FP32>
+__device__ __forceinline__ void stage_value(int S, int dim, int64_t i, int d, double x, void *dst,
+                                            double *zkeep, int64_t k) {
+  if (d >= dim) {
+    if (zkeep) zkeep[k / 3] = x;
+    return;
+  }
+  if (FP32) {
+    float *q = static_cast<float *>(dst);
+    const float hi = __double2float_rn(x), lo = __double2float_rn(x - (double)hi);
+    if (S == 2) {
+      q[4 * i + d] = hi;
+      q[4 * i + 2 + d] = lo;
+    } else {
+      q[8 * i + d] = hi;
+      q[8 * i + 4 + d] = lo;
+    }
+  } else {
+    static_cast<double *>(dst)[S * i + d] = x;
+  }
+}
+
+template <bool FP32>
+__global__ void k_host_in(int64_t n, int S, int dim, const int *iperm, const double2 *hu,
+                          const double2 *hv, const double2 *hf, void *su, void *sv, void *sf,
+                          double *zu, double *zv, int *bad) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (2 * t >= 3 * n) return;
+  const double2 a = hu[t], b = hv[t], c = hf[t];
+  if (!(isfinite(a.x) && isfinite(a.y) && isfinite(b.x) && isfinite(b.y) && isfinite(c.x) &&
+        isfinite(c.y)))
+    atomicExch(bad, 1);
+  for (int h = 0; h < 2; h++) {
+    const int64_t k = 2 * t + h;
+    const int64_t o = k / 3;
+    const int d = (int)(k - 3 * o);
+    const int64_t i = iperm[o];
+    stage_value<FP32>(S, dim, i, d, h ? a.y : a.x, su, zu, k);
+    stage_value<FP32>(S, dim, i, d, h ? b.y : b.x, sv, zv, k);
+    if (d < dim) {
+      if (FP32)
+        static_cast<float *>(sf)[S * i + d] = (float)(h ? c.y : c.x);
+      else
+        static_cast<double *>(sf)[S * i + d] = h ? c.y : c.x;
+    }
+  }
+}
+
+// The state written into the pinned caller arrays in place, two doubles per
+// thread with 16-byte stores: the model's components of u and v, their z in
+// 2-D from zkeep (the caller's own values, which the reference's 2-D
+// integrator never changes), and f with z = 0 in 2-D (the reference resets f
+// every step).
+template <bool FP32>
+__device__ __forceinline__ double state_value(int S, int64_t i, int d, const void *src) {
+  if (FP32) {
+    const float *q = static_cast<const float *>(src);
+    if (S == 2) return (double)q[4 * i + d] + (double)q[4 * i + 2 + d];
+    return (double)q[8 * i + d] + (double)q[8 * i + 4 + d];
+  }
+  return static_cast<const double *>(src)[S * i + d];
+}
+
+template <bool FP32>
+__global__ void k_host_out(int64_t n, int S, int dim, const int *iperm, const void *u,
+                           const void *v, const void *f, const double *zu, const double *zv,
+                           double2 *hu, double2 *hv, double2 *hf) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (2 * t >= 3 * n) return;
+  double a[2], b[2], c[2];
+  for (int h = 0; h < 2; h++) {
+    const int64_t k = 2 * t + h;
+    const int64_t o = k / 3;
+    const int d = (int)(k - 3 * o);
+    const int64_t i = iperm[o];
+    if (d < dim) {
+      a[h] = state_value<FP32>(S, i, d, u);
+      b[h] = state_value<FP32>(S, i, d, v);
+      c[h] = FP32 ? (double)static_cast<const float *>(f)[S * i + d]
+                  : static_cast<const double *>(f)[S * i + d];
+    } else {
+      a[h] = zu[o];
+      b[h] = zv[o];
+      c[h] = 0.;
+    }
+  }
+  hu[t] = make_double2(a[0], a[1]);
+  hv[t] = make_double2(b[0], b[1]);
+  hf[t] = make_double2(c[0], c[1]);
+}
+
 __global__ void k_nonfinite(int64_t m, const double *a, int *flag) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k < m && !isfinite(a[k])) atomicExch(flag, 1);
@@ -304,13 +406,19 @@ __global__ void k_scatter_f32(int64_t n, int S, int dim, const int *perm, const 
   const double *p = src + 3 * (int64_t)perm[i];
   for (int d = 0; d < S; d++) dst[S * i + d] = (d < dim && d < 3) ? (float)p[d] : 0.f;
 }
-__global__ void k_gather_vec(int64_t n, int S, const int *perm, const double *src, double *dst) {
+// keep_z (2-D): the z entry of dst is left as it is (the caller's own value,
+// uploaded into the same slot), as the reference's 2-D integrator never
+// writes the z component of u and v.
+__global__ void k_gather_vec(int64_t n, int S, const int *perm, const double *src, double *dst,
+                             bool keep_z = false) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   double *p = dst + 3 * (int64_t)perm[i];
-  for (int d = 0; d < 3; d++) p[d] = d < S ? src[S * i + d] : 0.;
+  for (int d = 0; d < 3; d++)
+    if (d < S || !keep_z) p[d] = d < S ? src[S * i + d] : 0.;
 }
-__global__ void k_gather_split(int64_t n, int S, const int *perm, const float4 *src, double *dst) {
+__global__ void k_gather_split(int64_t n, int S, const int *perm, const float4 *src, double *dst,
+                               bool keep_z = false) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   double *p = dst + 3 * (int64_t)perm[i];
@@ -318,7 +426,7 @@ __global__ void k_gather_split(int64_t n, int S, const int *perm, const float4 *
     const float4 a = src[i];
     p[0] = (double)a.x + (double)a.z;
     p[1] = (double)a.y + (double)a.w;
-    p[2] = 0.;
+    if (!keep_z) p[2] = 0.;
   } else {
     const float4 a = src[2 * i], b = src[2 * i + 1];
     p[0] = (double)a.x + (double)b.x;
@@ -405,6 +513,9 @@ struct nlm_fd {
   // staging
   double *stage = nullptr;   // 3 slots of 3n doubles (u, v, f in Point3 layout)
   int *bad_input = nullptr;  // set by k_nonfinite
+  int *iperm = nullptr;      // original -> internal node id (in-place host I/O)
+  char *zstage = nullptr;    // state-layout staging of in-place host input
+  int host_io = 0;           // last nlm_fd_step_host: 0 copies, 1 in place
   float *dmg_phi = nullptr, *dmg_Z = nullptr;
   float *en_buf = nullptr;     // nlm_fd_energies: 4 n floats
   double *en_fext = nullptr;   // external force at the current time, S n doubles
@@ -447,6 +558,8 @@ struct nlm_fd {
     if (stream) cudaStreamDestroy(stream);
   }
 };
+
+int get_state_impl(nlm_fd *h, double *u, double *v, double *f, bool keep_z);
 
 namespace {
 
@@ -1408,7 +1521,11 @@ int nlm_fd_sync(nlm_fd *h) {
   return NLM_OK;
 }
 
-int nlm_fd_get_state(nlm_fd *h, double *u, double *v, double *f) {
+}  // extern "C"
+
+// keep_z: the staging slots of u and v hold the caller's arrays as uploaded
+// by the call (nlm_fd_step_host), and their z entries go back unchanged in 2-D.
+int get_state_impl(nlm_fd *h, double *u, double *v, double *f, bool keep_z) {
   if (!h) return fail(NLM_ERR_INVALID, "null handle");
   const int64_t n = h->n;
   cudaStream_t s = h->stream;
@@ -1420,17 +1537,17 @@ int nlm_fd_get_state(nlm_fd *h, double *u, double *v, double *f) {
   double *su = h->stage, *sv = h->stage + 3 * n, *sf = h->stage + 6 * n;
   if (u) {
     if (fp32)
-      k_gather_split<<<g, 256, 0, s>>>(n, h->S, P, h->D.u32[h->cur], su);
+      k_gather_split<<<g, 256, 0, s>>>(n, h->S, P, h->D.u32[h->cur], su, keep_z);
     else
-      k_gather_vec<<<g, 256, 0, s>>>(n, h->S, P, h->D.u64[h->cur], su);
+      k_gather_vec<<<g, 256, 0, s>>>(n, h->S, P, h->D.u64[h->cur], su, keep_z);
     NLM_CUDA(cudaGetLastError());
     NLM_CUDA(cudaMemcpyAsync(u, su, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
   }
   if (v) {
     if (fp32)
-      k_gather_split<<<g, 256, 0, s>>>(n, h->S, P, h->D.v32[h->vidx()], sv);
+      k_gather_split<<<g, 256, 0, s>>>(n, h->S, P, h->D.v32[h->vidx()], sv, keep_z);
     else
-      k_gather_vec<<<g, 256, 0, s>>>(n, h->S, P, h->D.v[h->vidx()], sv);
+      k_gather_vec<<<g, 256, 0, s>>>(n, h->S, P, h->D.v[h->vidx()], sv, keep_z);
     NLM_CUDA(cudaGetLastError());
     NLM_CUDA(cudaMemcpyAsync(v, sv, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
   }
@@ -1444,6 +1561,12 @@ int nlm_fd_get_state(nlm_fd *h, double *u, double *v, double *f) {
   }
   NLM_CUDA(cudaStreamSynchronize(s));
   return NLM_OK;
+}
+
+extern "C" {
+
+int nlm_fd_get_state(nlm_fd *h, double *u, double *v, double *f) {
+  return get_state_impl(h, u, v, f, false);
 }
 
 int nlm_fd_set_state(nlm_fd *h, const double *u, const double *v) {
@@ -1463,11 +1586,12 @@ int nlm_fd_set_state(nlm_fd *h, const double *u, const double *v) {
     NLM_CUDA(cudaGetLastError());
   }
   if (v) {
-    NLM_CUDA(cudaMemcpyAsync(h->stage, v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+    double *sv = h->stage + 3 * n;
+    NLM_CUDA(cudaMemcpyAsync(sv, v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
     if (h->precision == NLM_PREC_FP32C)
-      k_scatter_split<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.v32[h->vidx()]);
+      k_scatter_split<<<g, 256, 0, s>>>(n, h->S, h->dim, P, sv, h->D.v32[h->vidx()]);
     else
-      k_scatter_vec<<<g, 256, 0, s>>>(n, h->S, h->dim, P, h->stage, h->D.v[h->vidx()]);
+      k_scatter_vec<<<g, 256, 0, s>>>(n, h->S, h->dim, P, sv, h->D.v[h->vidx()]);
     NLM_CUDA(cudaGetLastError());
   }
   NLM_CUDA(cudaStreamSynchronize(s));
@@ -1795,15 +1919,142 @@ int nlm_fd_kernel_stats(nlm_fd *h, int reset, double *avg_ms, int64_t *launches,
   return NLM_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+typedef int (*PtrAttrFn)(void *, int, unsigned long long);
+
+// The driver's cuPointerGetAttribute, looked up through the runtime (no link
+// dependency on the driver library).
+PtrAttrFn ptr_attr_fn() {
+  static PtrAttrFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &f, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PtrAttrFn>(f);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+// True when [p, p + bytes) lies inside one page-locked host allocation that
+// the device addresses at the same virtual address, so kernels may read and
+// write it in place.
+bool in_place_ok(const void *p, size_t bytes) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (a.type != cudaMemoryTypeHost || a.devicePointer != p) return false;
+  PtrAttrFn fn = ptr_attr_fn();
+  if (!fn) return false;
+  unsigned long long start = 0;
+  size_t size = 0;
+  if (fn(&start, 11 /* CU_POINTER_ATTRIBUTE_RANGE_START_ADDR */, (unsigned long long)p) != 0 ||
+      fn(&size, 12 /* CU_POINTER_ATTRIBUTE_RANGE_SIZE */, (unsigned long long)p) != 0)
+    return false;
+  const unsigned long long q = (unsigned long long)p;
+  return size > 0 && q >= start && q + bytes <= start + size;
+}
+
+// nlm_fd_step_host with u, v, f read and written in place by kernels (one
+// pass each way over the host link), the state replaced only once the input
+// is known to be finite.
+int step_host_in_place(nlm_fd *h, double *u, double *v, double *f, int64_t nsteps) {
+  const int64_t n = h->n;
+  const int S = h->S;
+  cudaStream_t s = h->stream;
+  const bool fp32 = h->precision == NLM_PREC_FP32C;
+  if (!h->iperm) {
+    if (h->alloc(&h->iperm, n) != cudaSuccess ||
+        h->alloc(&h->zstage, (size_t)24 * S * n + 16 * n) != cudaSuccess)
+      return fail(NLM_ERR_OOM, "in-place host I/O buffers");
+    // padding entries of the staged layouts are never written: zero them once
+    NLM_CUDA(cudaMemsetAsync(h->zstage, 0, (size_t)24 * S * n + 16 * n, s));
+    k_invert_perm<<<nblk(n, 256), 256, 0, s>>>(n, h->D.perm_dev, h->iperm);
+    NLM_CUDA(cudaGetLastError());
+  }
+  const size_t bu = fp32 ? sizeof(float4) * (S / 2) * n : sizeof(double) * S * n;
+  const size_t bf = fp32 ? sizeof(float) * S * n : sizeof(double) * S * n;
+  char *su = h->zstage, *sv = su + bu, *sf = sv + bu;
+  double *zu = reinterpret_cast<double *>(h->zstage + (size_t)24 * S * n), *zv = zu + n;
+  const int64_t pairs = (3 * n + 1) / 2;
+  const double2 *u2 = reinterpret_cast<const double2 *>(u);
+  const double2 *v2 = reinterpret_cast<const double2 *>(v);
+  const double2 *f2 = reinterpret_cast<const double2 *>(f);
+  NLM_CUDA(cudaMemsetAsync(h->bad_input, 0, sizeof(int), s));
+  if (fp32)
+    k_host_in<true><<<nblk(pairs, 256), 256, 0, s>>>(n, S, h->dim, h->iperm, u2, v2, f2, su, sv,
+                                                     sf, zu, zv, h->bad_input);
+  else
+    k_host_in<false><<<nblk(pairs, 256), 256, 0, s>>>(n, S, h->dim, h->iperm, u2, v2, f2, su, sv,
+                                                      sf, zu, zv, h->bad_input);
+  NLM_CUDA(cudaGetLastError());
+  int bad = 0;
+  NLM_CUDA(cudaMemcpyAsync(&bad, h->bad_input, sizeof(int), cudaMemcpyDeviceToHost, s));
+  NLM_CUDA(cudaStreamSynchronize(s));
+  if (bad) return fail(NLM_ERR_NONFINITE, "non-finite state");
+  void *du = fp32 ? (void *)h->D.u32[h->cur] : (void *)h->D.u64[h->cur];
+  void *dv = fp32 ? (void *)h->D.v32[h->vidx()] : (void *)h->D.v[h->vidx()];
+  void *df_ = fp32 ? (void *)h->D.f32 : (void *)h->D.f64;
+  NLM_CUDA(cudaMemcpyAsync(du, su, bu, cudaMemcpyDeviceToDevice, s));
+  NLM_CUDA(cudaMemcpyAsync(dv, sv, bu, cudaMemcpyDeviceToDevice, s));
+  NLM_CUDA(cudaMemcpyAsync(df_, sf, bf, cudaMemcpyDeviceToDevice, s));
+  cudaError_t e = launch_drift(h->P, h->D, h->T, h->cur, h->time + h->dt, fp32, s);
+  if (e != cudaSuccess) return cuda_fail(e, "drift kernel");
+  int rc = do_run(h, nsteps);
+  if (rc) return rc;
+  const void *ou = fp32 ? (const void *)h->D.u32[h->cur] : (const void *)h->D.u64[h->cur];
+  const void *ov = fp32 ? (const void *)h->D.v32[h->vidx()] : (const void *)h->D.v[h->vidx()];
+  const void *of = fp32 ? (const void *)h->D.f32 : (const void *)h->D.f64;
+  double2 *u2o = reinterpret_cast<double2 *>(u), *v2o = reinterpret_cast<double2 *>(v);
+  double2 *f2o = reinterpret_cast<double2 *>(f);
+  if (fp32)
+    k_host_out<true><<<nblk(pairs, 256), 256, 0, s>>>(n, S, h->dim, h->iperm, ou, ov, of, zu, zv,
+                                                      u2o, v2o, f2o);
+  else
+    k_host_out<false><<<nblk(pairs, 256), 256, 0, s>>>(n, S, h->dim, h->iperm, ou, ov, of, zu,
+                                                       zv, u2o, v2o, f2o);
+  NLM_CUDA(cudaGetLastError());
+  NLM_CUDA(cudaStreamSynchronize(s));
+  h->host_io = 1;
+  return NLM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nlm_fd_host_io(const nlm_fd *h, int *mode) {
+  if (!h || !mode) return fail(NLM_ERR_INVALID, "null argument");
+  *mode = h->host_io;
+  return NLM_OK;
+}
+
 int nlm_fd_step_host(nlm_fd *h, double *u, double *v, double *f, int64_t nsteps) {
   if (!h || !u || !v || !f || nsteps < 0) return fail(NLM_ERR_INVALID, "null argument");
   if (!h->started) {
     int rc = nlm_fd_set_state(h, u, v);
     if (rc) return rc;
     if ((rc = do_run(h, nsteps))) return rc;
-    return nlm_fd_get_state(h, u, v, f);
+    return get_state_impl(h, u, v, f, true);
   }
   const int64_t n = h->n;
+  const size_t bytes = sizeof(double) * 3 * n;
+  // in place: page-locked arrays on 16-byte boundaries holding an even
+  // number of doubles (whole 16-byte pairs)
+  const bool aligned = ((uintptr_t)u | (uintptr_t)v | (uintptr_t)f) % 16 == 0 && n % 2 == 0;
+  if (aligned && in_place_ok(u, bytes) && in_place_ok(v, bytes) && in_place_ok(f, bytes))
+    return step_host_in_place(h, u, v, f, nsteps);
+  h->host_io = 0;
   cudaStream_t s = h->stream;
   const int *P = h->D.perm_dev;
   const unsigned g = nblk(n, 256);
@@ -1835,7 +2086,7 @@ int nlm_fd_step_host(nlm_fd *h, double *u, double *v, double *f, int64_t nsteps)
   if (e != cudaSuccess) return cuda_fail(e, "drift kernel");
   int rc = do_run(h, nsteps);
   if (rc) return rc;
-  return nlm_fd_get_state(h, u, v, f);
+  return get_state_impl(h, u, v, f, true);
 }
 
 int nlm_fd_set_graph(nlm_fd *h, int steps_per_graph) {

@@ -165,6 +165,13 @@ class FDModel:
         _check(load().nlm_fd_step_host(self.h, C.cast(u_ptr, P), C.cast(v_ptr, P),
                                        C.cast(f_ptr, P), C.c_int64(int(nsteps))))
 
+    def host_io(self):
+        """1 if the last step_host read and wrote the arrays in place
+        (page-locked buffers), 0 if it copied them."""
+        m = C.c_int()
+        _check(load().nlm_fd_host_io(self.h, C.byref(m)))
+        return m.value
+
     def run_timed(self, nsteps):
         """Run nsteps; returns the device time in ms (CUDA events on the
         handle's stream)."""

@@ -397,3 +397,34 @@ def test_graph_replay_with_force_loads(gpu):
         runs.append(m.state())
     for a, b in zip(*runs):
         assert np.array_equal(a, b)
+
+
+def test_step_host_in_place_matches_copies(gpu):
+    """Page-locked arrays are read and written in place by kernels; pageable
+    ones go through copies.  Both give the same state bit for bit, keep the
+    caller's z of u and v in 2-D, write f's z as 0, and refuse a non-finite
+    input without touching the model."""
+    torch = pytest.importorskip("torch")
+    p = configs.rnp_plate(30, 1e-3, 3, 0.008, 0.1, 2e-8, 50, seed=2)
+    n = p.n
+    for prec in (abi.FP64, abi.FP32C):
+        a = gpu.FDModel(p, precision=prec, decomposition=abi.DECOMP_THREAD)
+        b = gpu.FDModel(p, precision=prec, decomposition=abi.DECOMP_THREAD)
+        host = [np.zeros((n, 3)) for _ in range(3)]
+        pin = [torch.zeros((n, 3), dtype=torch.float64).pin_memory() for _ in range(3)]
+        for arr in (host[0], host[1], pin[0].numpy(), pin[1].numpy()):
+            arr[:, 2] = 7.0
+        ptrs = [t.data_ptr() for t in pin]
+        for k in range(4):
+            a.step_host(*host, nsteps=3)
+            b.step_host_ptr(*ptrs, nsteps=3)
+        assert a.host_io() == 0 and b.host_io() == 1
+        for x, y in zip(host, pin):
+            assert np.array_equal(x, y.numpy())
+        assert np.all(host[0][:, 2] == 7.0) and np.all(host[1][:, 2] == 7.0)
+        assert np.all(host[2][:, 2] == 0.0)
+        t0, u0 = b.time(), b.state()[0].copy()
+        pin[1].numpy()[5, 0] = np.inf
+        with pytest.raises(gpu.NLMError):
+            b.step_host_ptr(*ptrs, nsteps=1)
+        assert b.time() == t0 and np.array_equal(b.state()[0], u0)

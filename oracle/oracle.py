@@ -379,3 +379,17 @@ class RefRNP:
         R = np.zeros((self.n, 3))
         self._chk(ref_lib().ref_rnp_reaction_force(self.h, abi.dptr(R)))
         return R
+
+
+def ref_mesh_volumes(dim, nodes, element_type, elements):
+    """The reference's own fe::Mesh::computeVol (mesh.cpp:231-309) on a mesh
+    given as nodes (n, 3) and element connectivity (refshim; test use)."""
+    x = np.ascontiguousarray(nodes, dtype=np.float64).reshape(-1, 3)
+    E = np.ascontiguousarray(elements, dtype=np.int64)
+    vol = np.zeros(x.shape[0])
+    rc = ref_lib().ref_mesh_volumes(C.c_int(dim), C.c_int64(x.shape[0]), abi.dptr(x),
+                                   C.c_int(int(element_type)), C.c_int64(E.shape[0]),
+                                   abi.ptr(E, C.c_int64), abi.dptr(vol))
+    if rc != 0:
+        raise RuntimeError("refshim error: %s" % ref_lib().ref_rnp_last_error().decode())
+    return vol

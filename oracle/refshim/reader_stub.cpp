@@ -2,13 +2,16 @@
 //
 // TEST INFRASTRUCTURE ONLY (oracle/refshim).  The reference's rw/reader.cpp
 // needs VTK and Gmsh; the refshim hands nodes and volumes to
-// fe::Mesh::setMeshData instead, so these entry points are never reached and
-// throw if they are.
+// fe::Mesh::setMeshData instead, so these entry points throw if they are
+// reached, except readMshFile, which hands over a mesh the driver put in
+// g_injected_mesh (nodes, element type, connectivity) so that the reference's
+// fe::Mesh::createData and computeVol run on it.
 #include <stdexcept>
 #include <string>
 #include <vector>
 
 #include "rw/reader.h"
+#include "reader_stub.h"
 
 namespace {
 [[noreturn]] void unavailable(const char *what) {
@@ -44,8 +47,22 @@ bool rw::reader::readVtuFilePointData(const std::string &, const std::string &,
                                       std::vector<util::Point3> *) {
   unavailable("vtu point data");
 }
-void rw::reader::readMshFile(const std::string &, size_t, std::vector<util::Point3> *, size_t &,
-                             size_t &, std::vector<size_t> *,
-                             std::vector<std::vector<size_t>> *, std::vector<double> *, bool) {
-  unavailable("msh");
+InjectedMesh g_injected_mesh;
+
+// The node-element lists as MshReader::readMesh forms them
+// (mshReader.cpp:95-113): element ids in connectivity order.
+void rw::reader::readMshFile(const std::string &, size_t, std::vector<util::Point3> *nodes,
+                             size_t &element_type, size_t &num_elem, std::vector<size_t> *enc,
+                             std::vector<std::vector<size_t>> *nec, std::vector<double> *volumes,
+                             bool) {
+  const InjectedMesh &m = g_injected_mesh;
+  if (m.nodes.empty()) unavailable("msh");
+  *nodes = m.nodes;
+  element_type = m.element_type;
+  *enc = m.enc;
+  volumes->clear();
+  nec->assign(m.nodes.size(), {});
+  const size_t nv = m.vertices;
+  for (size_t j = 0; j < m.enc.size(); j++) (*nec)[m.enc[j]].push_back(j / nv);
+  num_elem = m.enc.size() / nv;
 }

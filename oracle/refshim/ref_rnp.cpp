@@ -44,6 +44,8 @@
 #include "loading/uLoading.h"
 #include "material/pd/rnpBond.h"
 #include "util/utilGeom.h"
+#include "inp/decks/meshDeck.h"
+#include "reader_stub.h"
 
 namespace {
 
@@ -463,6 +465,36 @@ int ref_rnp_reaction_force(ref_rnp *h, double *R) {
       R[3 * i + 2] = r.d_z;
     }
   } catch (const std::exception &e) {
+    return fail(e.what());
+  }
+  return 0;
+}
+
+// fe::Mesh::computeVol (mesh.cpp:231-309) on a mesh given as nodes and
+// element connectivity: the reference's Mesh constructor reads it through the
+// stub readMshFile and computes the nodal volumes with its own quadrature.
+int ref_mesh_volumes(int dim, int64_t n, const double *x, int etype, int64_t nelem,
+                     const int64_t *enc, double *vol) {
+  try {
+    const size_t nv = etype == 5 ? 3 : (etype == 9 || etype == 10 ? 4 : 0);
+    if (!nv) return fail("element type must be triangle (5), quad (9) or tetrahedron (10)");
+    InjectedMesh &m = g_injected_mesh;
+    m.nodes.clear();
+    for (int64_t i = 0; i < n; i++) m.nodes.emplace_back(x[3 * i], x[3 * i + 1], x[3 * i + 2]);
+    m.element_type = (size_t)etype;
+    m.vertices = nv;
+    m.enc.assign(enc, enc + nelem * (int64_t)nv);
+    inp::MeshDeck deck;
+    deck.d_dim = (size_t)dim;
+    deck.d_spatialDiscretization = "finite_difference";
+    deck.d_filename = "injected.msh";
+    deck.d_h = 0.;  // the constructor's volume floor 0.01 h^dim stays 0
+    fe::Mesh mesh(&deck);
+    const auto &v = mesh.getNodalVolumes();
+    for (int64_t i = 0; i < n; i++) vol[i] = v[i];
+    m.nodes.clear();
+  } catch (const std::exception &e) {
+    g_injected_mesh.nodes.clear();
     return fail(e.what());
   }
   return 0;

@@ -313,3 +313,32 @@ def test_reference_gmsh_deck_reads_its_mesh():
                         (x[E[:, 2], 0] - x[E[:, 0], 0]) * (x[E[:, 1], 1] - x[E[:, 0], 1]))
     assert abs(p.volume.sum() - area.sum()) < 1e-12 * area.sum()
     assert p.fbc[0].spatial_fn == "sin_x" and p.fbc[0].time_params == [1.5e9]
+
+
+@pytest.mark.skipif(not orc.refshim_available(), reason="reference source tree not present")
+def test_nodal_volumes_match_reference_computevol():
+    """meshfile.compute_volumes against the reference's fe::Mesh::computeVol
+    (its own quadrature, run through the refshim) on jittered triangle and
+    quadrangle meshes and, with the reference tree, its Gmsh example."""
+    rng = np.random.default_rng(3)
+    n = 9
+    g = np.linspace(0.0, 2.0, n + 1)
+    X, Y = np.meshgrid(g, g, indexing="ij")
+    nodes = np.stack([X.ravel(), Y.ravel(), 0 * X.ravel()], axis=1)
+    nodes[:, :2] += rng.uniform(-0.04, 0.04, size=(nodes.shape[0], 2))
+    idx = np.arange((n + 1) ** 2).reshape(n + 1, n + 1)
+    tris, quads = [], []
+    for i in range(n):
+        for j in range(n):
+            a, b, c, d = idx[i, j], idx[i + 1, j], idx[i + 1, j + 1], idx[i, j + 1]
+            tris += [[a, b, c], [a, c, d]]
+            quads.append([a, b, c, d])
+    cases = [(meshfile.VTK_TRIANGLE, np.array(tris)), (meshfile.VTK_QUAD, np.array(quads))]
+    logo = os.path.join(REF, "examples/fdModel/logo/mesh.msh")
+    meshes = [meshfile.Mesh(nodes=nodes, volumes=None, element_type=t, elements=E) for t, E in cases]
+    if os.path.exists(logo):
+        meshes.append(meshfile.read_msh(logo, 2))
+    for m in meshes:
+        ours = meshfile.compute_volumes(m)
+        ref = orc.ref_mesh_volumes(2, m.nodes, m.element_type, m.elements)
+        assert np.abs(ours - ref).max() <= 1e-13 * np.abs(ref).max(), m.element_type

@@ -66,6 +66,53 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+class Ranks:
+    """Barrier and reductions over the ranks of a replicas run: one process
+    per GPU, each stepping its own specimen (seed = rank); the job's time is
+    the slowest rank's, its work the sum over ranks.  With one rank no
+    process group exists.  device "cuda" synchronises the GPU around each
+    barrier; "cpu" (a gloo group) is for tests of the reduction logic."""
+
+    def __init__(self, world, device="cuda"):
+        self.world = world
+        self.device = device
+
+    def _sync(self):
+        if self.device == "cuda":
+            import torch
+            torch.cuda.synchronize()
+
+    def barrier(self):
+        self._sync()
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+            self._sync()
+
+    def _reduce(self, v, op):
+        if self.world == 1:
+            return v
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([v], dtype=torch.float64, device=self.device)
+        dist.all_reduce(t, op=op)
+        return float(t.item())
+
+    def max(self, v):
+        import torch.distributed as dist
+        return self._reduce(v, dist.ReduceOp.MAX)
+
+    def sum(self, v):
+        import torch.distributed as dist
+        return self._reduce(v, dist.ReduceOp.SUM)
+
+
+def throughput(bonds_per_rank, steps, seconds_per_rank, ranks):
+    """Whole-job bond-updates/s: the bonds of every rank's specimen times the
+    steps, over the slowest rank's time."""
+    return ranks.sum(float(bonds_per_rank)) * steps / ranks.max(seconds_per_rank)
+
+
 def problem(nx, seed):
     from nlmech_gb300 import configs
     if nx == 1000:
@@ -212,25 +259,8 @@ def run_ours(a):
     p = problem(a.nx, seed=rank)
     n = p.n
 
-    def barrier_sync():
-        torch.cuda.synchronize()
-        if world > 1:
-            torch.distributed.barrier()
-            torch.cuda.synchronize()
-
-    def max_over_ranks(v):
-        if world == 1:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
-
-    def sum_over_ranks(v):
-        if world == 1:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t)
-        return float(t.item())
+    ranks = Ranks(world, "cuda")
+    barrier_sync, max_over_ranks, sum_over_ranks = ranks.barrier, ranks.max, ranks.sum
 
     # ---- FP32-compensated (headline) ----
     dmap = {"auto": abi.DECOMP_AUTO, "thread": abi.DECOMP_THREAD,

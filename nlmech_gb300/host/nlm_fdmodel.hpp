@@ -160,12 +160,124 @@ class FDModel {
     Z.resize(d_deck.nodes.size());
     check(nlm_fd_damage(d_h, phi.data(), Z.data()));
   }
+  // computePostProcFields energies: Strain_Energy, Work_Done, kinetic and
+  // fracture energy per node; totals = their sums.
+  void energies(std::vector<float> &strain, std::vector<float> &work,
+                std::vector<float> &kinetic, std::vector<float> &fracture,
+                double totals[4]) const {
+    const size_t n = d_deck.nodes.size();
+    strain.resize(n);
+    work.resize(n);
+    kinetic.resize(n);
+    fracture.resize(n);
+    check(nlm_fd_energies(d_h, strain.data(), work.data(), kinetic.data(), fracture.data(),
+                          totals));
+  }
+  // Reaction_Force per node and its sum (computeForce, 2-D RNPBond).
+  std::vector<Point3> reactionForce(Point3 *sum = nullptr) const {
+    std::vector<Point3> R(d_deck.nodes.size());
+    double s[3];
+    check(nlm_fd_reaction_force(d_h, reinterpret_cast<double *>(R.data()), nullptr, s));
+    if (sum) *sum = {s[0], s[1], s[2]};
+    return R;
+  }
+  // fe::Mesh fixity bits as the displacement loading sets them.
+  std::vector<uint8_t> fixity() const {
+    std::vector<uint8_t> fx(d_deck.nodes.size());
+    check(nlm_fd_get_fixity(d_h, fx.data()));
+    return fx;
+  }
+  // FDModel::restart: start at Restart.Step with the given u and v.
+  void restart(int64_t step, const std::vector<Point3> &u, const std::vector<Point3> &v) {
+    check(nlm_fd_set_state(d_h, reinterpret_cast<const double *>(u.data()),
+                           reinterpret_cast<const double *>(v.data())));
+    check(nlm_fd_set_time(d_h, double(step) * d_deck.dt, step));
+    sync_state();
+  }
+  // Checkpoint with the bond state (save) and continue from one (load).
+  void save(const std::string &path) const { check(nlm_fd_save(d_h, path.c_str())); }
+  void load(const std::string &path) {
+    check(nlm_fd_load(d_h, path.c_str()));
+    sync_state();
+  }
   nlm_fd *handle() const { return d_h; }
 
  private:
   Deck d_deck;
   nlm_fd *d_h = nullptr;
   std::vector<Point3> d_u, d_v, d_f;
+};
+
+// QuasiStaticModel<ElasticState> (src/model/quasistatic/QuasiStaticModel.cpp):
+// the Solver block and one solve per load step (solver, :526-594).
+struct SolverDeck {
+  int max_iters = 100;         // Solver.Max_Iteration
+  double tol = 1e-6;           // Solver.Tolerance
+  double perturbation = 1e-7;  // Solver.Perturbation
+  int full_jacobian = 0;       // 0: the reference's (i, r; j, r) entries
+  int lin_max_iters = 5000;
+  double lin_tol = 1e-12;
+};
+
+template <class T>
+class QuasiStaticModel {
+ public:
+  QuasiStaticModel(const Deck &deck, const SolverDeck &solver) : d_n(deck.nodes.size()) {
+    static_assert(T::kind == NLM_MAT_ELASTIC_STATE,
+                  "QuasiStaticModel is instantiated for ElasticState");
+    nlm_fd_desc d{};
+    d.dim = deck.dim;
+    d.n_nodes = (int64_t)deck.nodes.size();
+    d.x = reinterpret_cast<const double *>(deck.nodes.data());
+    d.volume = deck.volumes.data();
+    d.horizon = deck.horizon;
+    d.mesh_size = deck.mesh_size;
+    d.material = deck.material;
+    d.material.kind = T::kind;
+    d.n_ubc = (int)deck.ubc.size();
+    d.ubc = deck.ubc.data();
+    d.n_fbc = (int)deck.fbc.size();
+    d.fbc = deck.fbc.data();
+    d.dt = deck.dt;
+    nlm_esqs_params p{};
+    p.jacobian = solver.full_jacobian;
+    p.max_iters = solver.max_iters;
+    p.tol = solver.tol;
+    p.perturbation = solver.perturbation;
+    p.lin_max_iters = solver.lin_max_iters;
+    p.lin_tol = solver.lin_tol;
+    p.dt = deck.dt;
+    check(nlm_esqs_create(&d, &p, &d_q));
+  }
+  ~QuasiStaticModel() {
+    if (d_q) nlm_esqs_destroy(d_q);
+  }
+  QuasiStaticModel(const QuasiStaticModel &) = delete;
+  QuasiStaticModel &operator=(const QuasiStaticModel &) = delete;
+
+  // n load steps; returns the Newton iterations of the last and its residual.
+  int solve(int n, double *residual = nullptr) {
+    std::vector<int> it(n > 0 ? n : 1);
+    double r = 0.;
+    check(nlm_esqs_solve(d_q, n, it.data(), nullptr, &r));
+    if (residual) *residual = r;
+    return n > 0 ? it[n - 1] : 0;
+  }
+  std::vector<Point3> displacement() const {
+    std::vector<Point3> u(d_n);
+    check(nlm_esqs_get_state(d_q, reinterpret_cast<double *>(u.data()), nullptr));
+    return u;
+  }
+  // The output's "Force": force density times nodal volume.
+  std::vector<Point3> force() const {
+    std::vector<Point3> f(d_n);
+    check(nlm_esqs_get_state(d_q, nullptr, reinterpret_cast<double *>(f.data())));
+    return f;
+  }
+
+ private:
+  size_t d_n;
+  nlm_esqs *d_q = nullptr;
 };
 
 }  // namespace nlm

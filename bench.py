@@ -339,6 +339,7 @@ def run_ours(a):
     barrier_sync()
     te = max_over_ranks(time.perf_counter() - t0)
     e2e_value = total_bonds * a.e2e_steps / te
+    e2e_io = me.host_io()
     me.close()
 
     if rank != 0:
@@ -368,7 +369,9 @@ def run_ours(a):
         "broken_bonds_after_run": broken,
         "e2e": {"value": e2e_value, "unit": UNIT, "steps": a.e2e_steps,
                 "h2d_bytes_per_step": 3 * 3 * 8 * n, "d2h_bytes_per_step": 3 * 3 * 8 * n,
-                "call": "nlm_fd_step_host (u, v, f in/out of pinned host memory each step)"},
+                "call": "nlm_fd_step_host (u, v, f in/out of pinned host memory each step)",
+                "host_io": {0: "copies", 1: "in place", 2: "banded copies overlapping the step"}
+                .get(e2e_io, e2e_io)},
         "gpu_launches": a.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,

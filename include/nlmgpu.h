@@ -347,9 +347,14 @@ int nlm_fd_step_host(nlm_fd *h, double *u, double *v, double *f,
 /* How the last nlm_fd_step_host moved the arrays: 1 = read and written in
  * place by kernels (each of u, v, f lies inside one page-locked allocation
  * the device maps at the same address, e.g. from cudaHostAlloc or
- * cudaHostRegister), 0 = copied through device staging buffers.  In 2-D the
- * z entries of u and v are left as the caller had them either way (the
- * reference's 2-D integrator never writes them) and f's z is written as 0. */
+ * cudaHostRegister), 0 = copied through device staging buffers, 2 = page-
+ * locked arrays moved in caller-order bands whose copies in and out overlap
+ * the step (one FP32C velocity-Verlet step of a 2-D model of at least 65536
+ * nodes on a tile decomposition; same results as the other two).  On a
+ * non-finite input every mode fails with the model unchanged; modes 1 and 2
+ * also leave the caller's arrays as they were.  In 2-D the z entries of u
+ * and v are left as the caller had them either way (the reference's 2-D
+ * integrator never writes them) and f's z is written as 0. */
 int nlm_fd_host_io(const nlm_fd *h, int *mode);
 /* nlm_fd_run bracketed by CUDA events on the handle's stream; *ms is the
  * device time of the whole run (the stream is synchronized). */

@@ -18,6 +18,8 @@
 // TwoProduct): GB300's FP64 rate is a small fraction of its FP32 rate, and the
 // per-node FP64 update would otherwise be the slowest part of the step.
 
+#include <algorithm>
+
 #include "fp32_common.cuh"
 
 namespace nlm {
@@ -288,9 +290,10 @@ __global__ void __launch_bounds__(kTileNodes, 3)
   __shared__ float4 s_pos[kTileMaxLocal];
   __shared__ float4 s_u[kTileMaxLocal];
   __shared__ uint8_t s_fl[(OPT & OPT_NOFAIL) ? kTileMaxLocal : 1];
-  const int64_t t0 = (int64_t)blockIdx.x * kTileNodes;
-  const int h0 = D.tile_hptr[blockIdx.x];
-  const int nh = D.tile_hptr[blockIdx.x + 1] - h0;
+  const int tb = A.tiles ? A.tiles[blockIdx.x] : (int)blockIdx.x;
+  const int64_t t0 = (int64_t)tb * kTileNodes;
+  const int h0 = D.tile_hptr[tb];
+  const int nh = D.tile_hptr[tb + 1] - h0;
   const int nt = (int)min((int64_t)kTileNodes, P.n - t0);
   const float4 *ucur = D.u32[A.cur];
   for (int e = threadIdx.x; e < kTileNodes + nh; e += blockDim.x) {
@@ -375,9 +378,10 @@ __global__ void __launch_bounds__(kTileNodes, 4)
   __shared__ float s_vol[kTileMaxLocal];  // K1 V (V with the contact term)
   constexpr bool KV = !(OPT & OPT_CONTACT);
   __shared__ uint8_t s_fl[(OPT & OPT_NOFAIL) ? kTileMaxLocal : 1];
-  const int64_t t0 = (int64_t)blockIdx.x * kTileNodes;
-  const int h0 = D.tile_hptr[blockIdx.x];
-  const int nh = D.tile_hptr[blockIdx.x + 1] - h0;
+  const int tb = A.tiles ? A.tiles[blockIdx.x] : (int)blockIdx.x;
+  const int64_t t0 = (int64_t)tb * kTileNodes;
+  const int h0 = D.tile_hptr[tb];
+  const int nh = D.tile_hptr[tb + 1] - h0;
   const int nt = (int)min((int64_t)kTileNodes, P.n - t0);
   const float4 *ucur = D.u32[A.cur];
   const float4 po = __ldg(D.pos32 + t0);
@@ -465,8 +469,11 @@ static void launch_opt(const StepParams &P, const Params32 &Q, const DevPtrs &D,
   const int64_t nodes = a.i1 - a.i0;
   if (nodes <= 0) return;
   if (DIM == 2 && !BATCH && decomp == NLM_DECOMP_TILE) {
-    // the tile store covers the whole node range [0, n)
-    const unsigned grid = (unsigned)((P.n + kTileNodes - 1) / kTileNodes);
+    // the tile store covers the whole node range [0, n); a tile list picks
+    // some of its tiles
+    const unsigned grid =
+        a.tiles ? (unsigned)a.ntiles : (unsigned)((P.n + kTileNodes - 1) / kTileNodes);
+    if (grid == 0) return;
     if (P.nw1)
       k_rnp32_tile<SCHEME, true, OPT><<<grid, kTileNodes, 0, s>>>(P, Q, D, T, a);
     else
@@ -474,7 +481,9 @@ static void launch_opt(const StepParams &P, const Params32 &Q, const DevPtrs &D,
     return;
   }
   if (DIM == 2 && !BATCH && decomp == NLM_DECOMP_TILE_LOCAL) {
-    const unsigned grid = (unsigned)((P.n + kTileNodes - 1) / kTileNodes);
+    const unsigned grid =
+        a.tiles ? (unsigned)a.ntiles : (unsigned)((P.n + kTileNodes - 1) / kTileNodes);
+    if (grid == 0) return;
     if (P.nw1)
       k_rnp32_tilel<SCHEME, true, OPT><<<grid, kTileNodes, 0, s>>>(P, Q, D, T, a);
     else
@@ -541,19 +550,15 @@ cudaError_t launch_rnp_step_fp32(const StepParams &P, const DevPtrs &D, const BC
                                          : launch32<3, NLM_CENTRAL_DIFFERENCE>(P, D, T, a, decomp, s);
 }
 
-// Drift after a host state upload: the second half of integrate_node32.
+// One node's drift from the state (u, v, f) of the last step: the second
+// half of integrate_node32, prescribed dofs from the loading at t_next.
 template <int DIM>
-__global__ void k_drift32(const StepParams P, const Params32 Q, const DevPtrs D,
-                          const BCTable T, int cur, double t_next) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= P.n) return;
-  const uint8_t fl = D.flags[i];
-  const int ref = (fl & 7) ? D.bcref[i] : -1;
-  float uh[3], ul[3], vh[3], vl[3], f[3] = {0.f, 0.f, 0.f};
-  ld_pair<DIM>(D.u32[cur], i, uh, ul);
-  ld_pair<DIM>(D.v32[P.scheme == NLM_CENTRAL_DIFFERENCE ? cur : 0], i, vh, vl);
-  for (int c = 0; c < DIM; c++) f[c] = D.f32[(int64_t)(DIM == 2 ? 2 : 4) * i + c];
-  df un[3], vn[3];
+__device__ __forceinline__ void drift_node32(const StepParams &P, const Params32 &Q,
+                                             const DevPtrs &D, const BCTable &T, uint8_t fl,
+                                             int ref, const float uh[3], const float ul[3],
+                                             const float vh[3], const float vl[3],
+                                             const float f[3], double t_next, df un[3],
+                                             df vn[3]) {
   for (int c = 0; c < DIM; c++) {
     if (!(fl >> c & 1)) {
       const df u{uh[c], ul[c]}, v{vh[c], vl[c]};
@@ -570,8 +575,143 @@ __global__ void k_drift32(const StepParams P, const Params32 Q, const DevPtrs D,
       bc_df(D, T, ref, c, t_next, un[c], vn[c]);
     }
   }
+}
+
+// Drift after a host state upload.
+template <int DIM>
+__global__ void k_drift32(const StepParams P, const Params32 Q, const DevPtrs D,
+                          const BCTable T, int cur, double t_next) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const uint8_t fl = D.flags[i];
+  const int ref = (fl & 7) ? D.bcref[i] : -1;
+  float uh[3], ul[3], vh[3], vl[3], f[3] = {0.f, 0.f, 0.f};
+  ld_pair<DIM>(D.u32[cur], i, uh, ul);
+  ld_pair<DIM>(D.v32[P.scheme == NLM_CENTRAL_DIFFERENCE ? cur : 0], i, vh, vl);
+  for (int c = 0; c < DIM; c++) f[c] = D.f32[(int64_t)(DIM == 2 ? 2 : 4) * i + c];
+  df un[3], vn[3];
+  drift_node32<DIM>(P, Q, D, T, fl, ref, uh, ul, vh, vl, f, t_next, un, vn);
   st_pair<DIM>(D.u32[1 - cur], i, un);
   if (P.scheme == NLM_CENTRAL_DIFFERENCE) st_pair<DIM>(D.v32[1 - cur], i, vn);
+}
+
+// Banded host step (2-D velocity Verlet, FP32C), input side: caller nodes
+// [o0, o1) of the staged caller arrays (caller order, 3 doubles per node)
+// into the internal order -- the drifted u into ua, v and f as the step
+// kernel reads them -- with the same (hi, lo) splits as a whole-state upload,
+// and a flag for any non-finite value.
+__global__ void k_pipe_in32(const StepParams P, const Params32 Q, const DevPtrs D,
+                            const BCTable T, double t_next, int64_t o0, int64_t o1,
+                            const int *iperm, const double *hu, const double *hv,
+                            const double *hf, float4 *ua, float4 *sv, float2 *sf, int *bad) {
+  const int64_t o = o0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (o >= o1) return;
+  double u[3], v[3], f[3];
+  bool ok = true;
+  for (int d = 0; d < 3; d++) {
+    u[d] = hu[3 * o + d];
+    v[d] = hv[3 * o + d];
+    f[d] = hf[3 * o + d];
+    ok = ok && isfinite(u[d]) && isfinite(v[d]) && isfinite(f[d]);
+  }
+  if (!ok) atomicExch(bad, 1);
+  const int64_t i = iperm[o];
+  const uint8_t fl = D.flags[i];
+  const int ref = (fl & 7) ? D.bcref[i] : -1;
+  float uh[3] = {0.f, 0.f, 0.f}, ul[3] = {0.f, 0.f, 0.f}, vh[3] = {0.f, 0.f, 0.f},
+        vl[3] = {0.f, 0.f, 0.f}, fs[3] = {0.f, 0.f, 0.f};
+  for (int c = 0; c < 2; c++) {
+    const df a = df_from_double(u[c]), b = df_from_double(v[c]);
+    uh[c] = a.hi;
+    ul[c] = a.lo;
+    vh[c] = b.hi;
+    vl[c] = b.lo;
+    fs[c] = __double2float_rn(f[c]);
+  }
+  df un[3], vn[3];
+  drift_node32<2>(P, Q, D, T, fl, ref, uh, ul, vh, vl, fs, t_next, un, vn);
+  st_pair<2>(ua, i, un);
+  sv[i] = make_float4(vh[0], vh[1], vl[0], vl[1]);
+  sf[i] = make_float2(fs[0], fs[1]);
+}
+
+// Output side: caller nodes [o0, o1) (or list[o0 .. o1) when a list is
+// given) after the step, as doubles in the caller order -- u from ua, v and f
+// as the step wrote them -- with the caller's own z of u and v (the 2-D
+// integrator never changes it) and f's z = 0.
+__global__ void k_pipe_out32(int64_t o0, int64_t o1, const int *list, const int *iperm,
+                             const float4 *ua, const float4 *sv, const float2 *sf,
+                             const double *hu_in, const double *hv_in, double *ou, double *ov,
+                             double *of) {
+  const int64_t t = o0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= o1) return;
+  const int64_t o = list ? (int64_t)list[t] : t;
+  const int64_t i = iperm[o];
+  const float4 a = ua[i], b = sv[i];
+  const float2 c = sf[i];
+  ou[3 * o] = (double)a.x + (double)a.z;
+  ou[3 * o + 1] = (double)a.y + (double)a.w;
+  ou[3 * o + 2] = hu_in[3 * o + 2];
+  ov[3 * o] = (double)b.x + (double)b.z;
+  ov[3 * o + 1] = (double)b.y + (double)b.w;
+  ov[3 * o + 2] = hv_in[3 * o + 2];
+  of[3 * o] = (double)c.x;
+  of[3 * o + 1] = (double)c.y;
+  of[3 * o + 2] = 0.;
+}
+
+// End of a banded step: with a finite input the step's arrays become the
+// state (u now, u of the next step, v, f); otherwise the bond bits the step
+// may have set are put back and the state is left as it was.
+__global__ void k_pipe_commit32(int64_t n, int64_t nbits, const int *bad, const float4 *ua,
+                                const float4 *ub, const float4 *sv, const float2 *sf,
+                                float4 *u_now, float4 *u_next, float4 *v, float2 *f,
+                                uint32_t *bits, const uint32_t *bits_saved) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (*bad) {
+    if (k < nbits) bits[k] = bits_saved[k];
+    return;
+  }
+  if (k < n) {
+    u_now[k] = ua[k];
+    u_next[k] = ub[k];
+    v[k] = sv[k];
+    f[k] = sf[k];
+  }
+}
+
+cudaError_t launch_pipe_in32(const StepParams &P, const DevPtrs &D, const BCTable &T,
+                             double t_next, int64_t o0, int64_t o1, const int *iperm,
+                             const double *hu, const double *hv, const double *hf, float4 *ua,
+                             float4 *sv, float2 *sf, int *bad, cudaStream_t s) {
+  if (o1 <= o0) return cudaSuccess;
+  const Params32 Q = make_p32(P);
+  k_pipe_in32<<<(unsigned)((o1 - o0 + 255) / 256), 256, 0, s>>>(P, Q, D, T, t_next, o0, o1,
+                                                                 iperm, hu, hv, hf, ua, sv, sf,
+                                                                 bad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pipe_out32(int64_t o0, int64_t o1, const int *list, const int *iperm,
+                              const float4 *ua, const float4 *sv, const float2 *sf,
+                              const double *hu_in, const double *hv_in, double *ou, double *ov,
+                              double *of, cudaStream_t s) {
+  if (o1 <= o0) return cudaSuccess;
+  k_pipe_out32<<<(unsigned)((o1 - o0 + 255) / 256), 256, 0, s>>>(o0, o1, list, iperm, ua, sv,
+                                                                  sf, hu_in, hv_in, ou, ov, of);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pipe_commit32(int64_t n, int64_t nbits, const int *bad, const float4 *ua,
+                                 const float4 *ub, const float4 *sv, const float2 *sf,
+                                 float4 *u_now, float4 *u_next, float4 *v, float2 *f,
+                                 uint32_t *bits, const uint32_t *bits_saved, cudaStream_t s) {
+  const int64_t m = std::max(n, nbits);
+  if (m == 0) return cudaSuccess;
+  k_pipe_commit32<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(n, nbits, bad, ua, ub, sv, sf,
+                                                               u_now, u_next, v, f, bits,
+                                                               bits_saved);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_drift32(const StepParams &P, const DevPtrs &D, const BCTable &T, int cur,

@@ -515,7 +515,25 @@ struct nlm_fd {
   int *bad_input = nullptr;  // set by k_nonfinite
   int *iperm = nullptr;      // original -> internal node id (in-place host I/O)
   char *zstage = nullptr;    // state-layout staging of in-place host input
-  int host_io = 0;           // last nlm_fd_step_host: 0 copies, 1 in place
+  int host_io = 0;           // last nlm_fd_step_host: 0 copies, 1 in place, 2 banded
+  // banded host step: the caller's arrays move in contiguous bands on the copy
+  // engines, each band's arrival releases the tiles whose nodes and halo it
+  // completes, and a band goes back out once all tiles owning its nodes ran
+  std::vector<int> tile_need;  // per tile: highest caller index its step reads
+  int pipe_state = 0;          // 0 not set up, 1 ready, -1 unavailable
+  int pipe_nbands = 0;
+  std::vector<int64_t> pipe_bounds;  // band b = caller nodes [bounds[b], bounds[b + 1])
+  std::vector<int> pipe_toff;  // stage k runs pipe_tiles[toff[k] .. toff[k + 1])
+  std::vector<std::vector<int>> pipe_out;  // bands written back after stage k
+  int *pipe_tiles = nullptr;
+  int *pipe_late = nullptr;    // caller nodes final only after their band went out
+  int64_t pipe_nlate = 0;
+  double *pipe_in = nullptr, *pipe_back = nullptr;  // staged u, v, f: 9 n doubles each
+  float4 *pipe_ua = nullptr, *pipe_ub = nullptr, *pipe_v = nullptr;
+  float2 *pipe_f = nullptr;
+  uint32_t *pipe_bits = nullptr;
+  cudaStream_t pipe_sin = nullptr, pipe_sout = nullptr;
+  std::vector<cudaEvent_t> pipe_ev;  // per band: input arrived, output ready
   float *dmg_phi = nullptr, *dmg_Z = nullptr;
   float *en_buf = nullptr;     // nlm_fd_energies: 4 n floats
   double *en_fext = nullptr;   // external force at the current time, S n doubles
@@ -555,6 +573,11 @@ struct nlm_fd {
     if (ev_times) cudaEventDestroy(ev_times);
     for (void *p : allocs) cudaFree(p);
     for (auto e : ev_pool) cudaEventDestroy(e);
+    if (pipe_sin) cudaStreamSynchronize(pipe_sin);
+    if (pipe_sout) cudaStreamSynchronize(pipe_sout);
+    for (auto e : pipe_ev) cudaEventDestroy(e);
+    if (pipe_sin) cudaStreamDestroy(pipe_sin);
+    if (pipe_sout) cudaStreamDestroy(pipe_sout);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -778,6 +801,7 @@ int build_tiles(nlm_fd *h, const int64_t *sell_ptr_dev) {
   std::vector<std::vector<int>> halo(nt);
   std::vector<uint16_t> lidx(h->sell_entries + 4, 0);
   std::vector<int> too_big(1, 0);
+  std::vector<int> need(nt, -1);
   unsigned nthr = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
   auto work = [&](unsigned w) {
     for (int64_t t = w; t < nt; t += nthr) {
@@ -791,6 +815,10 @@ int build_tiles(nlm_fd *h, const int64_t *sell_ptr_dev) {
         too_big[0] = 1;
         continue;
       }
+      int m = -1;
+      for (int64_t i = a; i < b; i++) m = std::max(m, h->perm[i]);
+      for (int j : hl) m = std::max(m, h->perm[j]);
+      need[t] = m;
       for (int64_t i = a; i < b; i++) {
         const int64_t base = sptr[i >> 5] + 4 * (i & 31);
         const int64_t len = rp[i + 1] - rp[i];
@@ -832,6 +860,7 @@ int build_tiles(nlm_fd *h, const int64_t *sell_ptr_dev) {
   h->D.tile_hptr = d_hp;
   h->D.tile_halo = d_h;
   h->tile_ok = true;
+  h->tile_need = std::move(need);
   return NLM_OK;
 }
 
@@ -1965,6 +1994,223 @@ bool in_place_ok(const void *p, size_t bytes) {
   return size > 0 && q >= start && q + bytes <= start + size;
 }
 
+// Caller -> internal node ids, built on first use.
+int ensure_iperm(nlm_fd *h) {
+  if (h->iperm) return NLM_OK;
+  if (h->alloc(&h->iperm, h->n) != cudaSuccess) return fail(NLM_ERR_OOM, "host I/O index");
+  k_invert_perm<<<nblk(h->n, 256), 256, 0, h->stream>>>(h->n, h->D.perm_dev, h->iperm);
+  NLM_CUDA(cudaGetLastError());
+  return NLM_OK;
+}
+
+// Banded host step: at least kPipeMinNodes nodes.  Band sizes ramp 1, 2, 4
+// units up, stay at 8 units (about kPipeMidBand nodes: a few MB per array
+// and copy, where a copy's fixed cost is small) and ramp 4, 2, 1 down, so the
+// first bands arrive and the last go out quickly.
+constexpr int64_t kPipeMinNodes = 1 << 16;
+constexpr int64_t kPipeMidBand = 1 << 18;
+constexpr int64_t kPipeLateDiv = 32;
+
+// The banded step covers one FP32C velocity-Verlet step of a 2-D RNPBond
+// model on a tile decomposition, with no per-launch timing and no timed
+// crack to cut first; other calls take the whole-state path.
+bool pipe_usable(const nlm_fd *h, int64_t nsteps) {
+  return nsteps == 1 && h->pipe_state >= 0 && h->precision == NLM_PREC_FP32C && h->dim == 2 &&
+         h->scheme == NLM_VELOCITY_VERLET && h->material == NLM_MAT_RNP_BOND && h->tile_ok &&
+         (h->decomp == NLM_DECOMP_TILE || h->decomp == NLM_DECOMP_TILE_LOCAL) && !h->timing &&
+         h->n >= kPipeMinNodes && !h->D.qtab &&
+         (h->timed_cracks.empty() || !crack_due(h, 1));
+}
+
+// Band schedule and buffers of the banded step.  Tile t can run once every
+// band up to the one holding caller node tile_need[t] is on the device: its
+// stage is that band.  A node is final after the stage of its tile.  Band b
+// goes out after the first stage k >= b by which all but at most
+// (its size) / kPipeLateDiv of its nodes are final;
+// those late nodes (tiles that straddle a jump of the Morton order, mostly)
+// are written into the caller's arrays directly once every band is out.
+int pipe_setup(nlm_fd *h) {
+  const int64_t n = h->n, nt = (n + kTileNodes - 1) / kTileNodes;
+  if ((int64_t)h->tile_need.size() != nt) {
+    h->pipe_state = -1;
+    return NLM_OK;
+  }
+  const int64_t unit = kPipeMidBand / 8;
+  const int64_t mid = std::max<int64_t>(0, (n - 14 * unit + 4 * unit) / (8 * unit));
+  std::vector<int64_t> w = {1, 2, 4};
+  for (int64_t k = 0; k < mid; k++) w.push_back(8);
+  for (int64_t x : {4, 2, 1}) w.push_back(x);
+  int64_t wsum = 0;
+  for (int64_t x : w) wsum += x;
+  const int K = (int)w.size();
+  std::vector<int64_t> bounds(K + 1, 0);
+  for (int b = 0, acc = 0; b < K; b++) {
+    acc += (int)w[b];
+    bounds[b + 1] = b + 1 == K ? n : (int64_t)((double)n * acc / wsum);
+  }
+  auto band_of = [&](int64_t o) {
+    return (int)(std::upper_bound(bounds.begin(), bounds.end(), o) - bounds.begin()) - 1;
+  };
+  std::vector<int> stage(nt);
+  std::vector<int> count(K + 1, 0);
+  for (int64_t t = 0; t < nt; t++) {
+    stage[t] = std::min(K - 1, band_of(std::max(0, h->tile_need[t])));
+    count[stage[t] + 1]++;
+  }
+  for (int k = 0; k < K; k++) count[k + 1] += count[k];
+  h->pipe_toff = count;
+  std::vector<int> tiles(std::max<int64_t>(1, nt));
+  for (int64_t t = 0; t < nt; t++) tiles[count[stage[t]]++] = (int)t;
+  // hist[b K + k]: nodes of band b final after stage k
+  std::vector<int64_t> hist((size_t)K * K, 0);
+  std::vector<int> cband(n);
+  for (int64_t i = 0; i < n; i++) {
+    cband[i] = band_of(h->perm[i]);
+    hist[(size_t)cband[i] * K + stage[i / kTileNodes]]++;
+  }
+  std::vector<int> release(K, K - 1);
+  for (int b = 0; b < K; b++) {
+    const int64_t cap = (bounds[b + 1] - bounds[b]) / kPipeLateDiv;
+    int64_t later = 0;
+    for (int k = K - 1; k >= b; k--) {
+      if (later + hist[(size_t)b * K + k] > cap) {
+        release[b] = k;
+        break;
+      }
+      later += hist[(size_t)b * K + k];
+      release[b] = k - 1;
+    }
+    release[b] = std::max(release[b], b);
+  }
+  h->pipe_out.assign(K, {});
+  for (int b = 0; b < K; b++) h->pipe_out[release[b]].push_back(b);
+  std::vector<int> late;
+  for (int64_t i = 0; i < n; i++)
+    if (stage[i / kTileNodes] > release[cband[i]]) late.push_back(h->perm[i]);
+  std::sort(late.begin(), late.end());
+  h->pipe_nlate = (int64_t)late.size();
+  if (int rc = ensure_iperm(h)) return rc;
+  const size_t nbits = (size_t)h->P.nwords * h->P.npad;
+  if (h->alloc(&h->pipe_tiles, tiles.size()) != cudaSuccess ||
+      h->alloc(&h->pipe_in, (size_t)9 * n) != cudaSuccess ||
+      h->alloc(&h->pipe_back, (size_t)9 * n) != cudaSuccess ||
+      h->alloc(&h->pipe_ua, n) != cudaSuccess || h->alloc(&h->pipe_ub, n) != cudaSuccess ||
+      h->alloc(&h->pipe_v, n) != cudaSuccess || h->alloc(&h->pipe_f, n) != cudaSuccess ||
+      h->alloc(&h->pipe_bits, nbits) != cudaSuccess ||
+      h->alloc(&h->pipe_late, std::max<size_t>(1, late.size())) != cudaSuccess)
+    return fail(NLM_ERR_OOM, "banded host step buffers");
+  NLM_CUDA(cudaMemcpyAsync(h->pipe_tiles, tiles.data(), sizeof(int) * tiles.size(),
+                           cudaMemcpyHostToDevice, h->stream));
+  if (!late.empty())
+    NLM_CUDA(cudaMemcpyAsync(h->pipe_late, late.data(), sizeof(int) * late.size(),
+                             cudaMemcpyHostToDevice, h->stream));
+  NLM_CUDA(cudaStreamSynchronize(h->stream));
+  NLM_CUDA(cudaStreamCreateWithFlags(&h->pipe_sin, cudaStreamNonBlocking));
+  NLM_CUDA(cudaStreamCreateWithFlags(&h->pipe_sout, cudaStreamNonBlocking));
+  for (int k = 0; k < 2 * K + 1; k++) {
+    cudaEvent_t e;
+    NLM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    h->pipe_ev.push_back(e);
+  }
+  h->pipe_nbands = K;
+  h->pipe_bounds = bounds;
+  h->pipe_state = 1;
+  return NLM_OK;
+}
+
+// One step of nlm_fd_step_host on page-locked arrays, banded: the copy-in of
+// later bands, the step of the tiles they release and the copy-out of
+// finished bands overlap, so both directions of the host link carry traffic
+// at once.  The step writes scratch arrays; they become the state only if
+// every input value was finite.  Otherwise the bond bits are put back, the
+// caller's arrays are restored from the staged input and the call fails with
+// the model unchanged.
+int step_host_banded(nlm_fd *h, double *u, double *v, double *f) {
+  const int64_t n = h->n;
+  const int K = h->pipe_nbands;
+  const std::vector<int64_t> &bd = h->pipe_bounds;
+  cudaStream_t s = h->stream, si = h->pipe_sin, so = h->pipe_sout;
+  const double tm = h->time + h->dt;
+  const int c = 1 - h->cur;  // ping index of u at the step's time
+  DevPtrs Dp = h->D;
+  Dp.u32[c] = h->pipe_ua;
+  Dp.u32[1 - c] = h->pipe_ub;
+  Dp.v32[0] = h->pipe_v;
+  Dp.f32 = reinterpret_cast<float *>(h->pipe_f);
+  double *in_u = h->pipe_in, *in_v = in_u + 3 * n, *in_f = in_v + 3 * n;
+  double *bk_u = h->pipe_back, *bk_v = bk_u + 3 * n, *bk_f = bk_v + 3 * n;
+  double *host[3] = {u, v, f}, *in[3] = {in_u, in_v, in_f}, *bk[3] = {bk_u, bk_v, bk_f};
+  const size_t nbits = (size_t)h->P.nwords * h->P.npad;
+  // the input stream starts once earlier work on the handle's stream is done
+  NLM_CUDA(cudaEventRecord(h->pipe_ev[0], s));
+  NLM_CUDA(cudaStreamWaitEvent(si, h->pipe_ev[0], 0));
+  // copy-in of band b, issued one band ahead of the stage that needs it
+  auto copy_in = [&](int b) -> int {
+    const int64_t o0 = bd[b], o1 = bd[b + 1];
+    for (int a = 0; a < 3; a++)
+      NLM_CUDA(cudaMemcpyAsync(in[a] + 3 * o0, host[a] + 3 * o0, sizeof(double) * 3 * (o1 - o0),
+                               cudaMemcpyHostToDevice, si));
+    NLM_CUDA(cudaEventRecord(h->pipe_ev[2 * b], si));
+    return NLM_OK;
+  };
+  for (int b = 0; b < std::min(K, 2); b++)
+    if (int rc = copy_in(b)) return rc;
+  NLM_CUDA(cudaMemsetAsync(h->bad_input, 0, sizeof(int), s));
+  NLM_CUDA(cudaMemcpyAsync(h->pipe_bits, h->D.bits, sizeof(uint32_t) * nbits,
+                           cudaMemcpyDeviceToDevice, s));
+  if (int rc = apply_fbc(h, tm)) return rc;
+  for (int k = 0; k < K; k++) {
+    const int64_t o0 = bd[k], o1 = bd[k + 1];
+    if (k + 2 < K)
+      if (int rc = copy_in(k + 2)) return rc;
+    NLM_CUDA(cudaStreamWaitEvent(s, h->pipe_ev[2 * k], 0));
+    NLM_CUDA(launch_pipe_in32(h->P, Dp, h->T, tm, o0, o1, h->iperm, in_u, in_v, in_f, h->pipe_ua,
+                              h->pipe_v, h->pipe_f, h->bad_input, s));
+    const int nk = h->pipe_toff[k + 1] - h->pipe_toff[k];
+    if (nk > 0) {
+      StepArgs a{c, false, tm, tm + h->dt, nullptr, 0, n, h->pipe_tiles + h->pipe_toff[k], nk};
+      const cudaError_t e = launch_rnp_step_fp32(h->P, Dp, h->T, a, h->decomp, s);
+      if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
+    }
+    for (int b : h->pipe_out[k]) {
+      const int64_t p0 = bd[b], p1 = bd[b + 1];
+      NLM_CUDA(launch_pipe_out32(p0, p1, nullptr, h->iperm, h->pipe_ua, h->pipe_v, h->pipe_f,
+                                 in_u, in_v, bk_u, bk_v, bk_f, s));
+      NLM_CUDA(cudaEventRecord(h->pipe_ev[2 * b + 1], s));
+      NLM_CUDA(cudaStreamWaitEvent(so, h->pipe_ev[2 * b + 1], 0));
+      for (int a = 0; a < 3; a++)
+        NLM_CUDA(cudaMemcpyAsync(host[a] + 3 * p0, bk[a] + 3 * p0, sizeof(double) * 3 * (p1 - p0),
+                                 cudaMemcpyDeviceToHost, so));
+    }
+  }
+  // the late nodes, written into the caller's arrays once every band's copy
+  // (which carried their values from before their tiles ran) has landed
+  if (h->pipe_nlate > 0) {
+    NLM_CUDA(cudaEventRecord(h->pipe_ev[2 * K], so));
+    NLM_CUDA(cudaStreamWaitEvent(s, h->pipe_ev[2 * K], 0));
+    NLM_CUDA(launch_pipe_out32(0, h->pipe_nlate, h->pipe_late, h->iperm, h->pipe_ua, h->pipe_v,
+                               h->pipe_f, in_u, in_v, u, v, f, s));
+  }
+  NLM_CUDA(launch_pipe_commit32(n, (int64_t)nbits, h->bad_input, h->pipe_ua, h->pipe_ub,
+                                h->pipe_v, h->pipe_f, h->D.u32[c], h->D.u32[1 - c], h->D.v32[0],
+                                reinterpret_cast<float2 *>(h->D.f32), h->D.bits, h->pipe_bits, s));
+  int bad = 0;
+  NLM_CUDA(cudaMemcpyAsync(&bad, h->bad_input, sizeof(int), cudaMemcpyDeviceToHost, s));
+  NLM_CUDA(cudaStreamSynchronize(s));
+  NLM_CUDA(cudaStreamSynchronize(so));
+  if (bad) {
+    for (int a = 0; a < 3; a++)
+      NLM_CUDA(cudaMemcpyAsync(host[a], in[a], sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+    NLM_CUDA(cudaStreamSynchronize(s));
+    return fail(NLM_ERR_NONFINITE, "non-finite state");
+  }
+  h->cur = c;
+  h->time = tm;
+  h->step++;
+  h->host_io = 2;
+  return NLM_OK;
+}
+
 // nlm_fd_step_host with u, v, f read and written in place by kernels (one
 // pass each way over the host link), the state replaced only once the input
 // is known to be finite.
@@ -1973,14 +2219,12 @@ int step_host_in_place(nlm_fd *h, double *u, double *v, double *f, int64_t nstep
   const int S = h->S;
   cudaStream_t s = h->stream;
   const bool fp32 = h->precision == NLM_PREC_FP32C;
-  if (!h->iperm) {
-    if (h->alloc(&h->iperm, n) != cudaSuccess ||
-        h->alloc(&h->zstage, (size_t)24 * S * n + 16 * n) != cudaSuccess)
+  if (int rc = ensure_iperm(h)) return rc;
+  if (!h->zstage) {
+    if (h->alloc(&h->zstage, (size_t)24 * S * n + 16 * n) != cudaSuccess)
       return fail(NLM_ERR_OOM, "in-place host I/O buffers");
     // padding entries of the staged layouts are never written: zero them once
     NLM_CUDA(cudaMemsetAsync(h->zstage, 0, (size_t)24 * S * n + 16 * n, s));
-    k_invert_perm<<<nblk(n, 256), 256, 0, s>>>(n, h->D.perm_dev, h->iperm);
-    NLM_CUDA(cudaGetLastError());
   }
   const size_t bu = fp32 ? sizeof(float4) * (S / 2) * n : sizeof(double) * S * n;
   const size_t bf = fp32 ? sizeof(float) * S * n : sizeof(double) * S * n;
@@ -2052,8 +2296,14 @@ int nlm_fd_step_host(nlm_fd *h, double *u, double *v, double *f, int64_t nsteps)
   // in place: page-locked arrays on 16-byte boundaries holding an even
   // number of doubles (whole 16-byte pairs)
   const bool aligned = ((uintptr_t)u | (uintptr_t)v | (uintptr_t)f) % 16 == 0 && n % 2 == 0;
-  if (aligned && in_place_ok(u, bytes) && in_place_ok(v, bytes) && in_place_ok(f, bytes))
+  if (aligned && in_place_ok(u, bytes) && in_place_ok(v, bytes) && in_place_ok(f, bytes)) {
+    if (pipe_usable(h, nsteps)) {
+      if (h->pipe_state == 0)
+        if (int rc = pipe_setup(h)) return rc;
+      if (h->pipe_state == 1) return step_host_banded(h, u, v, f);
+    }
     return step_host_in_place(h, u, v, f, nsteps);
+  }
   h->host_io = 0;
   cudaStream_t s = h->stream;
   const int *P = h->D.perm_dev;

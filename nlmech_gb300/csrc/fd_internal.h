@@ -68,6 +68,10 @@ struct StepArgs {
   double t_next;  // t_{m+1}
   const double *tdev;  // if set: t_m = tdev[0], t_{m+1} = tdev[1] (graph replay)
   int64_t i0, i1;      // node range of this launch (FP32C RNP kernels)
+  // tile decompositions: if set, the launch runs the ntiles tiles listed
+  // (device array) instead of every tile
+  const int *tiles;
+  int64_t ntiles;
 };
 
 // Launchers (return cudaError_t of the launch).
@@ -85,6 +89,20 @@ cudaError_t launch_drift(const StepParams &P, const DevPtrs &D, const BCTable &T
                          double t_next, bool fp32, cudaStream_t s);
 cudaError_t launch_drift32(const StepParams &P, const DevPtrs &D, const BCTable &T, int cur,
                            double t_next, cudaStream_t s);
+// Banded host step (FP32C, 2-D velocity Verlet): caller-order bands in and
+// out of staged copies of the caller's arrays, and the final commit.
+cudaError_t launch_pipe_in32(const StepParams &P, const DevPtrs &D, const BCTable &T,
+                             double t_next, int64_t o0, int64_t o1, const int *iperm,
+                             const double *hu, const double *hv, const double *hf, float4 *ua,
+                             float4 *sv, float2 *sf, int *bad, cudaStream_t s);
+cudaError_t launch_pipe_out32(int64_t o0, int64_t o1, const int *list, const int *iperm,
+                              const float4 *ua, const float4 *sv, const float2 *sf,
+                              const double *hu_in, const double *hv_in, double *ou, double *ov,
+                              double *of, cudaStream_t s);
+cudaError_t launch_pipe_commit32(int64_t n, int64_t nbits, const int *bad, const float4 *ua,
+                                 const float4 *ub, const float4 *sv, const float2 *sf,
+                                 float4 *u_now, float4 *u_next, float4 *v, float2 *f,
+                                 uint32_t *bits, const uint32_t *bits_saved, cudaStream_t s);
 cudaError_t launch_es_setup(const StepParams &P, const DevPtrs &D, double *mw, cudaStream_t s);
 cudaError_t launch_damage(const StepParams &P, const DevPtrs &D, int cur, bool fp32,
                           bool es, float *phi, float *Z, cudaStream_t s);

@@ -166,8 +166,10 @@ class FDModel:
                                        C.cast(f_ptr, P), C.c_int64(int(nsteps))))
 
     def host_io(self):
-        """1 if the last step_host read and wrote the arrays in place
-        (page-locked buffers), 0 if it copied them."""
+        """How the last step_host moved the arrays: 0 copies (pageable
+        arrays), 1 read and written in place by kernels (page-locked), 2 in
+        caller-order bands overlapped with the step (page-locked, one FP32C
+        2-D step on a tile decomposition)."""
         m = C.c_int()
         _check(load().nlm_fd_host_io(self.h, C.byref(m)))
         return m.value

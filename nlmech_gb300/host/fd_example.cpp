@@ -54,7 +54,7 @@ static int quasi_static() {
     double umax = 0.;
     for (const auto &p : model.displacement())
       umax = std::fmax(umax, std::sqrt(p.x * p.x + p.y * p.y + p.z * p.z));
-    std::printf("qs newton %d residual %.6e umax %.6e\n", it, res, umax);
+    std::printf("qs newton %d residual %.6e umax %.17e\n", it, res, umax);
   } catch (const nlm::Error &e) {
     std::fprintf(stderr, "%s\n", e.what());
     return 1;

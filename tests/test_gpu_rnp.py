@@ -428,3 +428,72 @@ def test_step_host_in_place_matches_copies(gpu):
         with pytest.raises(gpu.NLMError):
             b.step_host_ptr(*ptrs, nsteps=1)
         assert b.time() == t0 and np.array_equal(b.state()[0], u0)
+
+
+def _pinned_state(torch, n):
+    pin = [torch.zeros((n, 3), dtype=torch.float64).pin_memory() for _ in range(3)]
+    pin[0].numpy()[:, 2] = 7.0
+    pin[1].numpy()[:, 2] = -3.0
+    return pin, [t.data_ptr() for t in pin]
+
+
+@pytest.mark.parametrize("nx", [300, 800])
+def test_step_host_banded_matches_copies(gpu, nx):
+    """Page-locked arrays of a large 2-D FP32C model on a tile decomposition
+    move in caller-order bands whose copies overlap the step (host_io 2: six
+    bands at 300 x 300, seven at 800 x 800, with late nodes where tiles
+    straddle a jump of the Morton order).  Arrays, state and bond bits
+    match the copy path bit for bit, through breaking at the loaded edges."""
+    torch = pytest.importorskip("torch")
+    p = configs.rnp_plate(nx, 1e-4, 3, 0.2 * nx * 1e-4, 50.0, 2e-9, 50, seed=4)
+    n = p.n
+    a = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_TILE_LOCAL)
+    b = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_TILE_LOCAL)
+    host = [np.zeros((n, 3)) for _ in range(3)]
+    host[0][:, 2] = 7.0
+    host[1][:, 2] = -3.0
+    pin, ptrs = _pinned_state(torch, n)
+    for k in range(13):
+        a.step_host(*host, nsteps=1)
+        b.step_host_ptr(*ptrs, nsteps=1)
+        if k > 0:
+            assert a.host_io() == 0 and b.host_io() == 2
+    assert a.time() == b.time()
+    for x, y in zip(host, pin):
+        assert np.array_equal(x, y.numpy())
+    assert a.count_broken() > 0
+    assert np.array_equal(a.bond_state(), b.bond_state())
+    for x, y in zip(a.state(), b.state()):
+        assert np.array_equal(x, y)
+    a.run(3)
+    b.run(3)
+    assert np.array_equal(a.state()[0], b.state()[0])
+
+
+def test_step_host_banded_rejects_nonfinite(gpu):
+    """A non-finite value in the last band is found after earlier bands were
+    already written back: the call fails, the model (time, state, bond bits)
+    is unchanged and the caller's arrays hold their input again."""
+    torch = pytest.importorskip("torch")
+    p = configs.rnp_plate(300, 1e-4, 3, 0.006, 50.0, 2e-9, 50, seed=4)
+    n = p.n
+    m = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_TILE_LOCAL)
+    pin, ptrs = _pinned_state(torch, n)
+    for _ in range(6):
+        m.step_host_ptr(*ptrs, nsteps=1)
+    assert m.host_io() == 2 and m.count_broken() > 0
+    t0, st0, bonds0 = m.time(), m.state(), m.bond_state()
+    pin[1].numpy()[n - 5, 0] = np.inf
+    keep = [t.numpy().copy() for t in pin]
+    with pytest.raises(gpu.NLMError):
+        m.step_host_ptr(*ptrs, nsteps=1)
+    assert m.time() == t0
+    for x, y in zip(m.state(), st0):
+        assert np.array_equal(x, y)
+    assert np.array_equal(m.bond_state(), bonds0)
+    for t, k in zip(pin, keep):
+        assert np.array_equal(t.numpy(), k)
+    # with the value put back the run continues
+    pin[1].numpy()[n - 5, 0] = st0[1][n - 5, 0]
+    m.step_host_ptr(*ptrs, nsteps=1)
+    assert m.time() > t0

@@ -90,6 +90,30 @@ __device__ __forceinline__ void es_ext32(const float X[3], const float et[3], fl
   e = fmaf(2.f, xe, ee) / (Yl + Xl);
 }
 
+// es_ext32 for the tile kernels: the same quantities with the division by
+// |Y| + |X| done by the hardware reciprocal (relative error ~1 ulp) and 1/|Y|
+// returned from the square-root step, so no bond takes an IEEE division.
+template <int DIM>
+__device__ __forceinline__ void es_ext32_fast(const float X[3], const float et[3], float Y[3],
+                                              float &Xl, float &iY, float &e) {
+  float x2 = X[0] * X[0] + X[1] * X[1];
+  float xe = X[0] * et[0] + X[1] * et[1];
+  float ee = et[0] * et[0] + et[1] * et[1];
+  if (DIM == 3) {
+    x2 = fmaf(X[2], X[2], x2);
+    xe = fmaf(X[2], et[2], xe);
+    ee = fmaf(et[2], et[2], ee);
+  }
+  for (int c = 0; c < 3; c++) Y[c] = X[c] + et[c];
+  float y2 = Y[0] * Y[0] + Y[1] * Y[1];
+  if (DIM == 3) y2 = fmaf(Y[2], Y[2], y2);
+  x2 = fmaxf(x2, 1e-30f);
+  y2 = fmaxf(y2, 1e-30f);
+  iY = rsqrt_approx(y2);
+  Xl = x2 * rsqrt_approx(x2);
+  e = fmaf(2.f, xe, ee) * rcp_approx(fmaf(y2, iY, Xl));
+}
+
 template <int DIM>
 __global__ void __launch_bounds__(128)
     k_es_dil32(const StepParams P, const Params32 Q, const ESConst32 E, const DevPtrs D,
@@ -168,6 +192,205 @@ __global__ void __launch_bounds__(128)
   integrate_node32<DIM, SCHEME>(P, Q, D, T, A, i, fl, uih, uil, fi);
 }
 
+// ---- tile-frame variants (NLM_DECOMP_TILE_LOCAL) ---------------------------
+// A block takes one tile of kTileNodes consecutive nodes.  It stages the
+// tile's nodes and their halo in shared memory, one record per node: the
+// reference position and the displacement relative to the tile's first node
+// o (each difference formed from the split values, then rounded once to
+// FP32), the volume, and in the force pass the node's force-state
+// coefficients (a, b).  A bond then reads its neighbour's record through
+// the bond's 16-bit index into the staged list (tile_lidx), not by a global
+// gather: X = x_j - x_i and eta = u_j - u_i are differences of two staged
+// values.  Per bond the arithmetic is that of k_es_dil32 / k_es_force32.
+template <int DIM>
+__device__ __forceinline__ void es_stage32(const Params32 &Q, const DevPtrs &D,
+                                           const float4 *ucur, int64_t g, const Node32<DIM> &no,
+                                           const float uoh[3], const float uol[3], float4 &sx,
+                                           float4 &su) {
+  Node32<DIM> ng;
+  ld_pos<DIM>(D, g, ng);
+  float uh[3], ul[3], X[3], et[3];
+  ld_pair<DIM>(ucur, g, uh, ul);
+  es_vec32<DIM>(Q, no, uoh, uol, ng, uh, ul, X, et);
+  sx = make_float4(X[0], X[1], X[2], ng.vol);
+  su = make_float4(et[0], et[1], et[2], 0.f);
+}
+
+template <int DIM, bool FORCE>
+__device__ __forceinline__ int es_stage_tile(const Params32 &Q, const DevPtrs &D,
+                                             const float4 *ucur, int64_t t0, int nt, float4 *s_x,
+                                             float4 *s_u, float *s_b, int tb) {
+  const int h0 = D.tile_hptr[tb];
+  const int nh = D.tile_hptr[tb + 1] - h0;
+  Node32<DIM> no;
+  ld_pos<DIM>(D, t0, no);
+  float uoh[3], uol[3];
+  ld_pair<DIM>(ucur, t0, uoh, uol);
+  for (int e = threadIdx.x; e < kTileNodes + nh; e += blockDim.x) {
+    if (e < kTileNodes && e >= nt) continue;
+    const int64_t g = e < kTileNodes ? t0 + e : (int64_t)D.tile_halo[h0 + e - kTileNodes];
+    float4 sx, su;
+    es_stage32<DIM>(Q, D, ucur, g, no, uoh, uol, sx, su);
+    if (FORCE) {
+      const float2 ab = __ldg(D.es_ab + g);
+      su.w = ab.x;
+      s_b[e] = ab.y;
+    }
+    s_x[e] = sx;
+    s_u[e] = su;
+  }
+  return nh;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kTileNodes)
+    k_es_dil32_tile(const StepParams P, const Params32 Q, const ESConst32 E, const DevPtrs D,
+                    const StepArgs A) {
+  extern __shared__ float4 es_sm[];
+  float4 *s_x = es_sm, *s_u = es_sm + D.tile_nmax;
+  const int tb = blockIdx.x;
+  const int64_t t0 = (int64_t)tb * kTileNodes;
+  const int nt = (int)min((int64_t)kTileNodes, P.n - t0);
+  es_stage_tile<DIM, false>(Q, D, D.u32[A.cur], t0, nt, s_x, s_u, nullptr, tb);
+  __syncthreads();
+  const int il = threadIdx.x;
+  if (il >= nt) return;
+  const int64_t i = t0 + il;
+  const float4 xi = s_x[il], ui = s_u[il];
+  const int len = D.rowlen[i];
+  const uint2 *lp = reinterpret_cast<const uint2 *>(D.tile_lidx + D.sell_ptr[i >> 5]) + (i & 31);
+  float th = 0.f;
+  uint32_t word = 0, nw = 0;
+  auto bond = [&](int k, int jl) {
+    const float4 xj = s_x[jl], uj = s_u[jl];
+    float X[3] = {xj.x - xi.x, xj.y - xi.y, xj.z - xi.z};
+    float et[3] = {uj.x - ui.x, uj.y - ui.y, uj.z - ui.z};
+    float Y[3], Xl, iY, e;
+    es_ext32_fast<DIM>(X, et, Y, Xl, iY, e);
+    const bool was = (word >> (k & 31)) & 1u;
+    const bool fs = was || e > E.sc_eff * Xl;
+    nw |= (uint32_t)(fs && !was) << (k & 31);
+    const float om = fminf(1.f, (E.check_up - Xl) * E.inv_h);
+    th += fs ? 0.f : Xl * e * om * xj.w;
+  };
+  auto group = [&](int g) {
+    if ((g & 7) == 0) {
+      if (nw) D.bits[(int64_t)((g >> 3) - 1) * P.npad + i] = word | nw;
+      word = D.bits[(int64_t)(g >> 3) * P.npad + i];
+      nw = 0;
+    }
+    return __ldg(lp + 32 * g);
+  };
+  // whole groups of four bonds, then the row's remainder
+  const int full = len >> 2;
+  for (int g = 0; g < full; g++) {
+    const uint2 c = group(g);
+    bond(4 * g, (int)(c.x & 0xffffu));
+    bond(4 * g + 1, (int)(c.x >> 16));
+    bond(4 * g + 2, (int)(c.y & 0xffffu));
+    bond(4 * g + 3, (int)(c.y >> 16));
+  }
+  if (len & 3) {
+    const uint2 c = group(full);
+    const int jl[3] = {(int)(c.x & 0xffffu), (int)(c.x >> 16), (int)(c.y & 0xffffu)};
+    for (int q = 0; q < (len & 3); q++) bond(4 * full + q, jl[q]);
+  }
+  if (nw) D.bits[(int64_t)((len - 1) >> 5) * P.npad + i] = word | nw;
+  const float minv = (float)(1.0 / D.mw64[i]);
+  const float theta = E.cfac * minv * th;
+  D.es_ab[i] = make_float2(E.ka * theta * minv, E.kb * minv);
+}
+
+template <int DIM, int SCHEME>
+__global__ void __launch_bounds__(kTileNodes)
+    k_es_force32_tile(const StepParams P, const Params32 Q, const ESConst32 E, const DevPtrs D,
+                      const BCTable T, const StepArgs A) {
+  extern __shared__ float4 es_sm[];
+  float4 *s_x = es_sm, *s_u = es_sm + D.tile_nmax;
+  float *s_b = reinterpret_cast<float *>(es_sm + 2 * D.tile_nmax);
+  const int tb = blockIdx.x;
+  const int64_t t0 = (int64_t)tb * kTileNodes;
+  const int nt = (int)min((int64_t)kTileNodes, P.n - t0);
+  const float4 *ucur = D.u32[A.cur];
+  es_stage_tile<DIM, true>(Q, D, ucur, t0, nt, s_x, s_u, s_b, tb);
+  __syncthreads();
+  const int il = threadIdx.x;
+  if (il >= nt) return;
+  const int64_t i = t0 + il;
+  const float4 xi = s_x[il], ui = s_u[il];
+  const float ai = ui.w, bi = s_b[il];
+  float uih[3], uil[3];
+  ld_pair<DIM>(ucur, i, uih, uil);
+  const uint8_t fl = D.flags[i];
+  const int len = D.rowlen[i];
+  const uint2 *lp = reinterpret_cast<const uint2 *>(D.tile_lidx + D.sell_ptr[i >> 5]) + (i & 31);
+  float fi[3] = {0.f, 0.f, 0.f};
+  uint32_t word = 0;
+  auto bond = [&](int k, int jl) {
+    const float4 xj = s_x[jl], uj = s_u[jl];
+    float X[3] = {xj.x - xi.x, xj.y - xi.y, xj.z - xi.z};
+    float et[3] = {uj.x - ui.x, uj.y - ui.y, uj.z - ui.z};
+    float Y[3], Xl, iY, e;
+    es_ext32_fast<DIM>(X, et, Y, Xl, iY, e);
+    const float tsum = (ai + uj.w) * Xl + (bi + s_b[jl]) * e;
+    const float om = fminf(1.f, (E.check_up - Xl) * E.inv_h);
+    // a broken bond carries no force
+    const float s = ((word >> (k & 31)) & 1u) ? 0.f : tsum * om * xj.w * iY;
+    fi[0] = fmaf(s, Y[0], fi[0]);
+    fi[1] = fmaf(s, Y[1], fi[1]);
+    if (DIM == 3) fi[2] = fmaf(s, Y[2], fi[2]);
+  };
+  auto group = [&](int g) {
+    if ((g & 7) == 0) word = D.bits[(int64_t)(g >> 3) * P.npad + i];
+    return __ldg(lp + 32 * g);
+  };
+  const int full = len >> 2;
+  for (int g = 0; g < full; g++) {
+    const uint2 c = group(g);
+    bond(4 * g, (int)(c.x & 0xffffu));
+    bond(4 * g + 1, (int)(c.x >> 16));
+    bond(4 * g + 2, (int)(c.y & 0xffffu));
+    bond(4 * g + 3, (int)(c.y >> 16));
+  }
+  if (len & 3) {
+    const uint2 c = group(full);
+    const int jl[3] = {(int)(c.x & 0xffffu), (int)(c.x >> 16), (int)(c.y & 0xffffu)};
+    for (int q = 0; q < (len & 3); q++) bond(4 * full + q, jl[q]);
+  }
+  integrate_node32<DIM, SCHEME>(P, Q, D, T, A, i, fl, uih, uil, fi);
+}
+
+// Above 48 KB a kernel's dynamic shared memory must be opted into; each
+// kernel is opted in once, for the largest staged list any tile store holds.
+template <class K>
+static void es_tile_smem(K kernel, bool &done) {
+  if (done) return;
+  const size_t most = (2 * sizeof(float4) + sizeof(float)) * kTileMaxLocalES;
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
+  done = true;
+}
+
+template <int DIM>
+static cudaError_t es32_tile(const StepParams &P, const DevPtrs &D, const BCTable &T,
+                             const StepArgs &a, cudaStream_t s) {
+  const Params32 Q = make_p32(P);
+  const ESConst32 E = make_es32(P);
+  const unsigned g = (unsigned)((P.n + kTileNodes - 1) / kTileNodes);
+  const size_t b1 = sizeof(float4) * 2 * D.tile_nmax;
+  const size_t b2 = b1 + sizeof(float) * D.tile_nmax;
+  static bool opt_d = false, opt_v = false, opt_c = false;
+  es_tile_smem(k_es_dil32_tile<DIM>, opt_d);
+  k_es_dil32_tile<DIM><<<g, kTileNodes, b1, s>>>(P, Q, E, D, a);
+  if (P.scheme == NLM_VELOCITY_VERLET) {
+    es_tile_smem(k_es_force32_tile<DIM, NLM_VELOCITY_VERLET>, opt_v);
+    k_es_force32_tile<DIM, NLM_VELOCITY_VERLET><<<g, kTileNodes, b2, s>>>(P, Q, E, D, T, a);
+  } else {
+    es_tile_smem(k_es_force32_tile<DIM, NLM_CENTRAL_DIFFERENCE>, opt_c);
+    k_es_force32_tile<DIM, NLM_CENTRAL_DIFFERENCE><<<g, kTileNodes, b2, s>>>(P, Q, E, D, T, a);
+  }
+  return cudaGetLastError();
+}
+
 template <int DIM>
 static cudaError_t es32(const StepParams &P, const DevPtrs &D, const BCTable &T,
                         const StepArgs &a, cudaStream_t s) {
@@ -184,8 +407,9 @@ static cudaError_t es32(const StepParams &P, const DevPtrs &D, const BCTable &T,
 
 cudaError_t launch_es_step_fp32(const StepParams &P, const DevPtrs &D, const BCTable &T,
                                 const StepArgs &a, int decomp, cudaStream_t s) {
-  (void)decomp;
   if (P.n == 0) return cudaSuccess;
+  if (decomp == NLM_DECOMP_TILE_LOCAL && D.tile_lidx && D.tile_nmax > 0)
+    return P.dim == 2 ? es32_tile<2>(P, D, T, a, s) : es32_tile<3>(P, D, T, a, s);
   return P.dim == 2 ? es32<2>(P, D, T, a, s) : es32<3>(P, D, T, a, s);
 }
 

@@ -788,7 +788,7 @@ int launch_step(nlm_fd *h, const StepArgs &a0) {
 // staged list (tile nodes 0..255, halo from 256), in the sliced layout of
 // sell_cols; padding entries point at the row's own node.  If some tile needs
 // more than kTileMaxLocal staged nodes the store is not built.
-int build_tiles(nlm_fd *h, const int64_t *sell_ptr_dev) {
+int build_tiles(nlm_fd *h, const int64_t *sell_ptr_dev, int max_local) {
   const int64_t n = h->n, nt = (n + kTileNodes - 1) / kTileNodes;
   std::vector<int> cols(h->nnz);
   std::vector<int64_t> sptr(h->nslices + 1);
@@ -811,7 +811,7 @@ int build_tiles(nlm_fd *h, const int64_t *sell_ptr_dev) {
         if (cols[q] < a || cols[q] >= b) hl.push_back(cols[q]);
       std::sort(hl.begin(), hl.end());
       hl.erase(std::unique(hl.begin(), hl.end()), hl.end());
-      if (kTileNodes + (int64_t)hl.size() > kTileMaxLocal) {
+      if (kTileNodes + (int64_t)hl.size() > max_local) {
         too_big[0] = 1;
         continue;
       }
@@ -844,7 +844,11 @@ int build_tiles(nlm_fd *h, const int64_t *sell_ptr_dev) {
     return NLM_OK;
   }
   std::vector<int> hptr(nt + 1, 0);
-  for (int64_t t = 0; t < nt; t++) hptr[t + 1] = hptr[t] + (int)halo[t].size();
+  size_t nmax = 0;
+  for (int64_t t = 0; t < nt; t++) {
+    hptr[t + 1] = hptr[t] + (int)halo[t].size();
+    nmax = std::max(nmax, halo[t].size());
+  }
   std::vector<int> hall(std::max(1, hptr[nt]));
   for (int64_t t = 0; t < nt; t++) std::copy(halo[t].begin(), halo[t].end(), hall.begin() + hptr[t]);
   uint16_t *d_l = nullptr;
@@ -859,6 +863,7 @@ int build_tiles(nlm_fd *h, const int64_t *sell_ptr_dev) {
   h->D.tile_lidx = d_l;
   h->D.tile_hptr = d_hp;
   h->D.tile_halo = d_h;
+  h->D.tile_nmax = kTileNodes + (int)nmax;
   h->tile_ok = true;
   h->tile_need = std::move(need);
   return NLM_OK;
@@ -892,9 +897,14 @@ int autotune(nlm_fd *h) {
   D.v32[1] = sv1;
   D.f32 = sf;
   D.bits = sb;
-  std::vector<int> cands = {NLM_DECOMP_THREAD, NLM_DECOMP_THREAD1, NLM_DECOMP_WARP};
+  const bool rnp = h->material == NLM_MAT_RNP_BOND;
+  std::vector<int> cands = {NLM_DECOMP_THREAD};
+  if (rnp) {
+    cands.push_back(NLM_DECOMP_THREAD1);
+    cands.push_back(NLM_DECOMP_WARP);
+  }
   if (h->tile_ok) {
-    cands.push_back(NLM_DECOMP_TILE);
+    if (rnp) cands.push_back(NLM_DECOMP_TILE);
     cands.push_back(NLM_DECOMP_TILE_LOCAL);
   }
   cudaEvent_t a, b;
@@ -904,9 +914,13 @@ int autotune(nlm_fd *h) {
   int pick = NLM_DECOMP_THREAD;
   StepArgs sa{0, false, h->time, h->time + h->dt, nullptr, 0, h->n};
   for (int c : cands) {
-    for (int w = 0; w < 2; w++) e = launch_rnp_step_fp32(h->P, D, h->T, sa, c, s);
+    auto launch = [&]() {
+      return rnp ? launch_rnp_step_fp32(h->P, D, h->T, sa, c, s)
+                 : launch_es_step_fp32(h->P, D, h->T, sa, c, s);
+    };
+    for (int w = 0; w < 2; w++) e = launch();
     cudaEventRecord(a, s);
-    for (int r = 0; r < 5; r++) e = launch_rnp_step_fp32(h->P, D, h->T, sa, c, s);
+    for (int r = 0; r < 5; r++) e = launch();
     cudaEventRecord(b, s);
     if (e == cudaSuccess) e = cudaEventSynchronize(b);
     float ms = 0.f;
@@ -1213,12 +1227,20 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
       h->decomp != NLM_DECOMP_THREAD1 && h->decomp != NLM_DECOMP_TILE &&
       h->decomp != NLM_DECOMP_TILE_LOCAL)
     return bail(fail(NLM_ERR_INVALID, "unknown decomposition"));
-  const bool tile_able = d->precision == NLM_PREC_FP32C && d->material.kind == NLM_MAT_RNP_BOND &&
-                         d->dim == 2;
+  // tile store: FP32C 2-D RNPBond (both tile kernels) and FP32C 2-D / 3-D
+  // ElasticState (the tile-frame kernels only)
+  const bool es_model = d->material.kind == NLM_MAT_ELASTIC_STATE;
+  const bool tile_able =
+      d->precision == NLM_PREC_FP32C &&
+      ((d->material.kind == NLM_MAT_RNP_BOND && d->dim == 2) || (es_model && d->dim >= 2));
   if ((h->decomp == NLM_DECOMP_TILE || h->decomp == NLM_DECOMP_TILE_LOCAL) && !tile_able)
-    return bail(fail(NLM_ERR_UNSUPPORTED, "the tile decomposition is for FP32C 2-D RNPBond"));
-  const bool want_tune = d->decomposition == NLM_DECOMP_AUTO &&
-                         d->precision == NLM_PREC_FP32C && d->material.kind == NLM_MAT_RNP_BOND;
+    return bail(fail(NLM_ERR_UNSUPPORTED,
+                     "the tile decompositions are for FP32C 2-D RNPBond and 2-D / 3-D "
+                     "ElasticState"));
+  if (h->decomp == NLM_DECOMP_TILE && es_model)
+    return bail(fail(NLM_ERR_UNSUPPORTED, "ElasticState takes NLM_DECOMP_TILE_LOCAL"));
+  const bool want_tune = d->decomposition == NLM_DECOMP_AUTO && d->precision == NLM_PREC_FP32C &&
+                         (d->material.kind == NLM_MAT_RNP_BOND || es_model);
 
   cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
@@ -1277,7 +1299,7 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
   D.bits = bits;
   if (tile_able &&
       (h->decomp == NLM_DECOMP_TILE || h->decomp == NLM_DECOMP_TILE_LOCAL || want_tune)) {
-    int rc_t = build_tiles(h, st.ptr);
+    int rc_t = build_tiles(h, st.ptr, es_model ? kTileMaxLocalES : kTileMaxLocal);
     if (rc_t) return bail(rc_t);
     if ((h->decomp == NLM_DECOMP_TILE || h->decomp == NLM_DECOMP_TILE_LOCAL) && !h->tile_ok)
       return bail(fail(NLM_ERR_UNSUPPORTED, "a tile's halo exceeds the tile store limit"));

@@ -52,6 +52,7 @@ struct DevPtrs {
   const uint16_t *tile_lidx;
   const int *tile_hptr;  // tiles + 1
   const int *tile_halo;
+  int tile_nmax;         // largest staged node list of any tile
 };
 
 // Tile decomposition: kTileNodes consecutive (Morton-ordered) nodes per
@@ -59,6 +60,9 @@ struct DevPtrs {
 // the decomposition for the handle.
 constexpr int kTileNodes = 256;
 constexpr int kTileMaxLocal = 1280;
+// ElasticState tile kernels size their staged lists at run time (dynamic
+// shared memory, 36 bytes per staged node); a larger tile disables them.
+constexpr int kTileMaxLocalES = 3072;
 
 // Which buffers a launch reads/writes.
 struct StepArgs {

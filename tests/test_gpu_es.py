@@ -84,19 +84,52 @@ def test_es2d_fp64_parity(gpu, oracle):
         assert rel_max(u, uo) <= 1e-12 and rel_max(v, vo) <= 1e-12 and rel_max(f, fo) <= 1e-12
 
 
-def test_es3d_fp32c_error(gpu, oracle):
+@pytest.mark.parametrize("decomp", [abi.DECOMP_THREAD, abi.DECOMP_TILE_LOCAL])
+def test_es3d_fp32c_error(gpu, oracle, decomp):
+    """FP32C against the FP64 oracle, thread-per-node kernels and tile-frame
+    kernels (neighbours staged in shared memory), same bar."""
     p = cube(vscale=20.0)
     o = oracle.OracleFD(p)
     o.run(200)
     uo = o.state()[0]
     rowptr, cols = o.neighbors()
     bo = pairs(rowptr, cols, o.bond_state())
-    m = gpu.FDModel(p, precision=abi.FP32C)
+    m = gpu.FDModel(p, precision=abi.FP32C, decomposition=decomp)
+    assert m.decomposition() == decomp
     m.run(200)
     u = m.state()[0]
     assert rel_l2(u, uo) <= 1e-5
     bm = pairs(rowptr, cols, m.bond_state())
     assert len(bm ^ bo) <= 1e-3 * max(len(bo), 1) + 2
+
+
+@pytest.mark.parametrize("decomp", [abi.DECOMP_THREAD, abi.DECOMP_TILE_LOCAL])
+def test_es2d_fp32c_error(gpu, oracle, decomp):
+    p = configs.rnp_plate(36, 1e-3, 3, 0.008, 0.5, 1e-8, 100, seed=4)
+    p.material = configs.MaterialDeck(kind="ElasticState", density=2440.0, K=40e9, G=30e9,
+                                      es_sc=2e-3)
+    m = gpu.FDModel(p, precision=abi.FP32C, decomposition=decomp)
+    o = oracle.OracleFD(p)
+    m.run(100)
+    o.run(100)
+    assert rel_l2(m.state()[0], o.state()[0]) <= 1e-5
+    assert rel_l2(m.state()[1], o.state()[1]) <= 1e-4
+
+
+def test_es3d_fp32c_tile_matches_thread_large(gpu):
+    """40^3 nodes (250 tiles, most of them interior with full halos, some
+    across jumps of the Morton order): the tile-frame kernels follow the
+    thread kernels through breaking."""
+    p = configs.elastic_state_cube(40, 1e-3, sc=5e-4, seed=3)
+    p.v0 = p.v0 * 50.0
+    a = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_THREAD)
+    b = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_TILE_LOCAL)
+    a.run(150)
+    b.run(150)
+    assert a.count_broken() > 0
+    assert abs(a.count_broken() - b.count_broken()) <= 1e-3 * a.count_broken() + 2
+    assert rel_l2(b.state()[0], a.state()[0]) <= 1e-5
+    assert rel_l2(b.state()[1], a.state()[1]) <= 1e-4
 
 
 def test_es_central_difference(gpu, oracle):
@@ -107,3 +140,6 @@ def test_es_central_difference(gpu, oracle):
     m.run(50)
     o.run(50)
     assert rel_max(m.state()[0], o.state()[0]) <= 1e-12
+    t = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_TILE_LOCAL)
+    t.run(50)
+    assert rel_l2(t.state()[0], o.state()[0]) <= 1e-5

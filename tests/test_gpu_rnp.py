@@ -260,6 +260,12 @@ def test_tile_decomposition_rejected_where_unsupported(gpu):
     for dec in (abi.DECOMP_TILE, abi.DECOMP_TILE_LOCAL):
         with pytest.raises(gpu.NLMError):
             gpu.FDModel(p, precision=abi.FP64, decomposition=dec)
+    # ElasticState has the tile-frame kernels only
+    q = configs.elastic_state_cube(8, 1e-3)
+    with pytest.raises(gpu.NLMError):
+        gpu.FDModel(q, precision=abi.FP32C, decomposition=abi.DECOMP_TILE)
+    assert gpu.FDModel(q, precision=abi.FP32C,
+                       decomposition=abi.DECOMP_TILE_LOCAL).decomposition() == abi.DECOMP_TILE_LOCAL
 
 
 def test_checkpoint_restart_continues_the_run(gpu, tmp_path):

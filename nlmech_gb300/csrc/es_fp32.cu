@@ -226,6 +226,8 @@ __device__ __forceinline__ int es_stage_tile(const Params32 &Q, const DevPtrs &D
   ld_pos<DIM>(D, t0, no);
   float uoh[3], uol[3];
   ld_pair<DIM>(ucur, t0, uoh, uol);
+  // unrolled so that several staged nodes' loads are in flight at once
+#pragma unroll 4
   for (int e = threadIdx.x; e < kTileNodes + nh; e += blockDim.x) {
     if (e < kTileNodes && e >= nt) continue;
     const int64_t g = e < kTileNodes ? t0 + e : (int64_t)D.tile_halo[h0 + e - kTileNodes];
@@ -273,13 +275,20 @@ __global__ void __launch_bounds__(kTileNodes)
     const float om = fminf(1.f, (E.check_up - Xl) * E.inv_h);
     th += fs ? 0.f : Xl * e * om * xj.w;
   };
+  // the next group's ids and bit word are loaded one group ahead
+  const int ng = (len + 3) >> 2;
+  uint2 nxt = ng > 0 ? __ldg(lp) : make_uint2(0u, 0u);
+  uint32_t wnext = ng > 0 ? D.bits[i] : 0u;
   auto group = [&](int g) {
     if ((g & 7) == 0) {
       if (nw) D.bits[(int64_t)((g >> 3) - 1) * P.npad + i] = word | nw;
-      word = D.bits[(int64_t)(g >> 3) * P.npad + i];
+      word = wnext;
       nw = 0;
+      if (8 * ((g >> 3) + 1) < ng) wnext = D.bits[(int64_t)((g >> 3) + 1) * P.npad + i];
     }
-    return __ldg(lp + 32 * g);
+    const uint2 c = nxt;
+    if (g + 1 < ng) nxt = __ldg(lp + 32 * (g + 1));
+    return c;
   };
   // whole groups of four bonds, then the row's remainder
   const int full = len >> 2;
@@ -340,9 +349,17 @@ __global__ void __launch_bounds__(kTileNodes)
     fi[1] = fmaf(s, Y[1], fi[1]);
     if (DIM == 3) fi[2] = fmaf(s, Y[2], fi[2]);
   };
+  const int ng = (len + 3) >> 2;
+  uint2 nxt = ng > 0 ? __ldg(lp) : make_uint2(0u, 0u);
+  uint32_t wnext = ng > 0 ? D.bits[i] : 0u;
   auto group = [&](int g) {
-    if ((g & 7) == 0) word = D.bits[(int64_t)(g >> 3) * P.npad + i];
-    return __ldg(lp + 32 * g);
+    if ((g & 7) == 0) {
+      word = wnext;
+      if (8 * ((g >> 3) + 1) < ng) wnext = D.bits[(int64_t)((g >> 3) + 1) * P.npad + i];
+    }
+    const uint2 c = nxt;
+    if (g + 1 < ng) nxt = __ldg(lp + 32 * (g + 1));
+    return c;
   };
   const int full = len >> 2;
   for (int g = 0; g < full; g++) {

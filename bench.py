@@ -427,8 +427,8 @@ def run_ensemble(a):
         ms = b.run_timed(a.steps)
     torch.cuda.synchronize()
     value = nnz * a.steps / (ms * 1e-3)
-    buckets = [{"nodes": int(nd), "decomposition": {1: "thread", 2: "warp", 3: "thread1"}[dc]}
-               for nd, dc in b.buckets()]
+    names = {1: "thread", 2: "warp", 3: "thread1", 5: "tile-frame"}
+    buckets = [{"nodes": int(nd), "decomposition": names.get(dc, dc)} for nd, dc in b.buckets()]
     b.close()
     # sequential single-plate runs (sample), each a separate model
     seq_ms, seq_bonds = 0.0, 0

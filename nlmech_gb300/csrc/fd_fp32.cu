@@ -370,15 +370,21 @@ __global__ void __launch_bounds__(kTileNodes, 3)
 // FP32 rounding of the tile-frame coordinates (~2^-24 of the tile span)
 // instead of ~2^-24 of themselves; the node's own update stays on the
 // (hi, lo) pairs.
-template <int SCHEME, bool NW1, int OPT>
+// BATCH: a batch of specimens in one layout.  A launch covers the tiles that
+// meet its node range [A.i0, A.i1) (a tile may hold nodes of two ranges and
+// of several specimens) and owns only the range's nodes that are not ghosts;
+// each node takes its own specimen's constants.  The staged volume is V, not
+// K1 V: specimens differ in K1, and a bond's two nodes share a specimen.
+template <int SCHEME, bool NW1, int OPT, bool BATCH>
 __global__ void __launch_bounds__(kTileNodes, 4)
     k_rnp32_tilel(const StepParams P, const Params32 Q, const DevPtrs D, const BCTable T,
                   const StepArgs A) {
   __shared__ float4 s_xu[kTileMaxLocal];  // x - x_o, y - y_o, ux - ux_o, uy - uy_o
-  __shared__ float s_vol[kTileMaxLocal];  // K1 V (V with the contact term)
-  constexpr bool KV = !(OPT & OPT_CONTACT);
+  __shared__ float s_vol[kTileMaxLocal];  // K1 V (V with the contact term or in a batch)
+  constexpr bool KV = !(OPT & OPT_CONTACT) && !BATCH;
   __shared__ uint8_t s_fl[(OPT & OPT_NOFAIL) ? kTileMaxLocal : 1];
-  const int tb = A.tiles ? A.tiles[blockIdx.x] : (int)blockIdx.x;
+  const int tb = A.tiles ? A.tiles[blockIdx.x]
+                         : (int)blockIdx.x + (BATCH ? (int)(A.i0 / kTileNodes) : 0);
   const int64_t t0 = (int64_t)tb * kTileNodes;
   const int h0 = D.tile_hptr[tb];
   const int nh = D.tile_hptr[tb + 1] - h0;
@@ -391,8 +397,10 @@ __global__ void __launch_bounds__(kTileNodes, 4)
   // overlaps it
   const int il = threadIdx.x;
   const int64_t i = t0 + il;
-  const bool own = il < nt;
+  bool own = il < nt;
+  if (BATCH) own = own && i >= A.i0 && i < A.i1;
   const uint8_t fl = own ? D.flags[i] : 0;
+  if (BATCH && (fl & FLAG_GHOST)) own = false;
   const int len = own ? D.rowlen[i] : 0;
   const int ng = (len + 3) >> 2;
   const uint2 *lp = reinterpret_cast<const uint2 *>(D.tile_lidx + (own ? D.sell_ptr[i >> 5] : 0)) +
@@ -421,6 +429,7 @@ __global__ void __launch_bounds__(kTileNodes, 4)
   }
   __syncthreads();
   if (!own) return;
+  const Params32 &Qn = BATCH ? static_cast<const Params32 *>(D.qtab)[D.slice_spec[i >> 5]] : Q;
   const float4 xi = s_xu[il];
   const float voli = s_vol[il];  // used by the contact term only (raw V there)
   float uih[3] = {ui4.x, ui4.y, 0.f}, uil[3] = {ui4.z, ui4.w, 0.f};
@@ -452,7 +461,7 @@ __global__ void __launch_bounds__(kTileNodes, 4)
       bool fs = was;
       bool breakable = true;
       if (OPT & OPT_NOFAIL) breakable = brk_i && !(s_fl[jl[q]] & FLAG_NOFAIL);
-      const float sc = rnp_bond32_core<2, OPT, KV>(Q, dv, xj[q].z - xi.z, xj[q].w - xi.w, 0.f,
+      const float sc = rnp_bond32_core<2, OPT, KV>(Qn, dv, xj[q].z - xi.z, xj[q].w - xi.w, 0.f,
                                                    vj[q], voli, breakable, fs);
       nw |= (uint32_t)(fs && !was) << (k & 31);
       fi[0] = fmaf(sc, dv[0], fi[0]);
@@ -460,7 +469,7 @@ __global__ void __launch_bounds__(kTileNodes, 4)
     }
   }
   if (nw) D.bits[NW1 ? i : (int64_t)((len - 1) >> 5) * P.npad + i] = word | nw;
-  integrate_node32<2, SCHEME>(P, Q, D, T, A, i, fl, uih, uil, fi);
+  integrate_node32<2, SCHEME>(P, Qn, D, T, A, i, fl, uih, uil, fi);
 }
 
 template <int DIM, int SCHEME, int OPT, bool BATCH>
@@ -480,14 +489,17 @@ static void launch_opt(const StepParams &P, const Params32 &Q, const DevPtrs &D,
       k_rnp32_tile<SCHEME, false, OPT><<<grid, kTileNodes, 0, s>>>(P, Q, D, T, a);
     return;
   }
-  if (DIM == 2 && !BATCH && decomp == NLM_DECOMP_TILE_LOCAL) {
+  if (DIM == 2 && decomp == NLM_DECOMP_TILE_LOCAL && D.tile_lidx) {
+    // a batch launch covers the tiles that meet its node range
     const unsigned grid =
-        a.tiles ? (unsigned)a.ntiles : (unsigned)((P.n + kTileNodes - 1) / kTileNodes);
+        a.tiles ? (unsigned)a.ntiles
+        : BATCH ? (unsigned)((a.i1 + kTileNodes - 1) / kTileNodes - a.i0 / kTileNodes)
+                : (unsigned)((P.n + kTileNodes - 1) / kTileNodes);
     if (grid == 0) return;
     if (P.nw1)
-      k_rnp32_tilel<SCHEME, true, OPT><<<grid, kTileNodes, 0, s>>>(P, Q, D, T, a);
+      k_rnp32_tilel<SCHEME, true, OPT, BATCH><<<grid, kTileNodes, 0, s>>>(P, Q, D, T, a);
     else
-      k_rnp32_tilel<SCHEME, false, OPT><<<grid, kTileNodes, 0, s>>>(P, Q, D, T, a);
+      k_rnp32_tilel<SCHEME, false, OPT, BATCH><<<grid, kTileNodes, 0, s>>>(P, Q, D, T, a);
     return;
   }
   if (decomp == NLM_DECOMP_WARP) {

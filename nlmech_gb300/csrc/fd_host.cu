@@ -788,18 +788,31 @@ int launch_step(nlm_fd *h, const StepArgs &a0) {
 // staged list (tile nodes 0..255, halo from 256), in the sliced layout of
 // sell_cols; padding entries point at the row's own node.  If some tile needs
 // more than kTileMaxLocal staged nodes the store is not built.
-int build_tiles(nlm_fd *h, const int64_t *sell_ptr_dev, int max_local) {
-  const int64_t n = h->n, nt = (n + kTileNodes - 1) / kTileNodes;
-  std::vector<int> cols(h->nnz);
-  std::vector<int64_t> sptr(h->nslices + 1);
-  NLM_CUDA(cudaMemcpyAsync(cols.data(), h->D.cols, sizeof(int) * h->nnz, cudaMemcpyDeviceToHost,
+// What a tile store is built from (one model or a batch's combined layout).
+struct TileInputs {
+  int64_t n, nnz, nslices, sell_entries;
+  const int *cols_dev;                 // internal column ids, CSR order
+  const int64_t *sell_ptr_dev;         // sliced-store offsets
+  const std::vector<int64_t> *rowptr;  // host CSR offsets
+  const std::vector<int> *perm;        // internal -> caller id (for tile_need), or null
+  int max_local;                       // largest staged list allowed
+};
+
+template <class H>
+int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *need_out) {
+  const int64_t n = in.n, nt = (n + kTileNodes - 1) / kTileNodes;
+  const int max_local = in.max_local;
+  ok = false;
+  std::vector<int> cols(in.nnz);
+  std::vector<int64_t> sptr(in.nslices + 1);
+  NLM_CUDA(cudaMemcpyAsync(cols.data(), in.cols_dev, sizeof(int) * in.nnz, cudaMemcpyDeviceToHost,
                            h->stream));
-  NLM_CUDA(cudaMemcpyAsync(sptr.data(), sell_ptr_dev, sizeof(int64_t) * (h->nslices + 1),
+  NLM_CUDA(cudaMemcpyAsync(sptr.data(), in.sell_ptr_dev, sizeof(int64_t) * (in.nslices + 1),
                            cudaMemcpyDeviceToHost, h->stream));
   NLM_CUDA(cudaStreamSynchronize(h->stream));
-  const std::vector<int64_t> &rp = h->rowptr;
+  const std::vector<int64_t> &rp = *in.rowptr;
   std::vector<std::vector<int>> halo(nt);
-  std::vector<uint16_t> lidx(h->sell_entries + 4, 0);
+  std::vector<uint16_t> lidx(in.sell_entries + 4, 0);
   std::vector<int> too_big(1, 0);
   std::vector<int> need(nt, -1);
   unsigned nthr = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
@@ -815,10 +828,12 @@ int build_tiles(nlm_fd *h, const int64_t *sell_ptr_dev, int max_local) {
         too_big[0] = 1;
         continue;
       }
-      int m = -1;
-      for (int64_t i = a; i < b; i++) m = std::max(m, h->perm[i]);
-      for (int j : hl) m = std::max(m, h->perm[j]);
-      need[t] = m;
+      if (in.perm) {
+        int m = -1;
+        for (int64_t i = a; i < b; i++) m = std::max(m, (*in.perm)[i]);
+        for (int j : hl) m = std::max(m, (*in.perm)[j]);
+        need[t] = m;
+      }
       for (int64_t i = a; i < b; i++) {
         const int64_t base = sptr[i >> 5] + 4 * (i & 31);
         const int64_t len = rp[i + 1] - rp[i];
@@ -839,10 +854,7 @@ int build_tiles(nlm_fd *h, const int64_t *sell_ptr_dev, int max_local) {
   std::vector<std::thread> pool;
   for (unsigned w = 0; w < nthr; w++) pool.emplace_back(work, w);
   for (auto &th : pool) th.join();
-  if (too_big[0]) {
-    h->tile_ok = false;
-    return NLM_OK;
-  }
+  if (too_big[0]) return NLM_OK;
   std::vector<int> hptr(nt + 1, 0);
   size_t nmax = 0;
   for (int64_t t = 0; t < nt; t++) {
@@ -864,9 +876,15 @@ int build_tiles(nlm_fd *h, const int64_t *sell_ptr_dev, int max_local) {
   h->D.tile_hptr = d_hp;
   h->D.tile_halo = d_h;
   h->D.tile_nmax = kTileNodes + (int)nmax;
-  h->tile_ok = true;
-  h->tile_need = std::move(need);
+  ok = true;
+  if (need_out) *need_out = std::move(need);
   return NLM_OK;
+}
+
+int build_tiles(nlm_fd *h, const int64_t *sell_ptr_dev, int max_local) {
+  TileInputs in{h->n, h->nnz, h->nslices, h->sell_entries, h->D.cols, sell_ptr_dev,
+                &h->rowptr, &h->perm, max_local};
+  return build_tile_store(h, in, h->tile_ok, &h->tile_need);
 }
 
 // Work-decomposition autotuner: time each candidate step kernel on scratch
@@ -2439,6 +2457,7 @@ struct nlm_batch {
     int decomp;
   };
   std::vector<Bucket> buckets;
+  bool tile_ok = false;  // tile store over the combined layout (2-D)
   int *bc_nodes = nullptr;
   int64_t n_bc_nodes = 0;
   double *stage = nullptr;
@@ -2739,6 +2758,24 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
   D.sell_ptr = ss.ptr;
   D.sell_w = ss.width;
   D.sell_cols = ss.cols;
+  // explicit decomposition: every specimen names the same one, used for all
+  // buckets; NLM_DECOMP_AUTO (any specimen) autotunes per bucket
+  int fixed = descs[0].decomposition;
+  for (int s = 1; s < nspec; s++)
+    if (descs[s].decomposition != fixed) fixed = NLM_DECOMP_AUTO;
+  if (fixed == NLM_DECOMP_TILE)
+    return bail(fail(NLM_ERR_UNSUPPORTED, "a batch takes NLM_DECOMP_TILE_LOCAL, not TILE"));
+  if (fixed != NLM_DECOMP_AUTO && fixed != NLM_DECOMP_THREAD && fixed != NLM_DECOMP_THREAD1 &&
+      fixed != NLM_DECOMP_WARP && fixed != NLM_DECOMP_TILE_LOCAL)
+    return bail(fail(NLM_ERR_INVALID, "unknown decomposition"));
+  if (b->dim == 2 && (fixed == NLM_DECOMP_AUTO || fixed == NLM_DECOMP_TILE_LOCAL)) {
+    TileInputs tin{N, nnz, ss.nslices, ss.entries, cols, ss.ptr, &b->rowptr, nullptr,
+                   kTileMaxLocal};
+    if (int rc_t = build_tile_store(b, tin, b->tile_ok, nullptr)) return bail(rc_t);
+  }
+  if (fixed == NLM_DECOMP_TILE_LOCAL && !b->tile_ok)
+    return bail(fail(NLM_ERR_UNSUPPORTED,
+                     "the tile-frame decomposition is for 2-D batches whose tiles fit the store"));
   uint32_t *bits;
   BTRY(b->alloc(&bits, (size_t)P.nwords * N));
   BTRY(cudaMemsetAsync(bits, 0, sizeof(uint32_t) * P.nwords * N, st));
@@ -2909,11 +2946,12 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
   for (int q = 0; q < nb; q++) {
     const int kend = (int)(((int64_t)(q + 1) * nspec) / nb);
     const int64_t end = kend < nspec ? b->off[b->order[kend]] : N;
-    if (end > prev) b->buckets.push_back({prev, end, NLM_DECOMP_THREAD});
+    if (end > prev)
+      b->buckets.push_back({prev, end, fixed == NLM_DECOMP_AUTO ? NLM_DECOMP_THREAD : fixed});
     prev = end;
   }
   BTRY(cudaStreamSynchronize(st));
-  {
+  if (fixed == NLM_DECOMP_AUTO) {
     // time each candidate per bucket on scratch velocity / force / bit copies
     DevPtrs Dt = D;
     float4 *sv0 = nullptr;
@@ -2935,7 +2973,9 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
       cudaEventCreate(&eb);
       for (auto &bk : b->buckets) {
         float best = 1e30f;
-        for (int c : {NLM_DECOMP_THREAD, NLM_DECOMP_THREAD1, NLM_DECOMP_WARP}) {
+        std::vector<int> cands = {NLM_DECOMP_THREAD, NLM_DECOMP_THREAD1, NLM_DECOMP_WARP};
+        if (b->tile_ok) cands.push_back(NLM_DECOMP_TILE_LOCAL);
+        for (int c : cands) {
           StepArgs a{0, false, 0., b->dt, nullptr, bk.i0, bk.i1};
           for (int w = 0; w < 2; w++) e2 = launch_rnp_step_fp32(P, Dt, b->T, a, c, st);
           cudaEventRecord(ea, st);

@@ -256,13 +256,16 @@ FDModel.set_graph = _fd_set_graph
 
 
 class Batch:
-    """Many independent RNPBond specimens stepped together (FP32C)."""
+    """Many independent RNPBond specimens stepped together (FP32C).
+    decomposition: None keeps each problem's own (autotuned per node-count
+    bucket unless every problem names the same one); a DECOMP_* value is used
+    for every bucket."""
 
-    def __init__(self, problems, scheme=None):
+    def __init__(self, problems, scheme=None, decomposition=None):
         self.problems = list(problems)
         descs, self._keep = [], []
         for p in self.problems:
-            d, keep = p.desc(precision=abi.FP32C, scheme=scheme)
+            d, keep = p.desc(precision=abi.FP32C, scheme=scheme, decomposition=decomposition)
             descs.append(d)
             self._keep.append(keep)
         arr = (abi.FDDesc * len(descs))(*descs)

@@ -27,9 +27,14 @@ def small_ensemble(n=7, seed=3):
     return configs.ensemble(nplates=n, nmin=600, nmax=3000, seed=seed, steps=300)
 
 
-def test_batch_matches_oracle_per_plate(gpu, oracle):
+@pytest.mark.parametrize("decomp", [None, abi.DECOMP_THREAD, abi.DECOMP_TILE_LOCAL])
+def test_batch_matches_oracle_per_plate(gpu, oracle, decomp):
+    """Autotuned buckets, thread kernels, and tile-frame kernels whose tiles
+    straddle specimens of a few hundred to a few thousand nodes."""
     plates = small_ensemble()
-    b = gpu.Batch(plates)
+    b = gpu.Batch(plates, decomposition=decomp)
+    if decomp is not None:
+        assert all(dc == decomp for _, dc in b.buckets())
     assert b.nnz() == sum(b.nnz(s) for s in range(len(plates)))
     bond0 = [b.bond_state(s) for s in range(len(plates))]
     b.run(300)
@@ -47,11 +52,12 @@ def test_batch_matches_oracle_per_plate(gpu, oracle):
     assert b.time()[1] == 300
 
 
-def test_batch_graph_replay_is_bit_identical(gpu):
+@pytest.mark.parametrize("decomp", [abi.DECOMP_THREAD, abi.DECOMP_TILE_LOCAL])
+def test_batch_graph_replay_is_bit_identical(gpu, decomp):
     plates = small_ensemble(n=5, seed=8)
-    a = gpu.Batch(plates)
+    a = gpu.Batch(plates, decomposition=decomp)
     a.run(101)
-    g = gpu.Batch(plates)
+    g = gpu.Batch(plates, decomposition=decomp)
     g.set_graph(20)
     g.run(101)
     assert a.time() == g.time()

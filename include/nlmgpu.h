@@ -69,11 +69,13 @@ enum nlm_decomposition {
                              four at a time                                */
   NLM_DECOMP_WARP = 2,    /* one warp per node, CSR bond storage           */
   NLM_DECOMP_THREAD1 = 3, /* one thread per node, one bond per iteration   */
-  NLM_DECOMP_TILE = 4,    /* FP32C 2-D: 256-node tiles with their halo staged
-                             in shared memory, 16-bit tile-local bond ids  */
+  NLM_DECOMP_TILE = 4,    /* FP32C 2-D RNPBond: 256-node tiles with their
+                             halo staged in shared memory, 16-bit
+                             tile-local bond ids                           */
   NLM_DECOMP_TILE_LOCAL = 5 /* as TILE with the staged positions and
                              displacements in the tile's frame, one FP32
-                             value per component                          */
+                             value per component: FP32C 2-D RNPBond (also
+                             batched) and FP32C 2-D / 3-D ElasticState     */
 };
 
 /* Displacement_BC / Force_BC region types (loading/uLoading.cpp:38-46). */
@@ -371,7 +373,9 @@ int nlm_fd_set_graph(nlm_fd *h, int steps_per_graph);
  * Many independent specimens (same dimension, dt, scheme and material kind;
  * FP32-compensated RNPBond) in one node space: each step is one launch per
  * node-count bucket over all specimens, each bucket with the decomposition
- * the autotuner picked for it.  Per-specimen constants live in a table in
+ * the autotuner picked for it (THREAD, THREAD1, WARP or, in 2-D,
+ * TILE_LOCAL), or with the one every desc names when all name the same
+ * (NLM_DECOMP_TILE is refused).  Per-specimen constants live in a table in
  * device memory.  Specimen ids below are positions in the descs array. */
 typedef struct nlm_batch nlm_batch;
 

@@ -9,6 +9,8 @@
 // rewritten with e_s = theta |X| / 3), so pass 2 gathers 8 bytes per
 // neighbour for t_ji.
 
+#include <atomic>
+
 #include "fp32_common.cuh"
 
 namespace nlm {
@@ -378,13 +380,18 @@ __global__ void __launch_bounds__(kTileNodes)
 }
 
 // Above 48 KB a kernel's dynamic shared memory must be opted into; each
-// kernel is opted in once, for the largest staged list any tile store holds.
+// kernel is opted in once per device (bit d of done), for the largest staged
+// list any tile store holds.
 template <class K>
-static void es_tile_smem(K kernel, bool &done) {
-  if (done) return;
+static void es_tile_smem(K kernel, std::atomic<uint64_t> &done) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const uint64_t bit = 1ull << (dev & 63);
+  if (done.load() & bit) return;
   const size_t most = (2 * sizeof(float4) + sizeof(float)) * kTileMaxLocalES;
-  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
-  done = true;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most) ==
+      cudaSuccess)
+    done.fetch_or(bit);
 }
 
 template <int DIM>
@@ -395,7 +402,7 @@ static cudaError_t es32_tile(const StepParams &P, const DevPtrs &D, const BCTabl
   const unsigned g = (unsigned)((P.n + kTileNodes - 1) / kTileNodes);
   const size_t b1 = sizeof(float4) * 2 * D.tile_nmax;
   const size_t b2 = b1 + sizeof(float) * D.tile_nmax;
-  static bool opt_d = false, opt_v = false, opt_c = false;
+  static std::atomic<uint64_t> opt_d{0}, opt_v{0}, opt_c{0};
   es_tile_smem(k_es_dil32_tile<DIM>, opt_d);
   k_es_dil32_tile<DIM><<<g, kTileNodes, b1, s>>>(P, Q, E, D, a);
   if (P.scheme == NLM_VELOCITY_VERLET) {

@@ -463,7 +463,8 @@ __global__ void __launch_bounds__(kTileNodes, 4)
       if (OPT & OPT_NOFAIL) breakable = brk_i && !(s_fl[jl[q]] & FLAG_NOFAIL);
       const float sc = rnp_bond32_core<2, OPT, KV>(Qn, dv, xj[q].z - xi.z, xj[q].w - xi.w, 0.f,
                                                    vj[q], voli, breakable, fs);
-      nw |= (uint32_t)(fs && !was) << (k & 31);
+      // a bond broken before keeps its bit: OR-ing it in again changes nothing
+      nw |= (uint32_t)fs << (k & 31);
       fi[0] = fmaf(sc, dv[0], fi[0]);
       fi[1] = fmaf(sc, dv[1], fi[1]);
     }

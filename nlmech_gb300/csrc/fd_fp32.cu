@@ -453,21 +453,24 @@ __global__ void __launch_bounds__(kTileNodes, 4)
       xj[q] = s_xu[jl[q]];
       vj[q] = s_vol[jl[q]];
     }
+    // the group's four state bits, and its four new-break bits
+    const int sh = (4 * g) & 31;
+    const uint32_t w4 = word >> sh;
+    uint32_t n4 = 0;
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-      const int k = 4 * g + q;
       float dv[3] = {xj[q].x - xi.x, xj[q].y - xi.y, 0.f};
-      const bool was = (word >> (k & 31)) & 1u;
-      bool fs = was;
+      bool fs = (w4 >> q) & 1u;
       bool breakable = true;
       if (OPT & OPT_NOFAIL) breakable = brk_i && !(s_fl[jl[q]] & FLAG_NOFAIL);
       const float sc = rnp_bond32_core<2, OPT, KV>(Qn, dv, xj[q].z - xi.z, xj[q].w - xi.w, 0.f,
                                                    vj[q], voli, breakable, fs);
       // a bond broken before keeps its bit: OR-ing it in again changes nothing
-      nw |= (uint32_t)fs << (k & 31);
+      n4 |= fs ? 1u << q : 0u;
       fi[0] = fmaf(sc, dv[0], fi[0]);
       fi[1] = fmaf(sc, dv[1], fi[1]);
     }
+    nw |= n4 << sh;
   }
   if (nw) D.bits[NW1 ? i : (int64_t)((len - 1) >> 5) * P.npad + i] = word | nw;
   integrate_node32<2, SCHEME>(P, Qn, D, T, A, i, fl, uih, uil, fi);

@@ -326,7 +326,8 @@ def run_ours(a):
             mm.close()
 
     # ---- end to end through the host-resident drop-in call ----
-    me = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_AUTO)
+    # the step kernel the device-resident run used (autotuned there, or named)
+    me = gpu.FDModel(p, precision=abi.FP32C, decomposition=dcode)
     bufs = [torch.zeros((n, 3), dtype=torch.float64).pin_memory() for _ in range(3)]
     ptrs = [b.data_ptr() for b in bufs]
     me.step_host_ptr(*ptrs, nsteps=1)  # step 0 + first step (untimed)

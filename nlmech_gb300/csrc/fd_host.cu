@@ -2338,8 +2338,12 @@ int nlm_fd_step_host(nlm_fd *h, double *u, double *v, double *f, int64_t nsteps)
   const bool aligned = ((uintptr_t)u | (uintptr_t)v | (uintptr_t)f) % 16 == 0 && n % 2 == 0;
   if (aligned && in_place_ok(u, bytes) && in_place_ok(v, bytes) && in_place_ok(f, bytes)) {
     if (pipe_usable(h, nsteps)) {
-      if (h->pipe_state == 0)
-        if (int rc = pipe_setup(h)) return rc;
+      // if the banded path cannot be set up (device memory), the in-place
+      // path below serves this and every later call, with the same results
+      if (h->pipe_state == 0 && pipe_setup(h) != NLM_OK) {
+        h->pipe_state = -1;
+        cudaGetLastError();
+      }
       if (h->pipe_state == 1) return step_host_banded(h, u, v, f);
     }
     return step_host_in_place(h, u, v, f, nsteps);

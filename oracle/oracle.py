@@ -271,7 +271,21 @@ class OracleQSR:
 
 
 # ---- the reference's own RNPBond sources (oracle/refshim) -------------------
-REF_TREE = os.environ.get("NLMECH_REFERENCE", "/root/reference")
+def _recipe_reference_tree():
+    """The tree the refshim recipe (refshim/Makefile) compiles from: its
+    `REF ?=` default, the one place that names where the tree lies."""
+    try:
+        for ln in open(os.path.join(HERE, "refshim", "Makefile")):
+            if ln.startswith("REF ?="):
+                return ln.split("=", 1)[1].strip()
+    except OSError:
+        pass
+    return ""
+
+
+# NLMECH_REFERENCE overrides the recipe's default; where neither holds the
+# tree, the checks that need it are skipped.
+REF_TREE = os.environ.get("NLMECH_REFERENCE") or _recipe_reference_tree()
 REF_LIB = os.path.join(HERE, "_ref", "libref_rnp.so")
 _ref = None
 

@@ -1,7 +1,7 @@
 """Build the golden fixtures of the quasi-static ElasticState examples.
 
-Run in a checkout that has the NLMech reference tree at REF (default
-/root/reference); writes qs_1d.npz and qs_2d.npz beside this script.  The
+Run in a checkout that has the NLMech reference tree (NLMECH_REFERENCE, or
+the refshim recipe's default location); writes qs_1d.npz and qs_2d.npz beside this script.  The
 fixtures are the reference's own stored results:
 
   examples/qsModel/1D/output_res.vtu  (33 nodes, deck examples/qsModel/1D/input.yaml)
@@ -27,8 +27,9 @@ import zlib
 
 import numpy as np
 
-REF = os.environ.get("NLM_REFERENCE", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+from oracle.oracle import REF_TREE as REF  # noqa: E402
 
 
 def read_vtu(path):

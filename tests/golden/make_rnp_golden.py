@@ -4,7 +4,7 @@ RNPBond, Neighbor, Fracture, InteriorFlags and ULoading/FLoading sources
 tests/refcases.py, for the GPU tests to compare against on machines without
 the reference tree.
 
-    python tests/golden/make_rnp_golden.py
+    python tests/golden/make_rnp_golden.py [case ...]   (default: every case)
 """
 import os
 import sys
@@ -21,8 +21,10 @@ import refcases  # noqa: E402
 CASES = refcases.GOLDEN_CASES
 
 
-def main():
+def main(names=None):
     for name, (make, steps) in CASES.items():
+        if names and name not in names:
+            continue
         p = make()
         r = orc.RefRNP(p)
         rowptr, cols = r.neighbors()
@@ -41,4 +43,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

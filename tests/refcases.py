@@ -130,6 +130,26 @@ def angled_regions_plate():
     return p
 
 
+def gaussian_plate():
+    """The growing-crack plate with the Gaussian influence function
+    J(r) = alpha exp(-r^2 / beta) at its default parameters (beta = 0.2,
+    alpha making the d-th moment one; influenceFn.h:278-307)."""
+    p = fracture_plate()
+    p.material.influence_type = 2
+    p.material.influence_params = []
+    return p
+
+
+def gaussian_params_plate():
+    """The Gaussian influence function with parameters from the deck
+    (alpha = 1.5, beta = 0.35; influenceFn.h:302-305), on the plate with
+    force BCs and a computed no-fail layer."""
+    p = loads_nofail_plate()
+    p.material.influence_type = 2
+    p.material.influence_params = [1.5, 0.35]
+    return p
+
+
 # name -> (problem, Verlet steps) of the committed reference outputs
 # (tests/golden/rnp_ref_<name>.npz)
 GOLDEN_CASES = {
@@ -142,4 +162,6 @@ GOLDEN_CASES = {
     "nofail_regions_plate": (nofail_regions_plate, 300),
     "force_functions_plate": (force_functions_plate, 200),
     "angled_regions_plate": (angled_regions_plate, 200),
+    "gaussian_plate": (gaussian_plate, 300),
+    "gaussian_params_plate": (gaussian_params_plate, 200),
 }

@@ -13,7 +13,7 @@ from nlmech_gb300 import abi, configs, deckfile, meshfile, vtu
 from nlmech_gb300.decks import BC, Crack
 from oracle import oracle as orc
 
-REF = os.environ.get("NLM_REFERENCE", "/root/reference")
+REF = orc.REF_TREE
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 needs_ref = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "examples")),
                                reason="reference tree not present")

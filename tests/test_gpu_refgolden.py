@@ -19,7 +19,8 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 RTOL = {"fracture_plate": 1e-12, "loads_nofail_plate": 1e-11, "cube3d": 1e-12,
         "contact_plate": 1e-12, "timed_crack_plate": 1e-12, "reaction_plate": 1e-12,
         "nofail_regions_plate": 1e-12, "force_functions_plate": 1e-12,
-        "angled_regions_plate": 1e-11}
+        "angled_regions_plate": 1e-11, "gaussian_plate": 1e-12,
+        "gaussian_params_plate": 1e-11}
 
 
 def _pairs(rowptr, cols, b):
@@ -73,6 +74,23 @@ def test_fp32c_matches_reference_golden(gpu):
         assert np.linalg.norm(u - z["u"]) <= 1e-5 * np.linalg.norm(z["u"])
         diff = len(_pairs(z["rowptr"], z["cols"], m.bond_state()) ^ ref)
         assert diff <= 1e-3 * len(ref), (diff, len(ref))
+
+
+@pytest.mark.parametrize("name", ["gaussian_plate", "gaussian_params_plate"])
+def test_fp32c_gaussian_influence_against_reference_golden(gpu, name):
+    """FP32C with the Gaussian influence function (J evaluated per bond with
+    ex2.approx; not folded into the bond constant) on every decomposition."""
+    make, steps = GOLDEN_CASES[name]
+    z = np.load(os.path.join(GOLDEN, "rnp_ref_%s.npz" % name))
+    ref = _pairs(z["rowptr"], z["cols"], z["broken"])
+    for dec in (abi.DECOMP_THREAD, abi.DECOMP_WARP, abi.DECOMP_TILE, abi.DECOMP_TILE_LOCAL):
+        m = gpu.FDModel(make(), precision=abi.FP32C, decomposition=dec)
+        m.run(steps)
+        u = m.state()[0]
+        err = np.linalg.norm(u - z["u"]) / np.linalg.norm(z["u"])
+        diff = len(_pairs(z["rowptr"], z["cols"], m.bond_state()) ^ ref)
+        assert err <= 1e-5, (name, dec, err)
+        assert diff <= 1e-3 * max(len(ref), 1), (name, dec, diff, len(ref))
 
 
 def test_fp32c_contact_against_reference_golden(gpu):

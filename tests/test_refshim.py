@@ -14,8 +14,8 @@ import pytest
 from nlmech_gb300 import configs
 from oracle import oracle as orc
 
-from refcases import (GOLDEN_CASES, contact_plate, cube3d, fracture_plate, loads_nofail_plate,
-                      reaction_plate, timed_crack_plate)
+from refcases import (GOLDEN_CASES, contact_plate, cube3d, fracture_plate, gaussian_params_plate,
+                      gaussian_plate, loads_nofail_plate, reaction_plate, timed_crack_plate)
 
 needs_ref = pytest.mark.skipif(not orc.refshim_available(),
                                reason="reference source tree not present")
@@ -56,6 +56,15 @@ def test_refshim_fracture_bit_exact():
 @needs_ref
 def test_refshim_loads_nofail_influence_bit_exact():
     _same_run(loads_nofail_plate(), 200)
+
+
+@needs_ref
+def test_refshim_gaussian_influence_bit_exact():
+    """GaussianInfluenceFn with the default parameters and with parameters
+    from the deck (influenceFn.h:278-402)."""
+    r, _ = _same_run(gaussian_plate(), 300, chunks=3)
+    assert int(r.bond_state().sum()) > int(orc.RefRNP(gaussian_plate()).bond_state().sum()) + 50
+    _same_run(gaussian_params_plate(), 200)
 
 
 @needs_ref

@@ -19,6 +19,7 @@
 // per-node FP64 update would otherwise be the slowest part of the step.
 
 #include <algorithm>
+#include <atomic>
 
 #include "fp32_common.cuh"
 
@@ -366,26 +367,229 @@ __global__ void __launch_bounds__(kTileNodes, 3)
 // writes, per staged node, x - x_o and u - u_o rounded once to FP32 (x_o, u_o
 // of the tile's first node, both differences formed in the split
 // representation), so a bond needs one 16-byte shared-memory read and two
-// subtractions per component for xi and eta.  xi and eta then carry the
-// FP32 rounding of the tile-frame coordinates (~2^-24 of the tile span)
-// instead of ~2^-24 of themselves; the node's own update stays on the
-// (hi, lo) pairs.
+// packed subtractions for xi and eta.  xi then carries the FP32 rounding of
+// the tile-frame position (~2^-24 of the tile span) instead of ~2^-24 of
+// itself, and eta 2^-24 of the largest |u - u_o| of the tile (its
+// displacement span).  A tile whose span exceeds Params32::span_max (its
+// error in S would exceed 2^-20 of the critical stretch: fragments in free
+// flight, loads that throw nodes far) forms eta from the (hi, lo) pairs
+// instead, as the thread kernels do: the staged record then holds the hi
+// parts of u and a second array their lo parts.  The choice is made per tile
+// from a block reduction of the span during staging.  The node's own update
+// always stays on the (hi, lo) pairs.
+//
+// Bonds are read through tile_boff, 16-bit byte offsets into the staged
+// arrays (an offset is an address without further arithmetic; padding
+// entries address the row's own node, whose bond has xi = eta = 0 and adds
+// no force).  The tile's block of tile_boff (its 8 slices, contiguous) is
+// brought into shared memory by one bulk copy issued before the node
+// staging, so the bond loops read no global memory.  With one nodal volume
+// for the whole model (UV) K1 V is a constant and no volume is staged.
+//
+// Two loops evaluate a row.  The fast loop serves rows with no broken bond
+// and no no-fail or contact terms: it keeps no bond-state bits, only the
+// largest S^2 r of the row.  If that exceeds the break threshold (a bond
+// breaks this step; rare) or the row already has broken bonds, the row is
+// evaluated again by the full loop, which keeps the bits and the broken-bond
+// terms.  Both loops form S^2 r by the same separately rounded operations
+// (tile_bond_core), so they take the same break decisions.
 // BATCH: a batch of specimens in one layout.  A launch covers the tiles that
 // meet its node range [A.i0, A.i1) (a tile may hold nodes of two ranges and
 // of several specimens) and owns only the range's nodes that are not ghosts;
 // each node takes its own specimen's constants.  The staged volume is V, not
 // K1 V: specimens differ in K1, and a bond's two nodes share a specimen.
-template <int SCHEME, bool NW1, int OPT, bool BATCH>
+
+// One bond in the tile frame: d = xi, e = eta, vj = K1 V_j (KV) or V_j.
+// Returns s0 (the linearised bond's F = s0 d), ex = exp(-beta r S^2) (the
+// unbroken bond's F = s0 ex d), bs2 = S^2 r (|S| > S_c <=> bs2 > Ksc) and r.
+// A padding bond (d = e = 0) gives s0 = bs2 = 0.
+template <int OPT, bool KV>
+__device__ __forceinline__ void tile_bond_core(const Params32 &Q, float2 d, float2 e, float vj,
+                                               float &s0, float &ex, float &bs2, float &r) {
+  const float r2 = fmaxf(__fmaf_rn(d.y, d.y, __fmul_rn(d.x, d.x)), 1e-30f);
+  const float de = __fmaf_rn(d.y, e.y, __fmul_rn(d.x, e.x));
+  const float rinv = rsqrt_approx(r2);
+  r = __fmul_rn(r2, rinv);
+  float kw = __fmul_rn(KV ? vj : __fmul_rn(Q.K1, vj), fminf(1.f, __fmaf_rn(-r, Q.inv_h, Q.cu_ih)));
+  if (!(OPT & OPT_CONSTJ) && Q.infl_type != 0) {  // type 0: J folded into K1
+    const float rr = __fmul_rn(r, Q.inv_delta);
+    kw = __fmul_rn(kw, Q.infl_type == 1
+                           ? __fmaf_rn(Q.a1, rr, Q.a0)
+                           : __fmul_rn(Q.alpha, ex2_approx(__fmul_rn(__fmul_rn(-rr, rr),
+                                                                     Q.ibeta * 1.4426950408889634f))));
+  }
+  const float a = __fmul_rn(de, rinv);  // S r
+  const float S = __fmul_rn(a, rinv);
+  bs2 = __fmul_rn(a, S);
+  s0 = __fmul_rn(kw, __fmul_rn(S, rinv));
+  ex = ex2_approx(__fmul_rn(Q.nbl2e, bs2));
+}
+
+__device__ __forceinline__ float4 lds_f4(const char *base, uint32_t off) {
+  return *reinterpret_cast<const float4 *>(base + off);
+}
+__device__ __forceinline__ float2 lds_f2(const char *base, uint32_t off) {
+  return *reinterpret_cast<const float2 *>(base + off);
+}
+__device__ __forceinline__ float lds_f(const char *base, uint32_t off) {
+  return *reinterpret_cast<const float *>(base + off);
+}
+
+// Staged arrays of a tile, as byte addresses for offset arithmetic.
+struct TileShared {
+  const char *xu;   // float4 per staged node (16 bytes: the offset unit)
+  const char *vol;  // float per staged node (offset / 4)
+  const char *ul;   // float2 per staged node (offset / 2), exact mode
+  const uint8_t *fl;
+};
+
+// xi, eta and the volume term of the bond at staged byte offset o.
+template <bool UV, bool EXACT>
+__device__ __forceinline__ void tile_bond_data(const TileShared &S, uint32_t o, float2 xi_x,
+                                               float2 xi_u, float2 uli, float kvu, float2 &d,
+                                               float2 &e, float &vj) {
+  const float4 xj = lds_f4(S.xu, o);
+  d = sub_f32x2(make_float2(xj.x, xj.y), xi_x);
+  e = sub_f32x2(make_float2(xj.z, xj.w), xi_u);
+  if (EXACT) {
+    const float2 ulj = lds_f2(S.ul, o >> 1);
+    const float2 dl = sub_f32x2(ulj, uli);
+    e = make_float2(e.x + dl.x, e.y + dl.y);
+  }
+  vj = UV ? kvu : lds_f(S.vol, o >> 2);
+}
+
+// The force on node i (row of len bonds at sb) and, in the full loop, its
+// bond-state bits; then the integrator epilogue.
+template <int SCHEME, bool NW1, int OPT, bool BATCH, bool UV, bool EXACT>
+__device__ __forceinline__ void tilel_node(const StepParams &P, const Params32 &Qn,
+                                           const DevPtrs &D, const BCTable &T, const StepArgs &A,
+                                           const TileShared &S, const uint2 *sb, int64_t i, int il,
+                                           uint8_t fl, int len, uint32_t word, float4 ui4) {
+  constexpr bool KV = !(OPT & OPT_CONTACT) && !BATCH;
+  constexpr bool FAST = !(OPT & (OPT_NOFAIL | OPT_CONTACT));
+  const int ng = (len + 3) >> 2;
+  const float4 xi = reinterpret_cast<const float4 *>(S.xu)[il];
+  const float2 xi_x = make_float2(xi.x, xi.y), xi_u = make_float2(xi.z, xi.w);
+  const float2 uli = EXACT ? reinterpret_cast<const float2 *>(S.ul)[il] : make_float2(0.f, 0.f);
+  const float voli = reinterpret_cast<const float *>(S.vol)[il];  // contact term only (raw V)
+  const float kvu = Qn.kv_uniform;
+  float uih[3] = {ui4.x, ui4.y, 0.f}, uil[3] = {ui4.z, ui4.w, 0.f};
+  const bool brk_i = !(fl & FLAG_NOFAIL);
+  float fi[3] = {0.f, 0.f, 0.f};
+  bool full = !FAST;
+  if (FAST) {
+    if (!NW1)
+      for (int w = 0; w * 32 < len; w++) word |= D.bits[(int64_t)w * P.npad + i];
+    full = word != 0u;
+  }
+  if (FAST && !full) {
+    float mx = 0.f;  // largest S^2 r of the row
+    for (int g = 0; g < ng; g++) {
+      const uint2 cur = sb[32 * g];
+      const uint32_t o[4] = {cur.x & 0xffffu, cur.x >> 16, cur.y & 0xffffu, cur.y >> 16};
+      float2 d[4], e[4];
+      float vj[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        tile_bond_data<UV, EXACT>(S, o[q], xi_x, xi_u, uli, kvu, d[q], e[q], vj[q]);
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        float s0, ex, bs2, r;
+        tile_bond_core<OPT, KV>(Qn, d[q], e[q], vj[q], s0, ex, bs2, r);
+        const float s1 = __fmul_rn(s0, ex);
+        mx = fmaxf(mx, bs2);
+        fi[0] = fmaf(s1, d[q].x, fi[0]);
+        fi[1] = fmaf(s1, d[q].y, fi[1]);
+      }
+    }
+    full = mx > Qn.ksc_on;
+  }
+  if (full) {
+    // the rows with broken bonds, bonds breaking now, no-fail or contact
+    // terms: bond-state bits kept per bond
+    fi[0] = fi[1] = 0.f;
+    uint32_t nw = 0;
+    word = NW1 ? D.bits[i] : 0u;
+    for (int g = 0; g < ng; g++) {
+      const uint2 c = sb[32 * g];
+      if (!NW1 && (g & 7) == 0) {
+        if (nw) D.bits[(int64_t)((g >> 3) - 1) * P.npad + i] = word | nw;
+        word = D.bits[(int64_t)(g >> 3) * P.npad + i];
+        nw = 0;
+      }
+      const uint32_t o[4] = {c.x & 0xffffu, c.x >> 16, c.y & 0xffffu, c.y >> 16};
+      const int sh = (4 * g) & 31;
+      const uint32_t w4 = word >> sh;
+      uint32_t n4 = 0;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        float2 d, e;
+        float vj;
+        tile_bond_data<UV, EXACT>(S, o[q], xi_x, xi_u, uli, kvu, d, e, vj);
+        float s0, ex, bs2, r;
+        tile_bond_core<OPT, KV>(Qn, d, e, vj, s0, ex, bs2, r);
+        bool fs = (w4 >> q) & 1u;
+        bool breakable = true;
+        if (OPT & OPT_NOFAIL) breakable = brk_i && !(S.fl[o[q] >> 4] & FLAG_NOFAIL);
+        if (breakable) fs = fs || bs2 > Qn.ksc_on;
+        float sc;
+        if (!breakable) {
+          // no-fail bond: the linearised force 4 J S C beta / invF V_j^c
+          sc = s0;
+        } else if ((OPT & OPT_CONTACT) && fs) {
+          // broken bond: normal contact only (rnpBond.cpp:281-291), along the
+          // deformed bond y = xi + eta
+          const float y0 = d.x + e.x, y1 = d.y + e.y;
+          const float R = sqrtf(y0 * y0 + y1 * y1);
+          const float vjc = vj * fminf(1.f, __fmaf_rn(-r, Qn.inv_h, Qn.cu_ih));
+          const float sf = Qn.kn * (voli * vjc / (voli + vjc)) * (Qn.rc - R) / R;
+          d = make_float2(y0, y1);
+          sc = -fmaxf(sf, 0.f);
+        } else {
+          sc = fs ? 0.f : __fmul_rn(s0, ex);
+        }
+        n4 |= fs ? 1u << q : 0u;
+        fi[0] = fmaf(sc, d.x, fi[0]);
+        fi[1] = fmaf(sc, d.y, fi[1]);
+      }
+      nw |= n4 << sh;
+    }
+    // bits past the row's end stay clear
+    if (len & 31) nw &= (1u << (len & 31)) - 1u;
+    if (nw) D.bits[NW1 ? i : (int64_t)((len - 1) >> 5) * P.npad + i] = word | nw;
+  }
+  integrate_node32<2, SCHEME>(P, Qn, D, T, A, i, fl, uih, uil, fi);
+}
+
+template <int SCHEME, bool NW1, int OPT, bool BATCH, bool UV>
 __global__ void __launch_bounds__(kTileNodes, 4)
     k_rnp32_tilel(const StepParams P, const Params32 Q, const DevPtrs D, const BCTable T,
                   const StepArgs A) {
-  __shared__ float4 s_xu[kTileMaxLocal];  // x - x_o, y - y_o, ux - ux_o, uy - uy_o
-  __shared__ float s_vol[kTileMaxLocal];  // K1 V (V with the contact term or in a batch)
+  // per staged node: x - x_o, y - y_o, and ux - ux_o, uy - uy_o (frame mode)
+  // or the hi parts of ux, uy (exact mode, lo parts in s_ul)
+  __shared__ float4 s_xu[kTileMaxLocal];
+  __shared__ float s_vol[UV ? 1 : kTileMaxLocal];  // K1 V (V with the contact term or in a batch)
+  __shared__ float2 s_ul[kTileMaxLocal];
   constexpr bool KV = !(OPT & OPT_CONTACT) && !BATCH;
   __shared__ uint8_t s_fl[(OPT & OPT_NOFAIL) ? kTileMaxLocal : 1];
+  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ float s_wspan[kTileNodes / 32];
+  extern __shared__ __align__(128) unsigned char s_ids[];  // the tile's id block
   const int tb = A.tiles ? A.tiles[blockIdx.x]
                          : (int)blockIdx.x + (BATCH ? (int)(A.i0 / kTileNodes) : 0);
   const int64_t t0 = (int64_t)tb * kTileNodes;
+  const int64_t sl0 = 8 * (int64_t)tb;
+  const int64_t ib0 = D.sell_ptr[sl0];
+  if (threadIdx.x == 0) {
+    mbar_init(&s_bar, 1);
+    const int64_t sl1 = min(sl0 + 8, (P.n + 31) >> 5);
+    const uint32_t bytes = (uint32_t)(2 * (D.sell_ptr[sl1] - ib0));
+    if (bytes > 0)
+      bulk_copy_g2s(s_ids, D.tile_boff + ib0, bytes, &s_bar);
+    else
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&s_bar)) : "memory");
+  }
   const int h0 = D.tile_hptr[tb];
   const int nh = D.tile_hptr[tb + 1] - h0;
   const int nt = (int)min((int64_t)kTileNodes, P.n - t0);
@@ -402,12 +606,9 @@ __global__ void __launch_bounds__(kTileNodes, 4)
   const uint8_t fl = own ? D.flags[i] : 0;
   if (BATCH && (fl & FLAG_GHOST)) own = false;
   const int len = own ? D.rowlen[i] : 0;
-  const int ng = (len + 3) >> 2;
-  const uint2 *lp = reinterpret_cast<const uint2 *>(D.tile_lidx + (own ? D.sell_ptr[i >> 5] : 0)) +
-                    (i & 31);
-  uint32_t word = (NW1 && own) ? D.bits[i] : 0u;
-  uint2 nxt = ng > 0 ? __ldg(lp) : make_uint2(0u, 0u);
-  float4 ui4 = own ? ucur[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const int64_t rbase = own ? D.sell_ptr[i >> 5] : ib0;
+  const uint32_t word = (NW1 && own) ? D.bits[i] : 0u;
+  const float4 ui4 = own ? ucur[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   if (own) {
     // the integrator's velocity and force reads, brought into L1 early
     const float4 *vp = D.v32[SCHEME == NLM_VELOCITY_VERLET ? 0 : A.cur] + i;
@@ -415,65 +616,86 @@ __global__ void __launch_bounds__(kTileNodes, 4)
     asm volatile("prefetch.global.L1 [%0];" ::"l"(vp));
     asm volatile("prefetch.global.L1 [%0];" ::"l"(fp));
   }
+  float span = 0.f;  // largest |u - u_o| staged by this thread
   for (int e = threadIdx.x; e < kTileNodes + nh; e += blockDim.x) {
     if (e < kTileNodes && e >= nt) continue;
     const int64_t g = e < kTileNodes ? t0 + e : (int64_t)D.tile_halo[h0 + e - kTileNodes];
     const float4 a = __ldg(D.pos32 + g);
     const float2 lo = __half22float2(*reinterpret_cast<const __half2 *>(&a.w));
     const float4 u = ucur[g];
+    const float dux = (u.x - uo.x) + (u.z - uo.z), duy = (u.y - uo.y) + (u.w - uo.w);
+    span = fmaxf(span, fmaxf(fabsf(dux), fabsf(duy)));
     s_xu[e] = make_float4(fmaf(lo.x - plo.x, Q.inv_lo, a.x - po.x),
-                          fmaf(lo.y - plo.y, Q.inv_lo, a.y - po.y),
-                          (u.x - uo.x) + (u.z - uo.z), (u.y - uo.y) + (u.w - uo.w));
-    s_vol[e] = KV ? Q.K1 * a.z : a.z;
+                          fmaf(lo.y - plo.y, Q.inv_lo, a.y - po.y), dux, duy);
+    if (!UV) s_vol[e] = KV ? Q.K1 * a.z : a.z;
     if (OPT & OPT_NOFAIL) s_fl[e] = D.flags[g];
   }
+  // the tile's displacement span (NaN counts as too large)
+  for (int o = 16; o > 0; o >>= 1) span = fmaxf(span, __shfl_xor_sync(0xffffffffu, span, o));
+  if ((threadIdx.x & 31) == 0) s_wspan[threadIdx.x >> 5] = span != span ? 3e38f : span;
   __syncthreads();
+  float bspan = 0.f;
+#pragma unroll
+  for (int w = 0; w < kTileNodes / 32; w++) bspan = fmaxf(bspan, s_wspan[w]);
+  const bool exact = bspan > Q.span_max;
+  if (exact) {
+    // block-uniform: restage eta's inputs as (hi, lo) pairs
+    for (int e = threadIdx.x; e < kTileNodes + nh; e += blockDim.x) {
+      if (e < kTileNodes && e >= nt) continue;
+      const int64_t g = e < kTileNodes ? t0 + e : (int64_t)D.tile_halo[h0 + e - kTileNodes];
+      const float4 u = ucur[g];
+      s_xu[e].z = u.x;
+      s_xu[e].w = u.y;
+      s_ul[e] = make_float2(u.z, u.w);
+    }
+    __syncthreads();
+  }
+  // the id block; a wait that gives up (which only a failing copy would
+  // cause) flags the error, waits once more for the copy and leaves
+  if (!mbar_wait(&s_bar, 0, 1u << 22)) {
+    if (threadIdx.x == 0) atomicExch(D.err, 1);
+    mbar_wait(&s_bar, 0, 1u << 22);
+    return;
+  }
   if (!own) return;
   const Params32 &Qn = BATCH ? static_cast<const Params32 *>(D.qtab)[D.slice_spec[i >> 5]] : Q;
-  const float4 xi = s_xu[il];
-  const float voli = s_vol[il];  // used by the contact term only (raw V there)
-  float uih[3] = {ui4.x, ui4.y, 0.f}, uil[3] = {ui4.z, ui4.w, 0.f};
-  const bool brk_i = !(fl & FLAG_NOFAIL);
-  float fi[3] = {0.f, 0.f, 0.f};
-  uint32_t nw = 0;
-  for (int g = 0; g < ng; g++) {
-    const uint2 cur = nxt;
-    if (g + 1 < ng) nxt = __ldg(lp + 32 * (g + 1));
-    if (!NW1 && (g & 7) == 0) {
-      if (nw) D.bits[(int64_t)((g >> 3) - 1) * P.npad + i] = word | nw;
-      word = D.bits[(int64_t)(g >> 3) * P.npad + i];
-      nw = 0;
-    }
-    const int jl[4] = {(int)(cur.x & 0xffffu), (int)(cur.x >> 16), (int)(cur.y & 0xffffu),
-                       (int)(cur.y >> 16)};
-    float4 xj[4];
-    float vj[4];
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      xj[q] = s_xu[jl[q]];
-      vj[q] = s_vol[jl[q]];
-    }
-    // the group's four state bits, and its four new-break bits
-    const int sh = (4 * g) & 31;
-    const uint32_t w4 = word >> sh;
-    uint32_t n4 = 0;
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      float dv[3] = {xj[q].x - xi.x, xj[q].y - xi.y, 0.f};
-      bool fs = (w4 >> q) & 1u;
-      bool breakable = true;
-      if (OPT & OPT_NOFAIL) breakable = brk_i && !(s_fl[jl[q]] & FLAG_NOFAIL);
-      const float sc = rnp_bond32_core<2, OPT, KV>(Qn, dv, xj[q].z - xi.z, xj[q].w - xi.w, 0.f,
-                                                   vj[q], voli, breakable, fs);
-      // a bond broken before keeps its bit: OR-ing it in again changes nothing
-      n4 |= fs ? 1u << q : 0u;
-      fi[0] = fmaf(sc, dv[0], fi[0]);
-      fi[1] = fmaf(sc, dv[1], fi[1]);
-    }
-    nw |= n4 << sh;
+  const uint2 *sb = reinterpret_cast<const uint2 *>(s_ids) + ((rbase - ib0) >> 2) + (i & 31);
+  const TileShared S{reinterpret_cast<const char *>(s_xu), reinterpret_cast<const char *>(s_vol),
+                     reinterpret_cast<const char *>(s_ul), s_fl};
+  if (exact)
+    tilel_node<SCHEME, NW1, OPT, BATCH, UV, true>(P, Qn, D, T, A, S, sb, i, il, fl, len, word,
+                                                  ui4);
+  else
+    tilel_node<SCHEME, NW1, OPT, BATCH, UV, false>(P, Qn, D, T, A, S, sb, i, il, fl, len, word,
+                                                   ui4);
+}
+
+// Dynamic shared memory above the default 48 KB for the tile-frame kernel's
+// id block: opted in once per device and kernel.
+template <class K>
+static void tile_ids_smem(K kernel, std::atomic<uint64_t> &done) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const uint64_t bit = 1ull << (dev & 63);
+  if (done.load() & bit) return;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kTileIdsMaxBytes) == cudaSuccess)
+    done.fetch_or(bit);
+}
+
+template <int SCHEME, int OPT, bool BATCH, bool UV>
+static void tilel_launch(const StepParams &P, const Params32 &Q, const DevPtrs &D,
+                         const BCTable &T, const StepArgs &a, unsigned grid, size_t dyn,
+                         cudaStream_t s) {
+  if (P.nw1) {
+    static std::atomic<uint64_t> opt{0};
+    tile_ids_smem(k_rnp32_tilel<SCHEME, true, OPT, BATCH, UV>, opt);
+    k_rnp32_tilel<SCHEME, true, OPT, BATCH, UV><<<grid, kTileNodes, dyn, s>>>(P, Q, D, T, a);
+  } else {
+    static std::atomic<uint64_t> opt{0};
+    tile_ids_smem(k_rnp32_tilel<SCHEME, false, OPT, BATCH, UV>, opt);
+    k_rnp32_tilel<SCHEME, false, OPT, BATCH, UV><<<grid, kTileNodes, dyn, s>>>(P, Q, D, T, a);
   }
-  if (nw) D.bits[NW1 ? i : (int64_t)((len - 1) >> 5) * P.npad + i] = word | nw;
-  integrate_node32<2, SCHEME>(P, Qn, D, T, A, i, fl, uih, uil, fi);
 }
 
 template <int DIM, int SCHEME, int OPT, bool BATCH>
@@ -493,17 +715,21 @@ static void launch_opt(const StepParams &P, const Params32 &Q, const DevPtrs &D,
       k_rnp32_tile<SCHEME, false, OPT><<<grid, kTileNodes, 0, s>>>(P, Q, D, T, a);
     return;
   }
-  if (DIM == 2 && decomp == NLM_DECOMP_TILE_LOCAL && D.tile_lidx) {
+  if (DIM == 2 && decomp == NLM_DECOMP_TILE_LOCAL && D.tile_boff) {
     // a batch launch covers the tiles that meet its node range
     const unsigned grid =
         a.tiles ? (unsigned)a.ntiles
         : BATCH ? (unsigned)((a.i1 + kTileNodes - 1) / kTileNodes - a.i0 / kTileNodes)
                 : (unsigned)((P.n + kTileNodes - 1) / kTileNodes);
     if (grid == 0) return;
-    if (P.nw1)
-      k_rnp32_tilel<SCHEME, true, OPT, BATCH><<<grid, kTileNodes, 0, s>>>(P, Q, D, T, a);
-    else
-      k_rnp32_tilel<SCHEME, false, OPT, BATCH><<<grid, kTileNodes, 0, s>>>(P, Q, D, T, a);
+    const size_t dyn = (size_t)D.tile_ids_bytes;
+    // one nodal volume for the whole model: K1 V as a constant
+    constexpr bool KV = !(OPT & OPT_CONTACT) && !BATCH;
+    if (KV && Q.kv_uniform > 0.f) {
+      tilel_launch<SCHEME, OPT, BATCH, KV>(P, Q, D, T, a, grid, dyn, s);
+    } else {
+      tilel_launch<SCHEME, OPT, BATCH, false>(P, Q, D, T, a, grid, dyn, s);
+    }
     return;
   }
   if (decomp == NLM_DECOMP_WARP) {

@@ -555,15 +555,37 @@ struct nlm_fd {
 
   int vidx() const { return scheme == NLM_CENTRAL_DIFFERENCE ? cur : 0; }
 
+  // device bytes the handle may still allocate (nlm_fd_set_alloc_limit); < 0: no limit
+  int64_t alloc_budget = -1;
+  std::vector<size_t> alloc_sizes;  // bytes of allocs[k]
+
   template <class Tp>
   cudaError_t alloc(Tp **p, size_t count) {
+    const size_t bytes = count * sizeof(Tp) + 16;
+    if (alloc_budget >= 0 && (int64_t)bytes > alloc_budget) return cudaErrorMemoryAllocation;
     void *q = nullptr;
-    cudaError_t e = cudaMalloc(&q, count * sizeof(Tp) + 16);
+    cudaError_t e = cudaMalloc(&q, bytes);
     if (e == cudaSuccess) {
       allocs.push_back(q);
+      alloc_sizes.push_back(bytes);
+      if (alloc_budget >= 0) alloc_budget -= (int64_t)bytes;
       *p = static_cast<Tp *>(q);
     }
     return e;
+  }
+  // free one allocation of alloc() (no-op for null) and clear the pointer
+  template <class Tp>
+  void release(Tp **p) {
+    if (!*p) return;
+    for (size_t k = 0; k < allocs.size(); k++)
+      if (allocs[k] == (void *)*p) {
+        cudaFree(allocs[k]);
+        if (alloc_budget >= 0) alloc_budget += (int64_t)alloc_sizes[k];
+        allocs.erase(allocs.begin() + k);
+        alloc_sizes.erase(alloc_sizes.begin() + k);
+        break;
+      }
+    *p = nullptr;
   }
   ~nlm_fd() {
     if (stream) cudaStreamSynchronize(stream);
@@ -787,7 +809,9 @@ int launch_step(nlm_fd *h, const StepArgs &a0) {
 // reach, ascending.  Each bond stores its neighbour's index in the tile's
 // staged list (tile nodes 0..255, halo from 256), in the sliced layout of
 // sell_cols; padding entries point at the row's own node.  If some tile needs
-// more than kTileMaxLocal staged nodes the store is not built.
+// more than kTileMaxLocal staged nodes the store is not built.  The 2-D
+// RNPBond store (max_local == kTileMaxLocal) also gets the byte-offset copy
+// tile_boff (16 x index).
 // What a tile store is built from (one model or a batch's combined layout).
 struct TileInputs {
   int64_t n, nnz, nslices, sell_entries;
@@ -812,7 +836,9 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
   NLM_CUDA(cudaStreamSynchronize(h->stream));
   const std::vector<int64_t> &rp = *in.rowptr;
   std::vector<std::vector<int>> halo(nt);
+  const bool boff_too = max_local == kTileMaxLocal;
   std::vector<uint16_t> lidx(in.sell_entries + 4, 0);
+  std::vector<uint16_t> boff(boff_too ? in.sell_entries + 4 : 0, 0);
   std::vector<int> too_big(1, 0);
   std::vector<int> need(nt, -1);
   unsigned nthr = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
@@ -847,6 +873,7 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
                                                          hl.begin());
           }
           lidx[base + (k >> 2) * 128 + (k & 3)] = (uint16_t)loc;
+          if (boff_too) boff[base + (k >> 2) * 128 + (k & 3)] = (uint16_t)(16 * loc);
         }
       }
     }
@@ -855,6 +882,13 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
   for (unsigned w = 0; w < nthr; w++) pool.emplace_back(work, w);
   for (auto &th : pool) th.join();
   if (too_big[0]) return NLM_OK;
+  // id block of a tile: its 8 slices, contiguous in the sliced layout
+  int64_t ids_max = 0;
+  for (int64_t t = 0; t < nt; t++) {
+    const int64_t s0 = 8 * t, s1 = std::min<int64_t>(8 * t + 8, in.nslices);
+    ids_max = std::max(ids_max, 2 * (sptr[s1] - sptr[s0]));
+  }
+  if (boff_too && ids_max > kTileIdsMaxBytes) return NLM_OK;
   std::vector<int> hptr(nt + 1, 0);
   size_t nmax = 0;
   for (int64_t t = 0; t < nt; t++) {
@@ -871,8 +905,16 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
   NLM_CUDA(cudaMemcpyAsync(d_l, lidx.data(), sizeof(uint16_t) * lidx.size(), cudaMemcpyHostToDevice, h->stream));
   NLM_CUDA(cudaMemcpyAsync(d_hp, hptr.data(), sizeof(int) * hptr.size(), cudaMemcpyHostToDevice, h->stream));
   NLM_CUDA(cudaMemcpyAsync(d_h, hall.data(), sizeof(int) * hall.size(), cudaMemcpyHostToDevice, h->stream));
+  uint16_t *d_b = nullptr;
+  if (boff_too) {
+    NLM_CUDA(h->alloc(&d_b, boff.size()));
+    NLM_CUDA(cudaMemcpyAsync(d_b, boff.data(), sizeof(uint16_t) * boff.size(),
+                             cudaMemcpyHostToDevice, h->stream));
+  }
   NLM_CUDA(cudaStreamSynchronize(h->stream));
   h->D.tile_lidx = d_l;
+  h->D.tile_boff = d_b;
+  h->D.tile_ids_bytes = (int)ids_max;
   h->D.tile_hptr = d_hp;
   h->D.tile_halo = d_h;
   h->D.tile_nmax = kTileNodes + (int)nmax;
@@ -1283,7 +1325,10 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
   h->rows_by_orig = h->precision == NLM_PREC_FP64;
   e = build_neighbors(nb, d->dim, n, dx, g, S, s, why, h->rows_by_orig);
   for (void *p : {(void *)nb.perm, (void *)nb.pos, (void *)nb.rowptr, (void *)nb.cols})
-    if (p) h->allocs.push_back(p);
+    if (p) {
+      h->allocs.push_back(p);
+      h->alloc_sizes.push_back(0);
+    }
   if (e != cudaSuccess)
     return bail(why.empty() ? cuda_fail(e, "neighbour build") : fail(NLM_ERR_INVALID, why));
   h->nnz = nb.nnz;
@@ -1291,7 +1336,10 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
   SellStore st;
   e = build_sell(n, nb.rowptr, nb.cols, st, s);
   for (void *p : {(void *)st.ptr, (void *)st.width, (void *)st.cols})
-    if (p) h->allocs.push_back(p);
+    if (p) {
+      h->allocs.push_back(p);
+      h->alloc_sizes.push_back(0);
+    }
   if (e != cudaSuccess) return bail(cuda_fail(e, "bond store build"));
   h->nslices = st.nslices;
   h->sell_entries = st.entries;
@@ -1448,6 +1496,11 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
     D.rowlen = drl;
   }
   P.nw1 = P.nwords == 1 ? 1 : 0;
+  // a common nodal volume (uniform grids) lets the FP32C tile kernel take
+  // K1 V as a constant instead of staging it per node
+  P.vol_uniform = n > 0 ? d->volume[0] : 0.;
+  for (int64_t i = 1; i < n && P.vol_uniform > 0.; i++)
+    if (d->volume[i] != d->volume[0]) P.vol_uniform = 0.;
   if (h->precision == NLM_PREC_FP32C) {
     double xmax = 0.;
     for (int64_t k = 0; k < 3 * n; k++) xmax = std::max(xmax, std::fabs(d->x[k]));
@@ -1817,19 +1870,43 @@ int nlm_fd_load(nlm_fd *h, const char *path) {
        std::fread(b.data(), 1, b.size(), fp) == b.size();
   std::fclose(fp);
   if (!ok) return fail(NLM_ERR_INVALID, std::string("not a complete checkpoint: ") + path);
-  int rc = nlm_fd_set_bond_state(h, b.data());
+  // everything that can be checked is checked before the handle changes
+  if (!finite_all(st.data(), (int64_t)st.size()) || !std::isfinite(hd.time) || hd.step < 0)
+    return fail(NLM_ERR_NONFINITE, std::string("checkpoint holds a non-finite state or time: ") +
+                                       path);
+  // what a later failure puts back
+  std::vector<uint8_t> bits0((size_t)h->nnz);
+  int rc = nlm_fd_get_bond_state(h, bits0.data());
   if (rc) return rc;
-  h->time = hd.time;
-  h->step = hd.step;
-  h->cracks_on = hd.cracks_on;
-  if (!hd.started) {
-    h->started = false;
-    return nlm_fd_set_state(h, st.data(), st.data() + 3 * n);
+  const double time0 = h->time;
+  const int64_t step0 = h->step;
+  const uint32_t cracks0 = h->cracks_on;
+  const bool started0 = h->started;
+  rc = nlm_fd_set_bond_state(h, b.data());
+  if (rc == NLM_OK) {
+    h->time = hd.time;
+    h->step = hd.step;
+    h->cracks_on = hd.cracks_on;
+    if (!hd.started) {
+      h->started = false;
+      rc = nlm_fd_set_state(h, st.data(), st.data() + 3 * n);
+    } else {
+      // a started run: u^m, v^m and f^m as step_host takes them, then the
+      // drift to u^{m+1} that the interrupted step had done
+      h->started = true;
+      rc = nlm_fd_step_host(h, st.data(), st.data() + 3 * n, st.data() + 6 * n, 0);
+    }
   }
-  // a started run: u^m, v^m and f^m as step_host takes them, then the drift
-  // to u^{m+1} that the interrupted step had done
-  h->started = true;
-  return nlm_fd_step_host(h, st.data(), st.data() + 3 * n, st.data() + 6 * n, 0);
+  if (rc != NLM_OK) {
+    const std::string msg = nlm_last_error();
+    h->time = time0;
+    h->step = step0;
+    h->cracks_on = cracks0;
+    h->started = started0;
+    nlm_fd_set_bond_state(h, bits0.data());
+    set_error(msg);
+  }
+  return rc;
 }
 
 int nlm_fd_set_time(nlm_fd *h, double time, int64_t step) {
@@ -2060,6 +2137,28 @@ bool pipe_usable(const nlm_fd *h, int64_t nsteps) {
          (h->decomp == NLM_DECOMP_TILE || h->decomp == NLM_DECOMP_TILE_LOCAL) && !h->timing &&
          h->n >= kPipeMinNodes && !h->D.qtab &&
          (h->timed_cracks.empty() || !crack_due(h, 1));
+}
+
+// Frees what pipe_setup allocated or created, so a failed set-up leaves the
+// handle as it was before.
+void pipe_teardown(nlm_fd *h) {
+  if (h->pipe_sin) cudaStreamSynchronize(h->pipe_sin);
+  if (h->pipe_sout) cudaStreamSynchronize(h->pipe_sout);
+  for (auto e : h->pipe_ev) cudaEventDestroy(e);
+  h->pipe_ev.clear();
+  if (h->pipe_sin) cudaStreamDestroy(h->pipe_sin);
+  if (h->pipe_sout) cudaStreamDestroy(h->pipe_sout);
+  h->pipe_sin = h->pipe_sout = nullptr;
+  h->release(&h->pipe_tiles);
+  h->release(&h->pipe_in);
+  h->release(&h->pipe_back);
+  h->release(&h->pipe_ua);
+  h->release(&h->pipe_ub);
+  h->release(&h->pipe_v);
+  h->release(&h->pipe_f);
+  h->release(&h->pipe_bits);
+  h->release(&h->pipe_late);
+  h->pipe_nbands = 0;
 }
 
 // Band schedule and buffers of the banded step.  Tile t can run once every
@@ -2317,6 +2416,12 @@ int step_host_in_place(nlm_fd *h, double *u, double *v, double *f, int64_t nstep
 
 extern "C" {
 
+int nlm_fd_set_alloc_limit(nlm_fd *h, int64_t bytes) {
+  if (!h) return fail(NLM_ERR_INVALID, "null handle");
+  h->alloc_budget = bytes < 0 ? -1 : bytes;
+  return NLM_OK;
+}
+
 int nlm_fd_host_io(const nlm_fd *h, int *mode) {
   if (!h || !mode) return fail(NLM_ERR_INVALID, "null argument");
   *mode = h->host_io;
@@ -2338,11 +2443,18 @@ int nlm_fd_step_host(nlm_fd *h, double *u, double *v, double *f, int64_t nsteps)
   const bool aligned = ((uintptr_t)u | (uintptr_t)v | (uintptr_t)f) % 16 == 0 && n % 2 == 0;
   if (aligned && in_place_ok(u, bytes) && in_place_ok(v, bytes) && in_place_ok(f, bytes)) {
     if (pipe_usable(h, nsteps)) {
-      // if the banded path cannot be set up (device memory), the in-place
-      // path below serves this and every later call, with the same results
-      if (h->pipe_state == 0 && pipe_setup(h) != NLM_OK) {
-        h->pipe_state = -1;
-        cudaGetLastError();
+      // if the banded path's buffers cannot be allocated, what it had set up
+      // is freed and the in-place path below serves this and every later
+      // call, with the same results; any other set-up error is returned
+      if (h->pipe_state == 0) {
+        const int rc = pipe_setup(h);
+        if (rc != NLM_OK) {
+          pipe_teardown(h);
+          cudaGetLastError();
+          if (rc != NLM_ERR_OOM) return rc;
+          h->pipe_state = -1;
+          set_error("");
+        }
       }
       if (h->pipe_state == 1) return step_host_banded(h, u, v, f);
     }
@@ -2794,6 +2906,7 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
   std::vector<double> volp(N, 0.);
   std::vector<uint16_t> rl(N, 0);
   bool any_nofail = false;
+  double span_min = 1e300;
   for (int s = 0; s < nspec; s++) {
     const nlm_fd_desc &d = descs[s];
     StepParams Ps{};
@@ -2811,6 +2924,9 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
     if (rc) return bail(rc);
     if (Ps.contact) return bail(fail(NLM_ERR_UNSUPPORTED, "contact forces are not batched"));
     qtab[s] = make_p32(Ps);
+    // the tile kernel decides per tile (specimens may share one): the
+    // smallest span limit of all specimens
+    span_min = std::min(span_min, (double)qtab[s].span_max);
     for (int64_t q = b->off[s] / 32; q < (b->off[s] + d.n_nodes + 31) / 32; q++) slice_spec[q] = s;
     for (int c = 0; c < d.n_cracks; c++) {
       if (d.cracks[c].kind == NLM_CRACK_EDGE && d.dim != 2)
@@ -2893,6 +3009,7 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
   BTRY(cudaMemcpyAsync(vol64, volp.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st));
   BTRY(cudaMemcpyAsync(drl, rl.data(), sizeof(uint16_t) * N, cudaMemcpyHostToDevice, st));
   D.qtab = dq;
+  P.tile_span_max = nspec > 0 ? span_min : 0.;
   D.bct = dbct;
   D.slice_spec = dss;
   D.flags = dflags;

@@ -50,6 +50,10 @@ struct DevPtrs {
   // neighbour in the tile's staged node list (the tile's kTileNodes nodes,
   // then its halo), same slice layout as sell_cols; per tile the halo ids
   const uint16_t *tile_lidx;
+  // the same entries as byte offsets into a 16-byte-per-node staged array
+  // (16 x index; 2-D RNPBond tile-frame kernel)
+  const uint16_t *tile_boff;
+  int tile_ids_bytes;    // largest id block of a tile (8 slices of tile_boff), bytes
   const int *tile_hptr;  // tiles + 1
   const int *tile_halo;
   int tile_nmax;         // largest staged node list of any tile
@@ -60,6 +64,9 @@ struct DevPtrs {
 // the decomposition for the handle.
 constexpr int kTileNodes = 256;
 constexpr int kTileMaxLocal = 1280;
+// the tile-frame kernel copies a tile's id block into shared memory; a
+// store whose largest block exceeds this is not built
+constexpr int kTileIdsMaxBytes = 64 * 1024;
 // ElasticState tile kernels size their staged lists at run time (dynamic
 // shared memory, 36 bytes per staged node); a larger tile disables them.
 constexpr int kTileMaxLocalES = 3072;

@@ -5,6 +5,8 @@
 
 #include <cuda_fp16.h>
 
+#include <cmath>
+
 #include "fd_internal.h"
 #include "state_io.cuh"
 
@@ -25,6 +27,15 @@ struct Params32 {
   float c_hi, c_lo;     // Verlet dt/(2 rho) or CD dt^2/rho
   float dt_hi, dt_lo;
   float idt_hi, idt_lo; // 1/dt
+  // tile-frame kernel: volume factor min(1, cu_ih - r inv_h), and the
+  // break threshold on S^2 r (+inf when breaking is off)
+  float cu_ih;
+  float ksc_on;
+  // largest |u - u_o| of a tile's staged nodes for which bonds are formed
+  // from tile-frame displacements; a tile above it forms them from the
+  // (hi, lo) pairs
+  float span_max;
+  float kv_uniform;  // K1 V when every node has the same volume V, else 0
 };
 
 inline void split_const(double v, float &hi, float &lo) {
@@ -57,6 +68,15 @@ inline Params32 make_p32(const StepParams &P) {
   split_const(1.0 / P.dt, q.idt_hi, q.idt_lo);
   q.kn = P.contact ? (float)P.contact_kn : 0.f;
   q.rc = (float)P.contact_rc;
+  q.cu_ih = (float)(P.check_up / P.h);
+  q.ksc_on = P.irrev ? q.Ksc : __builtin_huge_valf();
+  // The tile frame rounds u - u_o to FP32: 2^-24 span absolute in eta, so
+  // 2^-24 span / |xi| in S.  Up to 16 h S_c(delta) of span that is at most
+  // 2^-20 of the critical stretch S_c(r) = f_sc rbar / sqrt(r) of any bond.
+  q.span_max = P.tile_span_max > 0.
+                   ? (float)P.tile_span_max
+                   : (float)(16.0 * P.h * P.fsc * P.rbar / std::sqrt(P.delta));
+  q.kv_uniform = P.vol_uniform > 0. ? (float)(k1 * P.vol_uniform) : 0.f;
   return q;
 }
 
@@ -75,6 +95,53 @@ __device__ __forceinline__ float ex2_approx(float x) {
   float y;
   asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
+}
+
+// ---- packed FP32 pairs (sm_100 and later: one instruction for both lanes) --
+__device__ __forceinline__ float2 sub_f32x2(float2 a, float2 b) {
+  unsigned long long ra, rb, rd;
+  asm("mov.b64 %0, {%1,%2};" : "=l"(ra) : "f"(a.x), "f"(a.y));
+  asm("mov.b64 %0, {%1,%2};" : "=l"(rb) : "f"(b.x), "f"(b.y));
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+  float2 d;
+  asm("mov.b64 {%0,%1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(rd));
+  return d;
+}
+
+// ---- bulk global -> shared copies completed on an mbarrier -----------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+  // make the initialised barrier visible to the copy engine (async proxy)
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// One arrival that also announces `bytes` of copies, then the copy of
+// `bytes` (16-byte aligned addresses, a multiple of 16 bytes) completing on it.
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes,
+                                              uint64_t *bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+// Wait for phase `parity` of the barrier, giving up after `limit` polls
+// (each poll may suspend the thread for a short while); false on give-up.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t limit) {
+  for (uint32_t it = 0; it < limit; it++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}" : "=r"(done) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    if (done) return true;
+  }
+  return false;
 }
 
 // ---- double-float arithmetic (error-free transformations) ------------------

@@ -56,6 +56,19 @@ def parse():
     ap.add_argument("--plates", type=int, default=256)
     ap.add_argument("--seq-plates", type=int, default=16,
                     help="plates timed one by one for the sequential comparison")
+    ap.add_argument("--graph", type=int, default=50,
+                    help="steps per CUDA graph in the timed FP32C run (0: launches one by one)")
+    ap.add_argument("--err-steps", type=int, default=5000,
+                    help="steps of the FP32C-vs-FP64 error run on the plate (0: skip)")
+    ap.add_argument("--es-err-steps", type=int, default=200,
+                    help="steps of the FP32C-vs-FP64 error run on the 100^3 cube (0: skip)")
+    ap.add_argument("--ens-plates", type=int, default=32,
+                    help="plates of the batched-ensemble line in the default run (0: skip)")
+    ap.add_argument("--ens-steps", type=int, default=200)
+    ap.add_argument("--qs-heldout", default="100,101",
+                    help="held-out training-geometry seeds also timed learned vs plain")
+    ap.add_argument("--cpu1-steps", type=int, default=2,
+                    help="steps of the 1-thread CPU baseline leg (0: skip)")
     ap.add_argument("--quick", action="store_true",
                     help="FP32C timed run only (profiling driver)")
     return ap.parse_args()
@@ -208,8 +221,39 @@ def profiled_traffic(decomp=1):
     return None
 
 
-def cpu_baseline(nx, steps, threads=None):
-    """The oracle (CPU restatement of FDModel<RNPBond>) on a bounded sample."""
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo) and core count."""
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.split(":")[0].strip() == "Model name":
+                name = ln.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not name:
+        try:
+            for ln in open("/proc/cpuinfo"):
+                if ln.lower().startswith("model name"):
+                    name = ln.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    return {"model": name or "unknown", "nproc": os.cpu_count()}
+
+
+# The port against the reference's own FDModel<RNPBond> sources compiled with
+# OpenMP loops (oracle/refshim), same 200 x 200 plate, same 8 x86 cores,
+# identical results: the port ran 3.4x faster (1.9e8 vs 5.5e7 bond-updates/s).
+# The reference tree is not on the GPU machine, so the refshim cannot be
+# timed there.
+PORT_OVER_REFSHIM_X86 = 3.4
+
+
+def cpu_baseline(nx, steps, threads=None, steps1=0):
+    """The oracle (CPU restatement of FDModel<RNPBond>) on a bounded sample,
+    with all host threads, and (steps1 > 0) on one thread."""
     from oracle import oracle as orc
     if threads:
         orc.set_threads(threads)
@@ -220,9 +264,25 @@ def cpu_baseline(nx, steps, threads=None):
     t0 = time.perf_counter()
     o.run(steps)
     dt = time.perf_counter() - t0
-    return {"value": nnz * steps / dt, "unit": UNIT, "cores": orc.num_threads(), "kind": "port",
-            "sample": "%d Verlet steps of the %dx%d plate (%d bonds), after 1 untimed step"
-                      % (steps, nx, nx, nnz)}
+    out = {"value": nnz * steps / dt, "unit": UNIT, "cores": orc.num_threads(), "kind": "port",
+           "sample": "%d Verlet steps of the %dx%d plate (%d bonds), after 1 untimed step"
+                     % (steps, nx, nx, nnz),
+           "cpu": cpu_model(),
+           "port_over_reference_code": {
+               "factor": PORT_OVER_REFSHIM_X86,
+               "note": "the port against the reference's own sources (refshim, OpenMP) on "
+                       "8 x86 cores of the build machine, 200 x 200 plate; the reference "
+                       "tree is not on the GPU machine, so its own code is not timed here"}}
+    if steps1 > 0:
+        nt = orc.num_threads()
+        orc.set_threads(1)
+        t0 = time.perf_counter()
+        o.run(steps1)
+        d1 = time.perf_counter() - t0
+        orc.set_threads(nt)
+        out["one_thread"] = {"value": nnz * steps1 / d1, "unit": UNIT, "cores": 1,
+                             "sample": "%d further Verlet steps of the same run" % steps1}
+    return out
 
 
 def run_reference(a):
@@ -246,6 +306,39 @@ def run_reference(a):
     return 0
 
 
+DTYPE = ("f32 bond arithmetic and force sums; u, v held as double-float f32 (hi, lo) "
+         "pairs (~48-bit significand), not f64")
+DECOMP_NAMES = {1: "thread-per-node, 4-bond groups", 2: "warp-per-node",
+                3: "thread-per-node, 1 bond/iteration",
+                4: "256-node tiles staged in shared memory",
+                5: "256-node tiles staged in shared memory, tile-frame FP32 bond data"}
+
+
+def survey_bytes(nnz, n):
+    """Compulsory bytes of one FP32C 2-D RNPBond step in the hot-path byte
+    model: 4 B neighbour id + 0.25 B bond bit read and write per directed
+    bond; x (8 B FP32 offset) + V 4 + flags 1 + rowptr 4 + u read/write 32 +
+    v read/write 32 = 81 B per node."""
+    return 4.25 * nnz + 81.0 * n
+
+
+def design_bytes(nnz, n):
+    """The same with this design's per-node arrays: the velocity-Verlet
+    half-kick reads the previous step's force, so f (2 x f32) is read and
+    written each step (16 B), and the row length (2 B) replaces the rowptr:
+    x split + V 16 + flags 1 + row length 2 + u 32 + v 32 + f 16 = 99 B."""
+    return 4.25 * nnz + 99.0 * n
+
+
+def warm_graphs(m, G):
+    """Capture both ping-pong phases' step graphs before a timed run."""
+    if G <= 0:
+        return
+    m.set_graph(G)
+    m.run(G + 1)
+    m.run(G)
+
+
 def run_ours(a):
     rank, world, local = dist_env()
     import torch
@@ -253,7 +346,7 @@ def run_ours(a):
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-    from nlmech_gb300 import abi, build, gpu
+    from nlmech_gb300 import abi, accuracy, build, gpu
     build.build()
     gpu.set_device(local)
     p = problem(a.nx, seed=rank)
@@ -265,15 +358,12 @@ def run_ours(a):
     # ---- FP32-compensated (headline) ----
     dmap = {"auto": abi.DECOMP_AUTO, "thread": abi.DECOMP_THREAD,
             "thread1": abi.DECOMP_THREAD1, "warp": abi.DECOMP_WARP, "tile": abi.DECOMP_TILE,
-               "tilel": abi.DECOMP_TILE_LOCAL}
+            "tilel": abi.DECOMP_TILE_LOCAL}
     m = gpu.FDModel(p, precision=abi.FP32C, decomposition=dmap[a.decomp])
     nnz = m.nnz()
     dcode = m.decomposition()
-    decomp = {1: "thread-per-node, 4-bond groups", 2: "warp-per-node",
-              3: "thread-per-node, 1 bond/iteration",
-              4: "256-node tiles staged in shared memory",
-              5: "256-node tiles staged in shared memory, tile-frame FP32 bond data"
-              }.get(m.decomposition(), "?")
+    decomp = DECOMP_NAMES.get(dcode, "?")
+    warm_graphs(m, a.graph)
     m.run(a.warmup)
     barrier_sync()
     with ClockSampler(local) as cs:
@@ -289,12 +379,6 @@ def run_ours(a):
                               "ms_per_step": ms / a.steps, "steps": a.steps,
                               "decomposition": decomp, "clocks": clocks}))
         return 0
-    # per-launch kernel time of the step kernel (separate timed pass)
-    m.set_timing(True)
-    m.kernel_stats(reset=True)
-    m.run(min(a.steps, 500))
-    kms, launches, bytes_per_launch = m.kernel_stats(reset=True)
-    m.set_timing(False)
     broken = m.count_broken()
     m.close()
 
@@ -308,9 +392,15 @@ def run_ours(a):
     value64 = total_bonds * a.fp64_steps / (ms64 * 1e-3)
     m64.close()
 
+    # ---- FP32C error against FP64 plain, same problem, full run ----
+    errors = None
+    if a.err_steps > 0:
+        errors = accuracy.fp32c_error(p, a.err_steps, decomposition=dcode)
+        errors["decomposition"] = DECOMP_NAMES.get(errors["decomposition"], "?")
+
     # ---- 3-D ElasticState cube (two-pass kernels), reported beside ----
     es = None
-    if a.es_steps > 0 and not a.quick:
+    if a.es_steps > 0:
         from nlmech_gb300 import configs
         pe = configs.config2(seed=rank)
         es = {"workload": "es3d_cube_100^3_d3h_verlet", "nodes": pe.n}
@@ -324,6 +414,9 @@ def run_ours(a):
             es[key] = {"value": sum_over_ranks(float(mm.nnz())) * k / (t * 1e-3), "unit": UNIT,
                        "steps": k, "ms_per_step": t / k}
             mm.close()
+        if a.es_err_steps > 0:
+            es["errors"] = accuracy.fp32c_error(pe, a.es_err_steps)
+            es["errors"]["decomposition"] = DECOMP_NAMES.get(es["errors"]["decomposition"], "?")
 
     # ---- end to end through the host-resident drop-in call ----
     # the step kernel the device-resident run used (autotuned there, or named)
@@ -343,6 +436,10 @@ def run_ours(a):
     e2e_io = me.host_io()
     me.close()
 
+    ens = None
+    if a.ens_plates > 0 and world == 1:
+        ens = ensemble_line(a.ens_plates, a.ens_steps, a.warmup, a.ens_plates)
+
     if rank != 0:
         return 0
     peaks = measured_peaks()
@@ -350,21 +447,27 @@ def run_ours(a):
         peak, peak_src = float(peaks["hbm_gbs"]), "measured"
     else:
         peak, peak_src = 6800.0, "fallback"
-    achieved = bytes_per_launch / (kms * 1e-3) / 1e9 if kms > 0 else None
+    # one step-kernel launch per step: the kernel's mean duration is the timed
+    # region's device time over its steps (CUDA events on the handle's stream)
+    kms = ms / a.steps
+    alg = survey_bytes(nnz, n)
+    achieved = alg / (kms * 1e-3) / 1e9
     traffic = profiled_traffic(dcode)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 bond math, f64 state",
+        "scaling": "weak", "vs_baseline": None, "dtype": DTYPE,
         "data": "synthetic (seeded jittered plate)",
         "config": {"workload": "rnp2d_plate_%dx%d_d3h_verlet" % (a.nx, a.nx), "nodes": n,
                    "bonds": nnz, "horizon": "3h", "dt": p.dt, "precision": "fp32c",
                    "decomposition": decomp + (" (autotuned)" if a.decomp == "auto" else ""),
+                   "graph_steps": a.graph,
                    "l2": "inputs larger than L2: %.0f MB moved per step vs 129 MB L2"
-                         % (bytes_per_launch / 1e6),
+                         % (design_bytes(nnz, n) / 1e6),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
+        "errors": errors,
         "fp64_plain": {"value": value64, "unit": UNIT, "steps": a.fp64_steps,
-                       "ms_per_step": ms64 / a.fp64_steps},
+                       "ms_per_step": ms64 / a.fp64_steps, "dtype": "f64"},
         "fp32_over_fp64": value / value64,
         "es3d": es,
         "broken_bonds_after_run": broken,
@@ -375,25 +478,34 @@ def run_ours(a):
                 .get(e2e_io, e2e_io)},
         "gpu_launches": a.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "frac": achieved / peak, "traffic": traffic,
                      "peak_source": peak_src,
                      "kernel": KERNELS.get(dcode, ("?", None))[0],
-                     "kernel_ms": kms, "bytes_per_launch": bytes_per_launch},
+                     "kernel_ms": kms, "bytes_per_launch": alg,
+                     "bytes_model": "4.25 B per directed bond + 81 B per node",
+                     "design_bytes_per_launch": design_bytes(nnz, n),
+                     "design_frac": design_bytes(nnz, n) / (kms * 1e-3) / 1e9 / peak,
+                     "dram_frac": (traffic / (kms * 1e-3) / 1e9 / peak) if traffic else None,
+                     "timing": "kernel_ms = timed region / steps (one launch per step)"},
         "clocks": clocks,
     }
-    if a.qs_steps > 0 and not a.quick:
-        out["qs_warm_start"] = qs_warm_start(a.qs_steps)
+    if ens is not None:
+        out["ensemble"] = ens
+    if a.qs_steps > 0:
+        seeds = [int(s) for s in a.qs_heldout.split(",") if s.strip()]
+        out["qs_warm_start"] = qs_warm_start(a.qs_steps, seeds)
     if not a.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(a.nx, a.cpu_steps)
+        out["cpu_baseline"] = cpu_baseline(a.nx, a.cpu_steps, steps1=a.cpu1_steps)
     print(json.dumps(out))
     return 0
 
 
-def qs_warm_start(steps):
+def qs_warm_start(steps, heldout=()):
     """Quasi-static Newton on the 200 x 200 pre-cracked RNP plate (top edge
     +1e-6 m per load step, bottom fixed, relative residual 1e-8): plain
     previous-step start vs the learned BF16 MLP start, wall time of the whole
-    load-step loop including feature building and inference."""
+    load-step loop including feature building and inference; then the same
+    on held-out training-geometry seeds."""
     from nlmech_gb300 import configs, warmstart as ws
     if not os.path.exists(ws.WEIGHTS):
         return {"unavailable": "warm-start weights not found"}
@@ -406,52 +518,74 @@ def qs_warm_start(steps):
                 "mlp": "10 -> 128 x 3 -> 2, bf16 GEMMs with fp32 accumulation",
                 "trained_on": "%d load steps of %d seeded pre-crack geometries (held out here)"
                               % (int(z["steps"]) * len(z["seeds"]), len(z["seeds"]))})
+    if heldout:
+        ps = [configs.qs_training_geometry(s) for s in heldout]
+        r = ws.evaluate(model, ps, steps, log=lambda *_: None, ablation=False)
+        res["heldout"] = {}
+        for s, q in zip(heldout, ps):
+            e = r[q.name]
+            res["heldout"]["seed%d" % s] = {
+                k: e[k] for k in ("speedup_wall", "newton_ratio", "u_rel_l2_vs_plain",
+                                  "broken_bonds_differing", "broken_bonds_plain") if k in e}
+            res["heldout"]["seed%d" % s]["plain_wall_s"] = e["plain"]["wall_s"]
+            res["heldout"]["seed%d" % s]["learned_wall_s"] = e["learned"]["wall_s"]
     return res
 
 
-def run_ensemble(a):
-    """Batched ensemble: all plates in one launch per node-count bucket, the
-    step loop replayed from CUDA graphs; against plates run one after another
-    as separate models (a sample of --seq-plates plates, scaled by bonds)."""
+def ensemble_line(nplates, steps, warmup, seq_plates, graph=20):
+    """Batched ensemble against the same plates run one after another as
+    separate autotuned models (each with its own step graphs)."""
     import torch
-    from nlmech_gb300 import abi, build, configs, gpu
-    build.build()
-    plates = configs.ensemble(nplates=a.plates, steps=a.steps)
+    from nlmech_gb300 import abi, configs, gpu
+    plates = configs.ensemble(nplates=nplates, steps=steps)
     t0 = time.perf_counter()
     b = gpu.Batch(plates)
     setup_s = time.perf_counter() - t0
     nnz = b.nnz()
-    b.set_graph(20)
-    b.run(a.warmup)
+    b.set_graph(graph)
+    b.run(graph + 1)
+    b.run(graph)
+    b.run(warmup)
     torch.cuda.synchronize()
     with ClockSampler(0) as cs:
-        ms = b.run_timed(a.steps)
+        ms = b.run_timed(steps)
     torch.cuda.synchronize()
-    value = nnz * a.steps / (ms * 1e-3)
+    value = nnz * steps / (ms * 1e-3)
     names = {1: "thread", 2: "warp", 3: "thread1", 5: "tile-frame"}
     buckets = [{"nodes": int(nd), "decomposition": names.get(dc, dc)} for nd, dc in b.buckets()]
     b.close()
-    # sequential single-plate runs (sample), each a separate model
     seq_ms, seq_bonds = 0.0, 0
-    for p in plates[:a.seq_plates]:
+    for p in plates[:seq_plates]:
         m = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_AUTO)
-        m.run(a.warmup)
-        seq_ms += m.run_timed(a.steps)
+        warm_graphs(m, graph)
+        m.run(warmup)
+        seq_ms += m.run_timed(steps)
         seq_bonds += m.nnz()
         m.close()
-    seq_value = seq_bonds * a.steps / (seq_ms * 1e-3)
-    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": a.steps,
-           "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f32 bond math, f64 state",
+    seq_value = seq_bonds * steps / (seq_ms * 1e-3)
+    return {"workload": "rnp2d_ensemble_%d_plates_5k-200k_d4h" % nplates, "plates": nplates,
+            "nodes": int(sum(p.n for p in plates)), "bonds": nnz, "steps": steps,
+            "graph_steps": graph, "buckets": buckets, "setup_s": setup_s,
+            "value": value, "unit": UNIT, "ms_per_step": ms / steps,
+            "sequential": {"value": seq_value, "unit": UNIT, "plates_timed": seq_plates,
+                           "note": "plates run one after another as separate models"},
+            "batched_over_sequential": value / seq_value, "clocks": cs.summary()}
+
+
+def run_ensemble(a):
+    """Batched ensemble line alone (--workload ensemble)."""
+    from nlmech_gb300 import build
+    build.build()
+    e = ensemble_line(a.plates, a.steps, a.warmup, a.seq_plates)
+    out = {"metric": METRIC, "value": e["value"], "unit": UNIT, "n_gpus": 1, "steps": a.steps,
+           "warmup": a.warmup, "ms_per_step": e["ms_per_step"], "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": DTYPE,
            "data": "synthetic (seeded plates)",
-           "config": {"workload": "rnp2d_ensemble_%d_plates_5k-200k_d4h" % a.plates,
-                      "plates": a.plates, "nodes": int(sum(p.n for p in plates)),
-                      "bonds": nnz, "graph_steps": 20, "buckets": buckets,
-                      "setup_s": setup_s},
-           "sequential": {"value": seq_value, "unit": UNIT, "plates_timed": a.seq_plates,
-                          "note": "plates run one after another as separate models"},
-           "batched_over_sequential": value / seq_value,
-           "clocks": cs.summary()}
+           "config": {"workload": e["workload"], "plates": e["plates"], "nodes": e["nodes"],
+                      "bonds": e["bonds"], "graph_steps": e["graph_steps"],
+                      "buckets": e["buckets"], "setup_s": e["setup_s"]},
+           "sequential": e["sequential"],
+           "batched_over_sequential": e["batched_over_sequential"], "clocks": e["clocks"]}
     print(json.dumps(out))
     return 0
 

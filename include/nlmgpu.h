@@ -246,9 +246,11 @@ int nlm_neighbor_search(int dim, int64_t n, const double *x, double horizon,
  * row are rejected with NLM_ERR_INVALID.  The per-cell counters, scatter
  * cursors and error word of the scratch must start at zero; each call clears
  * them itself before its first kernel.  Calls that overlap in time on the
- * same device (two host threads) race on that one array: serialise them.  The
- * first call on a device looks up the array's address (cudaGetSymbolAddress,
- * with that device current); make it before any stream capture on that
+ * same device (two host threads) race on that one array: serialise them.
+ * Every call looks up the array's address in the current context
+ * (cudaGetSymbolAddress, with the device current), so a device reset or a
+ * non-primary context between calls is safe; the first call on a device
+ * also loads the module, so make it before any stream capture on that
  * device.  Works on the calling thread's current device and per-thread
  * default stream, and returns after the results are on the host. */
 int nlm_neighbor_search_noalloc(int dim, int64_t n, const double *x, double horizon,
@@ -358,6 +360,14 @@ int nlm_fd_step_host(nlm_fd *h, double *u, double *v, double *f,
  * and v are left as the caller had them either way (the reference's 2-D
  * integrator never writes them) and f's z is written as 0. */
 int nlm_fd_host_io(const nlm_fd *h, int *mode);
+/* Cap the device memory the handle may allocate from this call on at
+ * `bytes` (memory it frees again counts back; bytes < 0 removes the cap).
+ * Buffers a path allocates lazily -- the banded host step's staging, the
+ * in-place path's staging, post-processing outputs -- then fail with
+ * NLM_ERR_OOM past the cap; the banded host step falls back to the in-place
+ * path, with the same results.  No reference counterpart (the reference
+ * allocates on the host only). */
+int nlm_fd_set_alloc_limit(nlm_fd *h, int64_t bytes);
 /* nlm_fd_run bracketed by CUDA events on the handle's stream; *ms is the
  * device time of the whole run (the stream is synchronized). */
 int nlm_fd_run_timed(nlm_fd *h, int64_t nsteps, double *ms);

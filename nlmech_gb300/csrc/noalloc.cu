@@ -28,7 +28,6 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
-#include <mutex>
 #include <string>
 
 #include "../../include/nlmgpu.h"
@@ -47,7 +46,6 @@ namespace {
 constexpr int64_t kNAMaxNodes = 65536;
 constexpr int64_t kNAMaxCells = 262144;
 constexpr int64_t kNAMaxBonds = 4194304;
-constexpr int kNAMaxDevices = 64;
 
 constexpr size_t na_round(size_t b) { return (b + 255) / 256 * 256; }
 // byte offsets of the regions of the scratch array
@@ -180,9 +178,6 @@ int na_fail(int code, const char *msg) {
   return code;
 }
 
-std::mutex g_na_mu;
-void *g_na_base[kNAMaxDevices] = {};
-
 }  // namespace
 
 extern "C" int nlm_neighbor_search_noalloc(int dim, int64_t n, const double *x, double horizon,
@@ -204,21 +199,16 @@ extern "C" int nlm_neighbor_search_noalloc(int dim, int64_t n, const double *x, 
                    "(static scratch limit)");
   const int64_t ncell = g.nc[0] * g.nc[1] * g.nc[2];
 
-  // scratch address of the current device, looked up once per device
-  int dev = 0;
-  NLM_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kNAMaxDevices)
-    return na_fail(NLM_ERR_INVALID, "nlm_neighbor_search_noalloc: device ordinal >= 64");
+  // the scratch array's device address in the current context, looked up on
+  // every call: a cached address would go stale after a device reset or in
+  // another context of the same device, where the module is loaded anew.
+  // Once the module is loaded the lookup allocates nothing.
   unsigned char *base = nullptr;
   {
-    std::lock_guard<std::mutex> lk(g_na_mu);
-    if (!g_na_base[dev]) {
-      void *p = nullptr;
-      const cudaError_t e = cudaGetSymbolAddress(&p, g_na_scratch);
-      if (e != cudaSuccess) return nlm::cuda_fail(e, "cudaGetSymbolAddress(scratch)");
-      g_na_base[dev] = p;
-    }
-    base = static_cast<unsigned char *>(g_na_base[dev]);
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_na_scratch);
+    if (e != cudaSuccess) return nlm::cuda_fail(e, "cudaGetSymbolAddress(scratch)");
+    base = static_cast<unsigned char *>(p);
   }
   double *dx = reinterpret_cast<double *>(base + kOffX);
   int *cellof = reinterpret_cast<int *>(base + kOffCellOf);

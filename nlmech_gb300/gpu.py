@@ -174,6 +174,10 @@ class FDModel:
         _check(load().nlm_fd_host_io(self.h, C.byref(m)))
         return m.value
 
+    def set_alloc_limit(self, nbytes):
+        """Cap the device bytes the handle may still allocate (< 0: no cap)."""
+        _check(load().nlm_fd_set_alloc_limit(self.h, C.c_int64(int(nbytes))))
+
     def run_timed(self, nsteps):
         """Run nsteps; returns the device time in ms (CUDA events on the
         handle's stream)."""

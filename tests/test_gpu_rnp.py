@@ -297,6 +297,34 @@ def test_checkpoint_restart_continues_the_run(gpu, tmp_path):
         q.load(path)
 
 
+def test_checkpoint_with_nonfinite_state_leaves_model_unchanged(gpu, tmp_path):
+    """A checkpoint whose state holds a NaN is refused before the handle
+    changes: time, step, bond state and u stay those of the running model,
+    and a sound checkpoint loads afterwards."""
+    p = configs.rnp_plate(48, 1e-3, 3, 0.012, 0.5, 2e-8, 300, seed=7)
+    a = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_THREAD)
+    a.run(150)
+    good = tmp_path / "good.bin"
+    a.save(good)
+    raw = bytearray(good.read_bytes())
+    header = 72  # CkptHeader: magic, 5 int32, uint32, 3 int64, 2 doubles
+    raw[header + 8 * 16: header + 8 * 17] = np.array([np.nan]).tobytes()  # u of node 5, y
+    bad = tmp_path / "bad.bin"
+    bad.write_bytes(bytes(raw))
+    b = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_THREAD)
+    b.run(20)
+    t0, bonds0, u0 = b.time(), b.bond_state(), b.state()[0]
+    with pytest.raises(gpu.NLMError) as e:
+        b.load(bad)
+    assert e.value.code == 7  # NLM_ERR_NONFINITE
+    assert b.time() == t0
+    assert np.array_equal(b.bond_state(), bonds0)
+    assert np.array_equal(b.state()[0], u0)
+    b.load(good)
+    assert b.time() == a.time()
+    assert np.array_equal(b.bond_state(), a.bond_state())
+
+
 def test_write_vtu_output_step(gpu, tmp_path):
     from nlmech_gb300 import vtu
     p = configs.rnp_plate(30, 1e-3, 3, 0.008, 0.3, 2e-8, 50, seed=2)
@@ -481,6 +509,35 @@ def test_step_host_banded_matches_copies(gpu, nx, shuffle):
     a.run(3)
     b.run(3)
     assert np.array_equal(a.state()[0], b.state()[0])
+
+
+def test_step_host_banded_falls_back_when_buffers_fail(gpu):
+    """With the handle's device allocations capped below what the banded
+    path stages (about 200 bytes per node) but above what the in-place path
+    needs (about 70), the first banded call frees what it had set up and the
+    in-place path serves it and every later call: results equal the copy
+    path bit for bit and no error text is left behind."""
+    torch = pytest.importorskip("torch")
+    p = configs.rnp_plate(300, 1e-4, 3, 0.006, 50.0, 2e-9, 50, seed=4)
+    n = p.n
+    a = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_TILE_LOCAL)
+    b = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_TILE_LOCAL)
+    host = [np.zeros((n, 3)) for _ in range(3)]
+    host[0][:, 2] = 7.0
+    host[1][:, 2] = -3.0
+    pin, ptrs = _pinned_state(torch, n)
+    a.step_host(*host, nsteps=1)
+    b.step_host_ptr(*ptrs, nsteps=1)
+    b.set_alloc_limit(80 * n + 4096)
+    for _ in range(6):
+        a.step_host(*host, nsteps=1)
+        b.step_host_ptr(*ptrs, nsteps=1)
+        assert a.host_io() == 0 and b.host_io() == 1
+    assert gpu.load().nlm_last_error() == b""
+    for x, y in zip(host, pin):
+        assert np.array_equal(x, y.numpy())
+    assert np.array_equal(a.bond_state(), b.bond_state())
+    b.set_alloc_limit(-1)
 
 
 def test_step_host_banded_rejects_nonfinite(gpu):

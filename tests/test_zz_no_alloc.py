@@ -74,6 +74,19 @@ def test_noalloc_empty_and_limits(gpu):
     rc, _, _ = _call(L, "nlm_neighbor_search_noalloc", x, 1e-3, 2)
     assert rc == NLM_ERR_INVALID
     assert b"262144" in L.nlm_last_error()
+    # more than 4,194,304 bonds from at most 65,536 nodes (about 73 per row):
+    # found after the counting pass, before any bond is written
+    x3, _ = configs.grid3d(40, 40, 40, 1e-3, seed=8)
+    rc, _, _ = _call(L, "nlm_neighbor_search_noalloc", x3, 2.6e-3, 3)
+    assert rc == NLM_ERR_INVALID
+    assert b"4194304" in L.nlm_last_error()
+    # a cluster of 600 nodes inside one horizon: rows of 599 entries
+    rng = np.random.default_rng(10)
+    xc = np.zeros((600, 3))
+    xc[:, :2] = rng.uniform(0, 1e-4, size=(600, 2))
+    rc, _, _ = _call(L, "nlm_neighbor_search_noalloc", xc, 1e-3, 2)
+    assert rc == NLM_ERR_INVALID
+    assert b"512" in L.nlm_last_error()
     # the next call in range still works after the rejections
     x2, _ = configs.grid2d(40, 30, 1e-3, seed=9)
     rc, rp_ref, cc_ref = _call(L, "nlm_neighbor_search", x2, 3e-3, 2)

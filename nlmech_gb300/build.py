@@ -23,6 +23,12 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 # translation unit -> extra flags
 UNITS = {
     "fd_host.cu": [],
+    "host_common.cu": [],
+    "fd_kernels.cu": [],
+    "host_io.cu": [],
+    "batch_host.cu": [],
+    "qs_host.cu": [],
+    "esqs_host.cu": [],
     "neighbor.cu": ["--fmad=false"],
     "fd_fp64.cu": ["--fmad=false"],
     "fd_fp32.cu": [],

@@ -1,0 +1,128 @@
+// tile_store.h -- building the tile store of the tile decompositions (one
+// model or a batch's combined layout).
+#pragma once
+
+#include "fd_handle.h"
+
+namespace nlm {
+
+// Tile store of NLM_DECOMP_TILE (FP32C, 2-D): tile t = internal nodes
+// [256 t, 256 t + 256); its halo = the nodes outside the tile its rows
+// reach, ascending.  Each bond stores its neighbour's index in the tile's
+// staged list (tile nodes 0..255, halo from 256), in the sliced layout of
+// sell_cols; padding entries point at the row's own node.  If some tile needs
+// more than kTileMaxLocal staged nodes the store is not built.  The 2-D
+// RNPBond store (max_local == kTileMaxLocal) also gets the byte-offset copy
+// tile_boff (16 x index).
+// What a tile store is built from (one model or a batch's combined layout).
+struct TileInputs {
+  int64_t n, nnz, nslices, sell_entries;
+  const int *cols_dev;                 // internal column ids, CSR order
+  const int64_t *sell_ptr_dev;         // sliced-store offsets
+  const std::vector<int64_t> *rowptr;  // host CSR offsets
+  const std::vector<int> *perm;        // internal -> caller id (for tile_need), or null
+  int max_local;                       // largest staged list allowed
+};
+
+template <class H>
+int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *need_out) {
+  const int64_t n = in.n, nt = (n + kTileNodes - 1) / kTileNodes;
+  const int max_local = in.max_local;
+  ok = false;
+  std::vector<int> cols(in.nnz);
+  std::vector<int64_t> sptr(in.nslices + 1);
+  NLM_CUDA(cudaMemcpyAsync(cols.data(), in.cols_dev, sizeof(int) * in.nnz, cudaMemcpyDeviceToHost,
+                           h->stream));
+  NLM_CUDA(cudaMemcpyAsync(sptr.data(), in.sell_ptr_dev, sizeof(int64_t) * (in.nslices + 1),
+                           cudaMemcpyDeviceToHost, h->stream));
+  NLM_CUDA(cudaStreamSynchronize(h->stream));
+  const std::vector<int64_t> &rp = *in.rowptr;
+  std::vector<std::vector<int>> halo(nt);
+  const bool boff_too = max_local == kTileMaxLocal;
+  std::vector<uint16_t> lidx(in.sell_entries + 4, 0);
+  std::vector<uint16_t> boff(boff_too ? in.sell_entries + 4 : 0, 0);
+  std::vector<int> too_big(1, 0);
+  std::vector<int> need(nt, -1);
+  unsigned nthr = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  auto work = [&](unsigned w) {
+    for (int64_t t = w; t < nt; t += nthr) {
+      const int64_t a = t * kTileNodes, b = std::min(n, a + kTileNodes);
+      std::vector<int> &hl = halo[t];
+      for (int64_t q = rp[a]; q < rp[b]; q++)
+        if (cols[q] < a || cols[q] >= b) hl.push_back(cols[q]);
+      std::sort(hl.begin(), hl.end());
+      hl.erase(std::unique(hl.begin(), hl.end()), hl.end());
+      if (kTileNodes + (int64_t)hl.size() > max_local) {
+        too_big[0] = 1;
+        continue;
+      }
+      if (in.perm) {
+        int m = -1;
+        for (int64_t i = a; i < b; i++) m = std::max(m, (*in.perm)[i]);
+        for (int j : hl) m = std::max(m, (*in.perm)[j]);
+        need[t] = m;
+      }
+      for (int64_t i = a; i < b; i++) {
+        const int64_t base = sptr[i >> 5] + 4 * (i & 31);
+        const int64_t len = rp[i + 1] - rp[i];
+        const int64_t wdt = (sptr[(i >> 5) + 1] - sptr[i >> 5]) / 32;
+        for (int64_t k = 0; k < wdt; k++) {
+          int loc = (int)(i - a);
+          if (k < len) {
+            const int j = cols[rp[i] + k];
+            loc = (j >= a && j < b) ? (int)(j - a)
+                                    : kTileNodes + (int)(std::lower_bound(hl.begin(), hl.end(), j) -
+                                                         hl.begin());
+          }
+          lidx[base + (k >> 2) * 128 + (k & 3)] = (uint16_t)loc;
+          if (boff_too) boff[base + (k >> 2) * 128 + (k & 3)] = (uint16_t)(16 * loc);
+        }
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (unsigned w = 0; w < nthr; w++) pool.emplace_back(work, w);
+  for (auto &th : pool) th.join();
+  if (too_big[0]) return NLM_OK;
+  // id block of a tile: its 8 slices, contiguous in the sliced layout
+  int64_t ids_max = 0;
+  for (int64_t t = 0; t < nt; t++) {
+    const int64_t s0 = 8 * t, s1 = std::min<int64_t>(8 * t + 8, in.nslices);
+    ids_max = std::max(ids_max, 2 * (sptr[s1] - sptr[s0]));
+  }
+  if (boff_too && ids_max > kTileIdsMaxBytes) return NLM_OK;
+  std::vector<int> hptr(nt + 1, 0);
+  size_t nmax = 0;
+  for (int64_t t = 0; t < nt; t++) {
+    hptr[t + 1] = hptr[t] + (int)halo[t].size();
+    nmax = std::max(nmax, halo[t].size());
+  }
+  std::vector<int> hall(std::max(1, hptr[nt]));
+  for (int64_t t = 0; t < nt; t++) std::copy(halo[t].begin(), halo[t].end(), hall.begin() + hptr[t]);
+  uint16_t *d_l = nullptr;
+  int *d_hp = nullptr, *d_h = nullptr;
+  NLM_CUDA(h->alloc(&d_l, lidx.size()));
+  NLM_CUDA(h->alloc(&d_hp, hptr.size()));
+  NLM_CUDA(h->alloc(&d_h, hall.size()));
+  NLM_CUDA(cudaMemcpyAsync(d_l, lidx.data(), sizeof(uint16_t) * lidx.size(), cudaMemcpyHostToDevice, h->stream));
+  NLM_CUDA(cudaMemcpyAsync(d_hp, hptr.data(), sizeof(int) * hptr.size(), cudaMemcpyHostToDevice, h->stream));
+  NLM_CUDA(cudaMemcpyAsync(d_h, hall.data(), sizeof(int) * hall.size(), cudaMemcpyHostToDevice, h->stream));
+  uint16_t *d_b = nullptr;
+  if (boff_too) {
+    NLM_CUDA(h->alloc(&d_b, boff.size()));
+    NLM_CUDA(cudaMemcpyAsync(d_b, boff.data(), sizeof(uint16_t) * boff.size(),
+                             cudaMemcpyHostToDevice, h->stream));
+  }
+  NLM_CUDA(cudaStreamSynchronize(h->stream));
+  h->D.tile_lidx = d_l;
+  h->D.tile_boff = d_b;
+  h->D.tile_ids_bytes = (int)ids_max;
+  h->D.tile_hptr = d_hp;
+  h->D.tile_halo = d_h;
+  h->D.tile_nmax = kTileNodes + (int)nmax;
+  ok = true;
+  if (need_out) *need_out = std::move(need);
+  return NLM_OK;
+}
+
+}  // namespace nlm

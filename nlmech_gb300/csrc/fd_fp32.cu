@@ -485,8 +485,10 @@ __device__ __forceinline__ void tilel_node(const StepParams &P, const Params32 &
   }
   if (FAST && !full) {
     float mx = 0.f;  // largest S^2 r of the row
+    uint2 nxt = ng > 0 ? sb[0] : make_uint2(0u, 0u);  // ids one group ahead
     for (int g = 0; g < ng; g++) {
-      const uint2 cur = sb[32 * g];
+      const uint2 cur = nxt;
+      if (g + 1 < ng) nxt = sb[32 * (g + 1)];
       const uint32_t o[4] = {cur.x & 0xffffu, cur.x >> 16, cur.y & 0xffffu, cur.y >> 16};
       float2 d[4], e[4];
       float vj[4];
@@ -608,7 +610,9 @@ __global__ void __launch_bounds__(kTileNodes, 4)
   const int len = own ? D.rowlen[i] : 0;
   const int64_t rbase = own ? D.sell_ptr[i >> 5] : ib0;
   const uint32_t word = (NW1 && own) ? D.bits[i] : 0u;
-  const float4 ui4 = own ? ucur[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 ui4 = il < nt ? __ldg(ucur + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 pown = il < nt ? __ldg(D.pos32 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+  const uint8_t fown = ((OPT & OPT_NOFAIL) && il < nt) ? D.flags[i] : 0;
   if (own) {
     // the integrator's velocity and force reads, brought into L1 early
     const float4 *vp = D.v32[SCHEME == NLM_VELOCITY_VERLET ? 0 : A.cur] + i;
@@ -616,20 +620,41 @@ __global__ void __launch_bounds__(kTileNodes, 4)
     asm volatile("prefetch.global.L1 [%0];" ::"l"(vp));
     asm volatile("prefetch.global.L1 [%0];" ::"l"(fp));
   }
+  // Staging: the thread's own tile node was loaded with the early loads
+  // above; halo entries come two per thread per round, their ids loaded
+  // together and then their nodes together, so a thread waits for memory
+  // twice per round rather than twice per staged node.
   float span = 0.f;  // largest |u - u_o| staged by this thread
-  for (int e = threadIdx.x; e < kTileNodes + nh; e += blockDim.x) {
-    if (e < kTileNodes && e >= nt) continue;
-    const int64_t g = e < kTileNodes ? t0 + e : (int64_t)D.tile_halo[h0 + e - kTileNodes];
-    const float4 a = __ldg(D.pos32 + g);
+  auto stage = [&](int e, const float4 a, const float4 u, uint8_t f) {
     const float2 lo = __half22float2(*reinterpret_cast<const __half2 *>(&a.w));
-    const float4 u = ucur[g];
     const float dux = (u.x - uo.x) + (u.z - uo.z), duy = (u.y - uo.y) + (u.w - uo.w);
     span = fmaxf(span, fmaxf(fabsf(dux), fabsf(duy)));
     s_xu[e] = make_float4(fmaf(lo.x - plo.x, Q.inv_lo, a.x - po.x),
                           fmaf(lo.y - plo.y, Q.inv_lo, a.y - po.y), dux, duy);
     if (!UV) s_vol[e] = KV ? Q.K1 * a.z : a.z;
-    if (OPT & OPT_NOFAIL) s_fl[e] = D.flags[g];
+    if (OPT & OPT_NOFAIL) s_fl[e] = f;
+  };
+  for (int base = 0; base < nh; base += 2 * kTileNodes) {
+    int g[2];
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      const int e = base + il + q * kTileNodes;
+      g[q] = e < nh ? __ldg(D.tile_halo + h0 + e) : -1;
+    }
+    float4 a[2], u[2];
+    uint8_t f[2] = {0, 0};
+#pragma unroll
+    for (int q = 0; q < 2; q++)
+      if (g[q] >= 0) {
+        a[q] = __ldg(D.pos32 + g[q]);
+        u[q] = __ldg(ucur + g[q]);
+        if (OPT & OPT_NOFAIL) f[q] = D.flags[g[q]];
+      }
+#pragma unroll
+    for (int q = 0; q < 2; q++)
+      if (g[q] >= 0) stage(kTileNodes + base + il + q * kTileNodes, a[q], u[q], f[q]);
   }
+  if (il < nt) stage(il, pown, ui4, fown);
   // the tile's displacement span (NaN counts as too large)
   for (int o = 16; o > 0; o >>= 1) span = fmaxf(span, __shfl_xor_sync(0xffffffffu, span, o));
   if ((threadIdx.x & 31) == 0) s_wspan[threadIdx.x >> 5] = span != span ? 3e38f : span;

@@ -70,6 +70,17 @@ struct nlm_batch {
 namespace {
 
 int batch_launch(nlm_batch *b, StepArgs a) {
+  // every bucket on the tile-frame kernel: one launch over all of them (its
+  // tiles take each node's own specimen constants, and a tile that straddles
+  // two buckets is staged once instead of once per bucket)
+  bool all_tile = !b->buckets.empty();
+  for (const auto &bk : b->buckets) all_tile = all_tile && bk.decomp == NLM_DECOMP_TILE_LOCAL;
+  if (all_tile) {
+    a.i0 = b->buckets.front().i0;
+    a.i1 = b->buckets.back().i1;
+    cudaError_t e = launch_rnp_step_fp32(b->P, b->D, b->T, a, NLM_DECOMP_TILE_LOCAL, b->stream);
+    return e == cudaSuccess ? NLM_OK : cuda_fail(e, "batched step launch");
+  }
   for (const auto &bk : b->buckets) {
     a.i0 = bk.i0;
     a.i1 = bk.i1;

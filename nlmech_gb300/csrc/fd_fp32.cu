@@ -300,6 +300,7 @@ __global__ void __launch_bounds__(kTileNodes, 3)
   for (int e = threadIdx.x; e < kTileNodes + nh; e += blockDim.x) {
     if (e < kTileNodes && e >= nt) continue;
     const int64_t g = e < kTileNodes ? t0 + e : (int64_t)D.tile_halo[h0 + e - kTileNodes];
+    if (g < 0) continue;  // an empty slot of a lattice-ordered halo
     s_pos[e] = __ldg(D.pos32 + g);
     s_u[e] = ucur[g];
     if (OPT & OPT_NOFAIL) s_fl[e] = D.flags[g];
@@ -668,6 +669,7 @@ __global__ void __launch_bounds__(kTileNodes, 4)
     for (int e = threadIdx.x; e < kTileNodes + nh; e += blockDim.x) {
       if (e < kTileNodes && e >= nt) continue;
       const int64_t g = e < kTileNodes ? t0 + e : (int64_t)D.tile_halo[h0 + e - kTileNodes];
+      if (g < 0) continue;  // an empty slot of a lattice-ordered halo
       const float4 u = ucur[g];
       s_xu[e].z = u.x;
       s_xu[e].w = u.y;

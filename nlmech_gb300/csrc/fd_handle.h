@@ -123,6 +123,9 @@ struct nlm_fd {
   DevPtrs D{};
   int64_t nslices = 0, sell_entries = 0;
   bool tile_ok = false;  // tile store built (NLM_DECOMP_TILE available)
+  // lattice residue (g_x mod 4, g_y mod 2 as a Morton code) of each node of
+  // a lattice-renumbered model, for the tile store's halo slots
+  std::vector<uint8_t> lattice_res;
   // host copies
   std::vector<int> perm;    // internal -> original
   std::vector<int64_t> rowptr;  // internal CSR offsets (host copy)

@@ -189,6 +189,103 @@ int rnp_constants(const nlm_material &m, int dim, double delta, StepParams &P) {
   return NLM_OK;
 }
 
+// Lattice renumbering of an FP32C 2-D RNPBond model (after the neighbour
+// build, which orders nodes by the Morton code of their search cell, edge
+// >= horizon).  Nodes are renumbered by the Morton code of their cell on the
+// mesh lattice (edge h, g = floor((x - lo) / h + 1/2)): consecutive nodes then
+// form 4 x 2, 8 x 4, 16 x 16 ... patches of a grid-like mesh, and a 256-node
+// tile is a 16 x 16 patch.  Each row is ordered by the lattice offset of its
+// neighbour (|offset|^2, then angle; ties by node): in the interior the k-th
+// neighbours of eight consecutive nodes are then the same offset from each of
+// them, a shifted 4 x 2 patch whose Morton residues (g_x mod 4, g_y mod 2) are
+// all different, which is what the tile kernel's shared-memory layout needs
+// to read the eight records of a quarter warp in one pass.  Any node set
+// works (the order is only a layout); only results' rounding changes.
+// lres receives each node's residue (new order) for the tile store.
+int lattice_relabel(nlm_fd *h, NeighborBuild &nb, int S, double mesh_h, cudaStream_t s,
+                    std::vector<uint8_t> &lres) {
+  const int64_t n = nb.n, nnz = nb.nnz;
+  if (n == 0) return NLM_OK;
+  std::vector<int> perm(n), cols(nnz);
+  std::vector<double> pos((size_t)S * n);
+  std::vector<int64_t> rp(n + 1);
+  NLM_CUDA(cudaMemcpyAsync(perm.data(), nb.perm, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  NLM_CUDA(cudaMemcpyAsync(pos.data(), nb.pos, sizeof(double) * S * n, cudaMemcpyDeviceToHost, s));
+  NLM_CUDA(cudaMemcpyAsync(rp.data(), nb.rowptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, s));
+  if (nnz) NLM_CUDA(cudaMemcpyAsync(cols.data(), nb.cols, sizeof(int) * nnz, cudaMemcpyDeviceToHost, s));
+  NLM_CUDA(cudaStreamSynchronize(s));
+  double lo[2] = {1e300, 1e300};
+  for (int64_t i = 0; i < n; i++)
+    for (int d = 0; d < 2; d++) lo[d] = std::min(lo[d], pos[(size_t)S * i + d]);
+  std::vector<int64_t> gx(n), gy(n);
+  std::vector<std::pair<uint64_t, int64_t>> key(n);
+  auto spread = [](uint64_t v) {
+    uint64_t r = 0;
+    for (int b = 0; b < 32; b++) r |= ((v >> b) & 1ull) << (2 * b);
+    return r;
+  };
+  for (int64_t i = 0; i < n; i++) {
+    gx[i] = (int64_t)std::floor((pos[(size_t)S * i] - lo[0]) / mesh_h + 0.5);
+    gy[i] = (int64_t)std::floor((pos[(size_t)S * i + 1] - lo[1]) / mesh_h + 0.5);
+    const uint64_t cx = (uint64_t)std::max<int64_t>(0, std::min<int64_t>(gx[i], 0xffffffffll));
+    const uint64_t cy = (uint64_t)std::max<int64_t>(0, std::min<int64_t>(gy[i], 0xffffffffll));
+    key[i] = {spread(cx) | (spread(cy) << 1), i};
+  }
+  std::sort(key.begin(), key.end());  // ties keep the search-cell order
+  std::vector<int64_t> order(n), inv(n);
+  for (int64_t k = 0; k < n; k++) {
+    order[k] = key[k].second;
+    inv[key[k].second] = k;
+  }
+  // rank of a lattice offset: |o|^2, then angle
+  const int R = (int)std::ceil(h->P.delta / mesh_h) + 2, W = 2 * R + 1;
+  std::vector<std::pair<std::pair<int, double>, int>> offs;
+  for (int oy = -R; oy <= R; oy++)
+    for (int ox = -R; ox <= R; ox++)
+      offs.push_back({{ox * ox + oy * oy, std::atan2((double)oy, (double)ox)}, (oy + R) * W + ox + R});
+  std::sort(offs.begin(), offs.end());
+  std::vector<int> orank(W * W);
+  for (size_t k = 0; k < offs.size(); k++) orank[offs[k].second] = (int)k;
+  std::vector<int> perm2(n), cols2(nnz);
+  std::vector<double> pos2((size_t)S * n);
+  std::vector<int64_t> rp2(n + 1, 0);
+  lres.assign(n, 0);
+  for (int64_t k = 0; k < n; k++) {
+    const int64_t o = order[k];
+    perm2[k] = perm[o];
+    for (int d = 0; d < S; d++) pos2[(size_t)S * k + d] = pos[(size_t)S * o + d];
+    rp2[k + 1] = rp2[k] + (rp[o + 1] - rp[o]);
+    lres[k] = (uint8_t)((gx[o] & 1) | ((gy[o] & 1) << 1) | ((gx[o] & 2) << 1));
+  }
+  unsigned nthr = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  auto work = [&](unsigned w) {
+    std::vector<std::pair<int64_t, int>> row;
+    for (int64_t k = w; k < n; k += nthr) {
+      const int64_t o = order[k];
+      row.clear();
+      for (int64_t q = rp[o]; q < rp[o + 1]; q++) {
+        const int64_t jo = cols[q];
+        const int64_t ox = gx[jo] - gx[o], oy = gy[jo] - gy[o];
+        const int64_t rk = (ox >= -R && ox <= R && oy >= -R && oy <= R)
+                               ? orank[(oy + R) * W + ox + R]
+                               : (int64_t)W * W + ox * ox + oy * oy;
+        row.push_back({rk * (int64_t)n + inv[jo], (int)inv[jo]});
+      }
+      std::sort(row.begin(), row.end());
+      for (size_t q = 0; q < row.size(); q++) cols2[rp2[k] + (int64_t)q] = row[q].second;
+    }
+  };
+  std::vector<std::thread> pool;
+  for (unsigned w = 0; w < nthr; w++) pool.emplace_back(work, w);
+  for (auto &th : pool) th.join();
+  NLM_CUDA(cudaMemcpyAsync(nb.perm, perm2.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  NLM_CUDA(cudaMemcpyAsync(nb.pos, pos2.data(), sizeof(double) * S * n, cudaMemcpyHostToDevice, s));
+  NLM_CUDA(cudaMemcpyAsync(nb.rowptr, rp2.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s));
+  if (nnz) NLM_CUDA(cudaMemcpyAsync(nb.cols, cols2.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
+  NLM_CUDA(cudaStreamSynchronize(s));
+  return NLM_OK;
+}
+
 int launch_step(nlm_fd *h, const StepArgs &a0) {
   StepArgs a = a0;
   if (a.i1 == 0) a.i1 = h->n;
@@ -221,7 +318,8 @@ int launch_step(nlm_fd *h, const StepArgs &a0) {
 
 int build_tiles(nlm_fd *h, const int64_t *sell_ptr_dev, int max_local) {
   TileInputs in{h->n, h->nnz, h->nslices, h->sell_entries, h->D.cols, sell_ptr_dev,
-                &h->rowptr, &h->perm, max_local};
+                &h->rowptr, &h->perm, max_local,
+                h->lattice_res.empty() ? nullptr : &h->lattice_res};
   return build_tile_store(h, in, h->tile_ok, &h->tile_need);
 }
 
@@ -629,6 +727,10 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
     return bail(why.empty() ? cuda_fail(e, "neighbour build") : fail(NLM_ERR_INVALID, why));
   h->nnz = nb.nnz;
   if (h->nnz > INT32_MAX) return bail(fail(NLM_ERR_INVALID, "too many bonds for one handle"));
+  if (tile_able && !es_model && d->mesh_size > 0.) {
+    int rc_l = lattice_relabel(h, nb, S, d->mesh_size, s, h->lattice_res);
+    if (rc_l) return bail(rc_l);
+  }
   SellStore st;
   e = build_sell(n, nb.rowptr, nb.cols, st, s);
   for (void *p : {(void *)st.ptr, (void *)st.width, (void *)st.cols})

@@ -13,7 +13,12 @@ namespace nlm {
 // sell_cols; padding entries point at the row's own node.  If some tile needs
 // more than kTileMaxLocal staged nodes the store is not built.  The 2-D
 // RNPBond store (max_local == kTileMaxLocal) also gets the byte-offset copy
-// tile_boff (16 x index).
+// tile_boff (16 x index).  With lattice residues (lres: a lattice-renumbered
+// model) the halo is laid out by residue: halo node j takes staged slot
+// 256 + 8 m + res(j) (m counting the tile's halo nodes of that residue), so
+// that eight neighbours of one lattice offset from a quarter warp's 4 x 2
+// patch land in eight different 16-byte bank groups; the slots left empty
+// hold -1 in the halo list and are skipped by the staging.
 // What a tile store is built from (one model or a batch's combined layout).
 struct TileInputs {
   int64_t n, nnz, nslices, sell_entries;
@@ -22,6 +27,7 @@ struct TileInputs {
   const std::vector<int64_t> *rowptr;  // host CSR offsets
   const std::vector<int> *perm;        // internal -> caller id (for tile_need), or null
   int max_local;                       // largest staged list allowed
+  const std::vector<uint8_t> *lres = nullptr;  // lattice residues per node, or null
 };
 
 template <class H>
@@ -43,6 +49,7 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
   std::vector<uint16_t> boff(boff_too ? in.sell_entries + 4 : 0, 0);
   std::vector<int> too_big(1, 0);
   std::vector<int> need(nt, -1);
+  std::vector<std::vector<int>> halo_slots(nt);  // lattice layout: halo by slot, -1 = empty
   unsigned nthr = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
   auto work = [&](unsigned w) {
     for (int64_t t = w; t < nt; t += nthr) {
@@ -52,15 +59,34 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
         if (cols[q] < a || cols[q] >= b) hl.push_back(cols[q]);
       std::sort(hl.begin(), hl.end());
       hl.erase(std::unique(hl.begin(), hl.end()), hl.end());
-      if (kTileNodes + (int64_t)hl.size() > max_local) {
-        too_big[0] = 1;
-        continue;
-      }
       if (in.perm) {
         int m = -1;
         for (int64_t i = a; i < b; i++) m = std::max(m, (*in.perm)[i]);
         for (int j : hl) m = std::max(m, (*in.perm)[j]);
         need[t] = m;
+      }
+      // staged slot (from kTileNodes) of each halo node, in hl's order
+      std::vector<int> hslot(hl.size());
+      for (size_t k = 0; k < hl.size(); k++) hslot[k] = (int)k;
+      if (in.lres && boff_too) {
+        int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (size_t k = 0; k < hl.size(); k++) {
+          const int r = (*in.lres)[hl[k]] & 7;
+          hslot[k] = 8 * cnt[r]++ + r;
+        }
+        int m = 0;
+        for (int r = 0; r < 8; r++) m = std::max(m, cnt[r]);
+        std::vector<int> bys(8 * (size_t)m, -1);
+        for (size_t k = 0; k < hl.size(); k++) bys[hslot[k]] = hl[k];
+        // the sorted list is needed below for lookups: keep it, store the
+        // slot-ordered one after the rows are written
+        halo_slots[t] = std::move(bys);
+      }
+      const int64_t nstaged = in.lres && boff_too ? (int64_t)halo_slots[t].size()
+                                                   : (int64_t)hl.size();
+      if (kTileNodes + nstaged > max_local) {
+        too_big[0] = 1;
+        continue;
       }
       for (int64_t i = a; i < b; i++) {
         const int64_t base = sptr[i >> 5] + 4 * (i & 31);
@@ -70,9 +96,9 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
           int loc = (int)(i - a);
           if (k < len) {
             const int j = cols[rp[i] + k];
-            loc = (j >= a && j < b) ? (int)(j - a)
-                                    : kTileNodes + (int)(std::lower_bound(hl.begin(), hl.end(), j) -
-                                                         hl.begin());
+            loc = (j >= a && j < b)
+                      ? (int)(j - a)
+                      : kTileNodes + hslot[std::lower_bound(hl.begin(), hl.end(), j) - hl.begin()];
           }
           lidx[base + (k >> 2) * 128 + (k & 3)] = (uint16_t)loc;
           if (boff_too) boff[base + (k >> 2) * 128 + (k & 3)] = (uint16_t)(16 * loc);
@@ -91,6 +117,8 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
     ids_max = std::max(ids_max, 2 * (sptr[s1] - sptr[s0]));
   }
   if (boff_too && ids_max > kTileIdsMaxBytes) return NLM_OK;
+  if (in.lres && boff_too)
+    for (int64_t t = 0; t < nt; t++) halo[t] = std::move(halo_slots[t]);
   std::vector<int> hptr(nt + 1, 0);
   size_t nmax = 0;
   for (int64_t t = 0; t < nt; t++) {

@@ -423,6 +423,16 @@ typedef struct nlm_qs_params {
   double guess_accept; /* a guess is used only if its linearised residual is
                           at most guess_accept times that of the plain
                           start (<= 0: 0.1)                                  */
+  int krylov_launch;   /* 0: the FP32 Krylov solve of a Newton step in one
+                          cooperative launch (grid barriers between its
+                          phases) where the device allows it; 1: two launches
+                          per iteration                                      */
+  double wait_limit_s; /* bound of each grid-barrier wait of that launch
+                          (<= 0: 1 s); a wait that runs out ends the solve
+                          with NLM_ERR_TIMEOUT and the handle stays usable   */
+  int barrier_extra;   /* testing the bound only: arrivals each barrier waits
+                          for beyond the launched blocks (0 in use; > 0 makes
+                          every wait run out)                                */
 } nlm_qs_params;
 
 typedef struct nlm_qs_stats {

@@ -157,6 +157,9 @@ class QSParams(C.Structure):
         ("break_bonds", C.c_int),
         ("max_break_rounds", C.c_int),
         ("guess_accept", C.c_double),
+        ("krylov_launch", C.c_int),
+        ("wait_limit_s", C.c_double),
+        ("barrier_extra", C.c_int),
     ]
 
 

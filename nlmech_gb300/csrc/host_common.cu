@@ -11,6 +11,8 @@ void set_error(const std::string &msg) { g_err = msg; }
 int cuda_fail(cudaError_t e, const char *what) {
   g_err = std::string(what) + ": " + cudaGetErrorString(e);
   if (e == cudaErrorMemoryAllocation) return NLM_ERR_OOM;
+  // the solvers' bounded grid-barrier waits report a wait that ran out so
+  if (e == cudaErrorTimeout) return NLM_ERR_TIMEOUT;
   return NLM_ERR_CUDA;
 }
 int fail(int code, const std::string &msg) {

@@ -621,6 +621,197 @@ __global__ void k_cg32_update(int64_t n, const uint8_t *flags, const float *dblk
   }
 }
 
+// ---- the FP32 PCG in one cooperative launch -------------------------------
+// The two-launch iteration above costs two kernel launches per iteration and
+// a host round trip every few iterations; at 40,000 nodes that, not the
+// work, sets the iteration time.  k_cg32_coop runs the whole solve in one
+// launch whose blocks are all resident (cudaLaunchCooperativeKernel): each
+// iteration is the same two phases separated by a grid barrier, and every
+// block forms alpha, beta and the convergence test itself from the block
+// partials, summed in one fixed order (so every block takes the same
+// decision and the result does not depend on timing).
+//
+// Grid barrier: an arrival counter and a generation word.  A waiting block
+// polls the generation with a bounded wait (wait_ns of globaltimer); a wait
+// that runs out sets status = NLM_ERR_TIMEOUT, and every block leaves at its
+// next barrier once status is set, so the launch always ends.  expect is the
+// number of arrivals a barrier completes on: gridDim.x in use (more only to
+// test the bound).
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// coop[0] arrivals, coop[1] generation, coop[2] status
+__device__ bool coop_barrier(unsigned *coop, unsigned expect, uint64_t wait_ns) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned *gen = coop + 1;
+    volatile int *status = reinterpret_cast<volatile int *>(coop + 2);
+    const unsigned g = *gen;
+    __threadfence();
+    int ok = 1;
+    if (atomicAdd(coop, 1u) == expect - 1) {
+      atomicExch(coop, 0u);
+      __threadfence();
+      atomicAdd(coop + 1, 1u);
+    } else {
+      const uint64_t t0 = globaltimer_ns();
+      while (*gen == g) {
+        if (*status != 0) {
+          ok = 0;
+          break;
+        }
+        if (globaltimer_ns() - t0 > wait_ns) {
+          atomicExch(reinterpret_cast<int *>(coop + 2), NLM_ERR_TIMEOUT);
+          ok = 0;
+          break;
+        }
+        __nanosleep(100);
+      }
+    }
+    __threadfence();
+    if (*status != 0) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Sum of part[0 .. nb) in a fixed order, the same in every block.
+__device__ double coop_sum(const double *part, int nb) {
+  __shared__ double sh[32];
+  double v = 0.;
+  for (int k = threadIdx.x; k < nb; k += blockDim.x) v += __ldcg(part + k);
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double t = 0.;
+  for (int k = 0; k < (int)(blockDim.x >> 5); k++) t += sh[k];
+  return t;
+}
+
+// out[0] = iterations done, out[1] = r.r at the end (as double bits in the
+// double array res)
+template <int DIM>
+__global__ void __launch_bounds__(256) k_cg32_coop(
+    int64_t n, const uint8_t *flags, const int64_t *rowptr, const int *cols, const float *blk,
+    const float *dblk, float *p0, float *p1, float *ap, float *x, float *r, float *z,
+    double *part, const double *rz0, double target, int max_iters, unsigned *coop,
+    unsigned expect, uint64_t wait_ns, double *res) {
+  constexpr int NB = DIM == 2 ? 3 : 6;
+  constexpr int NP = DIM == 2 ? 4 : 8;
+  const int G = (int)gridDim.x;
+  double *pap_p = part, *rz_p = part + G, *rr_p = part + 2 * G;
+  double rz = *rz0, rr = 0.;
+  float beta = 0.f;
+  int it = 0;
+  bool ok = true;
+  while (it < max_iters) {
+    const float *pold = (it & 1) ? p0 : p1;
+    float *pnew = (it & 1) ? p1 : p0;
+    // phase 1: p_k = z_k + beta p_{k-1}, Ap_k, partials of p_k.Ap_k
+    float dot = 0.f;
+    const int64_t work = n * kG;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < work;
+         base += (int64_t)G * blockDim.x) {
+      const int64_t t = base + threadIdx.x;
+      const int64_t i = t / kG;
+      const int g = (int)(t % kG);
+      float acc[3] = {0.f, 0.f, 0.f}, tv[3];
+      if (i < n) {
+        const int64_t q1 = rowptr[i + 1];
+        for (int64_t qb = rowptr[i] + g; qb < q1; qb += 4 * kG) {
+          int jj[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) jj[u] = qb + u * kG < q1 ? cols[qb + u * kG] : -1;
+          float bb[4][NP], pj[4][3];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const int j = jj[u] < 0 ? (int)i : jj[u];
+            const int64_t q = jj[u] < 0 ? qb : qb + u * kG;
+            const float4 *bp = reinterpret_cast<const float4 *>(blk + NP * q);
+            const float4 b0 = bp[0];
+            bb[u][0] = b0.x; bb[u][1] = b0.y; bb[u][2] = b0.z; bb[u][3] = b0.w;
+            if (DIM == 3) {
+              const float4 b1 = bp[1];
+              bb[u][4] = b1.x; bb[u][5] = b1.y; bb[u][6] = b1.z; bb[u][7] = b1.w;
+            }
+            for (int c = 0; c < DIM; c++) pj[u][c] = fmaf(beta, pold[DIM * j + c], z[DIM * j + c]);
+            if (DIM == 2) pj[u][2] = 0.f;
+          }
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            if (jj[u] < 0) continue;
+            sym_mul<float>(DIM, bb[u], pj[u], tv);
+            for (int c = 0; c < DIM; c++) acc[c] -= tv[c];
+          }
+        }
+      }
+      for (int o = kG / 2; o > 0; o >>= 1)
+        for (int c = 0; c < DIM; c++) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+      if (i < n && g == 0) {
+        const uint8_t fl = flags[i];
+        float pi[3] = {0.f, 0.f, 0.f};
+        for (int c = 0; c < DIM; c++) {
+          pi[c] = fmaf(beta, pold[DIM * i + c], z[DIM * i + c]);
+          pnew[DIM * i + c] = pi[c];
+        }
+        sym_mul<float>(DIM, dblk + NB * i, pi, tv);
+        for (int c = 0; c < DIM; c++) {
+          const float yc = (fl >> c & 1) ? 0.f : acc[c] + tv[c];
+          ap[DIM * i + c] = yc;
+          dot = fmaf(pi[c], yc, dot);
+        }
+      }
+    }
+    block_sum_f(dot, pap_p);
+    if (!(ok = coop_barrier(coop, expect, wait_ns))) break;
+    const double pap = coop_sum(pap_p, G);
+    const float alpha = (float)(pap != 0. ? rz / pap : 0.);
+    // phase 2: x += alpha p, r -= alpha Ap, z = block-Jacobi(r), partials of
+    // r.z and r.r
+    float drz = 0.f, drr = 0.f;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)G * blockDim.x) {
+      const uint8_t fl = flags[i];
+      float rv[3] = {0.f, 0.f, 0.f}, zv[3] = {0.f, 0.f, 0.f};
+      for (int c = 0; c < DIM; c++) {
+        const int64_t k = DIM * i + c;
+        x[k] = fmaf(alpha, pnew[k], x[k]);
+        const float rk = fmaf(-alpha, ap[k], r[k]);
+        r[k] = rk;
+        drr = fmaf(rk, rk, drr);
+        rv[c] = (fl >> c & 1) ? 0.f : rk;
+      }
+      block_jacobi<DIM, float>(dblk + NB * i, fl, rv, zv);
+      for (int c = 0; c < DIM; c++) {
+        z[DIM * i + c] = zv[c];
+        drz = fmaf(rv[c], zv[c], drz);
+      }
+    }
+    block_sum2_f(drz, drr, rz_p, rr_p);
+    if (!(ok = coop_barrier(coop, expect, wait_ns))) break;
+    const double rz_next = coop_sum(rz_p, G);
+    rr = coop_sum(rr_p, G);
+    beta = (float)(rz != 0. ? rz_next / rz : 0.);
+    rz = rz_next;
+    it++;
+    if (!(rr > target)) break;
+    // the partials are rewritten next iteration only after the next barrier,
+    // which every block reaches after reading them
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    res[0] = (double)it;
+    res[1] = rr;
+  }
+  (void)ok;
+}
+
 __global__ void k_cg32_seed(float *fs, float *pold, int64_t m) {
   // beta = 0 for the first direction (p_0 = z_0); p_{-1} = 0
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -813,6 +1004,45 @@ static cudaError_t qs_cg32(const StepParams &P, const DevPtrs &D, const QSWork &
     *iters = 0;
     return cudaMemsetAsync(dx, 0, sizeof(double) * m, s);
   }
+  if (W.coop && W.coop_blocks > 0) {
+    // the whole solve in one cooperative launch
+    if ((e = cudaMemsetAsync(W.coop, 0, sizeof(unsigned), s))) return e;  // arrivals
+    if ((e = cudaMemsetAsync(W.coop + 2, 0, sizeof(unsigned), s))) return e;  // status
+    int64_t n = P.n;
+    const uint8_t *flags = D.flags;
+    const int64_t *rowptr = D.rowptr;
+    const int *cols = D.cols;
+    const float *blk = W.blk32, *dblk = W.dblk32;
+    float *p0 = pbuf[0], *p1 = pbuf[1], *ap = W.ap32, *x = W.x32, *r = W.r32, *z = W.z32;
+    double *part = W.cgpart;
+    const double *rz0 = tot + 0;
+    double tgt = target;
+    int mi = max_iters;
+    unsigned *coop = W.coop;
+    unsigned expect = (unsigned)W.coop_blocks + (unsigned)W.coop_extra;
+    uint64_t wait_ns = W.coop_wait_ns;
+    double *res = W.cgs + 6;
+    void *args[] = {&n, &flags, &rowptr, &cols, &blk, &dblk, &p0, &p1, &ap, &x, &r, &z,
+                    &part, &rz0, &tgt, &mi, &coop, &expect, &wait_ns, &res};
+    // p_{-1} = 0 lives in pbuf[1] (zeroed by the seed), p_0 goes to pbuf[0]
+    e = dim == 2 ? cudaLaunchCooperativeKernel((const void *)k_cg32_coop<2>, W.coop_blocks, 256,
+                                               args, 0, s)
+                 : cudaLaunchCooperativeKernel((const void *)k_cg32_coop<3>, W.coop_blocks, 256,
+                                               args, 0, s);
+    if (e != cudaSuccess) return e;
+    double hres[2] = {0., 0.};
+    int status = 0;
+    if ((e = cudaMemcpyAsync(hres, res, sizeof(hres), cudaMemcpyDeviceToHost, s))) return e;
+    if ((e = cudaMemcpyAsync(&status, W.coop + 2, sizeof(int), cudaMemcpyDeviceToHost, s)))
+      return e;
+    if ((e = cudaStreamSynchronize(s))) return e;
+    if (status != 0) return cudaErrorTimeout;
+    it = (int)hres[0];
+    *converged = !(hres[1] > target) || it < max_iters;
+    k_to_f64<<<qblk(m), 256, 0, s>>>(m, W.x32, dx);
+    *iters = it;
+    return cudaGetLastError();
+  }
   while (it < max_iters) {
     for (int q = 0; q < check_every && it < max_iters; q++, it++) {
       const int cur = it & 1, prv = cur ^ 1;
@@ -842,6 +1072,25 @@ static cudaError_t qs_cg32(const StepParams &P, const DevPtrs &D, const QSWork &
   k_to_f64<<<qblk(m), 256, 0, s>>>(m, W.x32, dx);
   *iters = it;
   return cudaGetLastError();
+}
+
+// Blocks of the cooperative solve: up to four per SM that can be resident
+// together, at most one per 256 (node, lane) items; 0 if the device cannot
+// launch it cooperatively.
+int qs_coop_blocks(int64_t n, int dim) {
+  int dev = 0, sms = 0, coop = 0, per = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  if (!coop || sms <= 0) return 0;
+  cudaError_t e = dim == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cg32_coop<2>, 256, 0)
+                           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cg32_coop<3>, 256, 0);
+  if (e != cudaSuccess || per <= 0) {
+    cudaGetLastError();
+    return 0;
+  }
+  const int64_t need = std::max<int64_t>(1, (int64_t)grp_blocks(n));
+  return (int)std::min<int64_t>((int64_t)sms * std::min(per, 4), need);
 }
 
 // Newton correction (-K) dx = rhs.  The FP32 solve is tried first; when it

@@ -145,6 +145,16 @@ int nlm_qs_create(const nlm_fd_desc *desc, const nlm_qs_params *prm, nlm_qs **ou
   q->W.nnz = nnz;
   if (e == cudaSuccess) e = q->alloc(&q->W.ticket, 4);
   if (e == cudaSuccess) e = cudaMemset(q->W.ticket, 0, 4 * sizeof(unsigned));
+  if (e == cudaSuccess && prm->krylov_launch == 0) {
+    q->W.coop_blocks = qs_coop_blocks(n, h->dim);
+    if (q->W.coop_blocks > 0) {
+      e = q->alloc(&q->W.coop, 4);
+      if (e == cudaSuccess) e = cudaMemset(q->W.coop, 0, 4 * sizeof(unsigned));
+      q->W.coop_extra = std::max(0, prm->barrier_extra);
+      const double lim = prm->wait_limit_s > 0. ? prm->wait_limit_s : 1.0;
+      q->W.coop_wait_ns = (uint64_t)(std::min(lim, 60.0) * 1e9);
+    }
+  }
   if (e == cudaSuccess) e = q->alloc(&q->W.sc, 8);
   if (e == cudaSuccess) e = q->alloc(&q->W.blk, (size_t)NB * (nnz + 1));
   if (e == cudaSuccess) e = q->alloc(&q->W.dblk, (size_t)NB * n);

@@ -21,7 +21,18 @@ struct QSWork {
   // FP32 Krylov solve: tangent copies and CG vectors
   float *blk32, *dblk32, *r32, *z32, *p32, *p32b, *ap32, *x32;
   int64_t nnz;
+  // the FP32 solve in one cooperative launch (coop == null: two launches
+  // per iteration): barrier words (arrivals, generation, status), grid
+  // size, extra arrivals a barrier waits for (testing the bound only) and
+  // the bound of each barrier wait
+  unsigned *coop;
+  int coop_blocks;
+  int coop_extra;
+  uint64_t coop_wait_ns;
 };
+
+// Grid size of the cooperative FP32 solve for n nodes (0: not available).
+int qs_coop_blocks(int64_t n, int dim);
 
 // count != NULL: bonds past the critical strain break during the evaluation
 // (RNPBond::getBondEF) and the number broken is added to *count.

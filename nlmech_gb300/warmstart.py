@@ -138,15 +138,24 @@ def run_steps(problem, nsteps, params=None, model=None, record=False, log=None,
     d2 = np.zeros((n, 2))
     phi = np.zeros(n, dtype=np.float32)
     stats, X, T = [], [], []
+    mlp_s = 0.0  # wall time of the network's inference calls (host in, host out)
+
+    def infer(F):
+        nonlocal mlp_s
+        t = time.perf_counter()
+        y = model.forward(F)
+        mlp_s += time.perf_counter() - t
+        return y
+
     t0 = time.perf_counter()
     for k in range(nsteps):
         hist = model is not None or record or secant
         F = fb.rows(k, d1, d2, phi) if (model is not None or record) else None
         if model is not None and start == "best":
             st = q.load_step(candidates=[fb.guess(u_prev, d1, None, phi),
-                                         fb.guess(u_prev, d1, model.forward(F), phi, deadzone)])
+                                         fb.guess(u_prev, d1, infer(F), phi, deadzone)])
         elif model is not None:
-            st = q.load_step(fb.guess(u_prev, d1, model.forward(F), phi, deadzone))
+            st = q.load_step(fb.guess(u_prev, d1, infer(F), phi, deadzone))
         elif secant:
             st = q.load_step(fb.guess(u_prev, d1, None, phi))
         else:
@@ -167,7 +176,8 @@ def run_steps(problem, nsteps, params=None, model=None, record=False, log=None,
                 k, st["newton_iters"], st["lin_iters"], st["used_guess"], st["broken"],
                 st["res_start"], st["res_final"], st["ms"]))
     wall = time.perf_counter() - t0
-    out = {"stats": stats, "wall_s": wall, "u": q.state(), "bonds": q.bond_state()}
+    out = {"stats": stats, "wall_s": wall, "mlp_s": mlp_s, "u": q.state(),
+           "bonds": q.bond_state()}
     if record:
         out["X"] = np.concatenate(X)
         out["T"] = np.concatenate(T)
@@ -183,6 +193,7 @@ def summary(run):
             "guess_used": int(sum(1 for s in st if s["used_guess"])),
 
             "wall_s": round(run["wall_s"], 4),
+            "mlp_infer_s": round(run.get("mlp_s", 0.0), 4),
             "solver_ms": round(sum(s["ms"] for s in st), 2),
             "all_steps_converged": bool(tol_ok)}
 

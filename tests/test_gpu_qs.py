@@ -80,3 +80,38 @@ def test_qs_guess_and_fallback(gpu):
     s3 = q3.load_step(guess=u2)
     assert s3["used_guess"] == 1
     assert s3["newton_iters"] <= 1
+
+
+def test_qs_single_launch_krylov_matches_two_launch(gpu):
+    """The FP32 Krylov solve in one cooperative launch (grid barriers between
+    its phases, convergence tested every iteration) and the same solve in two
+    launches per iteration reach the same Newton solutions: every load step
+    converges to the 1e-8 relative residual in both, with equal broken bonds
+    and displacements equal to the Newton tolerance."""
+    p = configs.qs_plate(48, h=5e-4, du=1e-6)
+    qa = gpu.QSModel(p, gpu.qs_params(lin_tol=1e-6, max_newton=60, krylov_launch=0))
+    qb = gpu.QSModel(p, gpu.qs_params(lin_tol=1e-6, max_newton=60, krylov_launch=1))
+    for k in range(4):
+        sa, sb = qa.load_step(), qb.load_step()
+        assert sa["res_final"] <= 1e-8 * sa["res_plain"], (k, sa)
+        assert sb["res_final"] <= 1e-8 * sb["res_plain"], (k, sb)
+    ua, ub = qa.state(), qb.state()
+    assert np.linalg.norm(ua - ub) <= 1e-2 * np.linalg.norm(ub)
+    ba, bb = qa.bond_state(), qb.bond_state()
+    assert np.count_nonzero(ba != bb) <= 0.01 * max(np.count_nonzero(bb), 1)
+
+
+def test_qs_barrier_wait_runs_out_with_status(gpu):
+    """Each grid-barrier wait of the single-launch solve is bounded: with
+    every barrier made to wait for one block that does not exist, each wait
+    runs out after 50 ms, the launch ends and the load step fails with
+    NLM_ERR_TIMEOUT; the device stays usable for the next model."""
+    p = configs.qs_plate(40, h=5e-4, du=1e-6)
+    bad = gpu.QSModel(p, gpu.qs_params(wait_limit_s=0.05, barrier_extra=1))
+    with pytest.raises(gpu.NLMError) as e:
+        bad.load_step()
+    assert e.value.code == 4  # NLM_ERR_TIMEOUT
+    bad.close()
+    good = gpu.QSModel(p, gpu.qs_params())
+    s = good.load_step()
+    assert s["res_final"] <= 1e-8 * s["res_plain"]

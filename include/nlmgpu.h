@@ -423,10 +423,11 @@ typedef struct nlm_qs_params {
   double guess_accept; /* a guess is used only if its linearised residual is
                           at most guess_accept times that of the plain
                           start (<= 0: 0.1)                                  */
-  int krylov_launch;   /* 0: the FP32 Krylov solve of a Newton step in one
-                          cooperative launch (grid barriers between its
-                          phases) where the device allows it; 1: two launches
-                          per iteration                                      */
+  int krylov_launch;   /* 0: the FP32 Krylov solve runs two launches per
+                          iteration (default; 30 us per iteration on the
+                          200 x 200 plate); 1: one cooperative launch per
+                          solve with grid barriers between its phases where
+                          the device allows it (37 us per iteration there)  */
   double wait_limit_s; /* bound of each grid-barrier wait of that launch
                           (<= 0: 1 s); a wait that runs out ends the solve
                           with NLM_ERR_TIMEOUT and the handle stays usable   */

@@ -11,6 +11,8 @@
 
 #include <atomic>
 
+#include <type_traits>
+
 #include "fp32_common.cuh"
 
 namespace nlm {
@@ -145,7 +147,7 @@ __global__ void __launch_bounds__(128)
     es_vec32<DIM>(Q, ni, uih, uil, nj, ujh, ujl, X, et);
     es_ext32<DIM>(X, et, Y, Xl, Yl, e);
     const bool was = (word >> (k & 31)) & 1u;
-    const bool fs = was || e > E.sc_eff * Xl;
+    const bool fs = was || e > __fmul_rn(E.sc_eff, Xl);
     nw |= (uint32_t)(fs && !was) << (k & 31);
     const float om = fminf(1.f, (E.check_up - Xl) * E.inv_h);
     th += fs ? 0.f : Xl * e * om * nj.vol;
@@ -233,6 +235,7 @@ __device__ __forceinline__ int es_stage_tile(const Params32 &Q, const DevPtrs &D
   for (int e = threadIdx.x; e < kTileNodes + nh; e += blockDim.x) {
     if (e < kTileNodes && e >= nt) continue;
     const int64_t g = e < kTileNodes ? t0 + e : (int64_t)D.tile_halo[h0 + e - kTileNodes];
+    if (g < 0) continue;  // an empty slot of a lattice-ordered halo
     float4 sx, su;
     es_stage32<DIM>(Q, D, ucur, g, no, uoh, uol, sx, su);
     if (FORCE) {
@@ -263,6 +266,46 @@ __global__ void __launch_bounds__(kTileNodes)
   const float4 xi = s_x[il], ui = s_u[il];
   const int len = D.rowlen[i];
   const uint2 *lp = reinterpret_cast<const uint2 *>(D.tile_lidx + D.sell_ptr[i >> 5]) + (i & 31);
+  const int ng = (len + 3) >> 2;
+  // fast loop: a row with no broken bond sums theta without bond-state bits
+  // and keeps the largest e - s_c |X|; a bond past its critical stretch (or
+  // an already broken one) sends the row through the full loop below, which
+  // forms e and |X| by the same function and decides with the same test
+  uint32_t any_bits = 0;
+  for (int w = 0; w * 32 < len; w++) any_bits |= D.bits[(int64_t)w * P.npad + i];
+  if (any_bits == 0u) {
+    float thf = 0.f, mx = -1.f;
+    auto fbond = [&](int jl) {
+      const float4 xj = s_x[jl], uj = s_u[jl];
+      float X[3] = {xj.x - xi.x, xj.y - xi.y, xj.z - xi.z};
+      float et[3] = {uj.x - ui.x, uj.y - ui.y, uj.z - ui.z};
+      float Y[3], Xl, iY, e;
+      es_ext32_fast<DIM>(X, et, Y, Xl, iY, e);
+      mx = fmaxf(mx, e - __fmul_rn(E.sc_eff, Xl));
+      const float om = fminf(1.f, (E.check_up - Xl) * E.inv_h);
+      thf += Xl * e * om * xj.w;
+    };
+    uint2 c = ng > 0 ? __ldg(lp) : make_uint2(0u, 0u);
+    const int full = len >> 2;
+    for (int g = 0; g < full; g++) {
+      const uint2 cur = c;
+      if (g + 1 < ng) c = __ldg(lp + 32 * (g + 1));
+      fbond((int)(cur.x & 0xffffu));
+      fbond((int)(cur.x >> 16));
+      fbond((int)(cur.y & 0xffffu));
+      fbond((int)(cur.y >> 16));
+    }
+    if (len & 3) {
+      const int jl[3] = {(int)(c.x & 0xffffu), (int)(c.x >> 16), (int)(c.y & 0xffffu)};
+      for (int q = 0; q < (len & 3); q++) fbond(jl[q]);
+    }
+    if (!(mx > 0.f)) {
+      const float minv = (float)(1.0 / D.mw64[i]);
+      const float theta = E.cfac * minv * thf;
+      D.es_ab[i] = make_float2(E.ka * theta * minv, E.kb * minv);
+      return;
+    }
+  }
   float th = 0.f;
   uint32_t word = 0, nw = 0;
   auto bond = [&](int k, int jl) {
@@ -272,13 +315,12 @@ __global__ void __launch_bounds__(kTileNodes)
     float Y[3], Xl, iY, e;
     es_ext32_fast<DIM>(X, et, Y, Xl, iY, e);
     const bool was = (word >> (k & 31)) & 1u;
-    const bool fs = was || e > E.sc_eff * Xl;
+    const bool fs = was || e > __fmul_rn(E.sc_eff, Xl);
     nw |= (uint32_t)(fs && !was) << (k & 31);
     const float om = fminf(1.f, (E.check_up - Xl) * E.inv_h);
     th += fs ? 0.f : Xl * e * om * xj.w;
   };
   // the next group's ids and bit word are loaded one group ahead
-  const int ng = (len + 3) >> 2;
   uint2 nxt = ng > 0 ? __ldg(lp) : make_uint2(0u, 0u);
   uint32_t wnext = ng > 0 ? D.bits[i] : 0u;
   auto group = [&](int g) {
@@ -337,45 +379,56 @@ __global__ void __launch_bounds__(kTileNodes)
   const uint2 *lp = reinterpret_cast<const uint2 *>(D.tile_lidx + D.sell_ptr[i >> 5]) + (i & 31);
   float fi[3] = {0.f, 0.f, 0.f};
   uint32_t word = 0;
-  auto bond = [&](int k, int jl) {
-    const float4 xj = s_x[jl], uj = s_u[jl];
-    float X[3] = {xj.x - xi.x, xj.y - xi.y, xj.z - xi.z};
-    float et[3] = {uj.x - ui.x, uj.y - ui.y, uj.z - ui.z};
-    float Y[3], Xl, iY, e;
-    es_ext32_fast<DIM>(X, et, Y, Xl, iY, e);
-    const float tsum = (ai + uj.w) * Xl + (bi + s_b[jl]) * e;
-    const float om = fminf(1.f, (E.check_up - Xl) * E.inv_h);
-    // a broken bond carries no force
-    const float s = ((word >> (k & 31)) & 1u) ? 0.f : tsum * om * xj.w * iY;
-    fi[0] = fmaf(s, Y[0], fi[0]);
-    fi[1] = fmaf(s, Y[1], fi[1]);
-    if (DIM == 3) fi[2] = fmaf(s, Y[2], fi[2]);
-  };
   const int ng = (len + 3) >> 2;
-  uint2 nxt = ng > 0 ? __ldg(lp) : make_uint2(0u, 0u);
-  uint32_t wnext = ng > 0 ? D.bits[i] : 0u;
-  auto group = [&](int g) {
-    if ((g & 7) == 0) {
-      word = wnext;
-      if (8 * ((g >> 3) + 1) < ng) wnext = D.bits[(int64_t)((g >> 3) + 1) * P.npad + i];
+  // a row without broken bonds skips the per-bond state test
+  uint32_t any_bits = 0;
+  for (int w = 0; w * 32 < len; w++) any_bits |= D.bits[(int64_t)w * P.npad + i];
+  auto run = [&](auto has_bits) {
+    constexpr bool HB = decltype(has_bits)::value;
+    auto bond = [&](int k, int jl) {
+      const float4 xj = s_x[jl], uj = s_u[jl];
+      float X[3] = {xj.x - xi.x, xj.y - xi.y, xj.z - xi.z};
+      float et[3] = {uj.x - ui.x, uj.y - ui.y, uj.z - ui.z};
+      float Y[3], Xl, iY, e;
+      es_ext32_fast<DIM>(X, et, Y, Xl, iY, e);
+      const float tsum = (ai + uj.w) * Xl + (bi + s_b[jl]) * e;
+      const float om = fminf(1.f, (E.check_up - Xl) * E.inv_h);
+      // a broken bond carries no force
+      const float s =
+          (HB && ((word >> (k & 31)) & 1u)) ? 0.f : tsum * om * xj.w * iY;
+      fi[0] = fmaf(s, Y[0], fi[0]);
+      fi[1] = fmaf(s, Y[1], fi[1]);
+      if (DIM == 3) fi[2] = fmaf(s, Y[2], fi[2]);
+    };
+    uint2 nxt = ng > 0 ? __ldg(lp) : make_uint2(0u, 0u);
+    uint32_t wnext = (HB && ng > 0) ? D.bits[i] : 0u;
+    auto group = [&](int g) {
+      if (HB && (g & 7) == 0) {
+        word = wnext;
+        if (8 * ((g >> 3) + 1) < ng) wnext = D.bits[(int64_t)((g >> 3) + 1) * P.npad + i];
+      }
+      const uint2 c = nxt;
+      if (g + 1 < ng) nxt = __ldg(lp + 32 * (g + 1));
+      return c;
+    };
+    const int full = len >> 2;
+    for (int g = 0; g < full; g++) {
+      const uint2 c = group(g);
+      bond(4 * g, (int)(c.x & 0xffffu));
+      bond(4 * g + 1, (int)(c.x >> 16));
+      bond(4 * g + 2, (int)(c.y & 0xffffu));
+      bond(4 * g + 3, (int)(c.y >> 16));
     }
-    const uint2 c = nxt;
-    if (g + 1 < ng) nxt = __ldg(lp + 32 * (g + 1));
-    return c;
+    if (len & 3) {
+      const uint2 c = group(full);
+      const int jl[3] = {(int)(c.x & 0xffffu), (int)(c.x >> 16), (int)(c.y & 0xffffu)};
+      for (int q = 0; q < (len & 3); q++) bond(4 * full + q, jl[q]);
+    }
   };
-  const int full = len >> 2;
-  for (int g = 0; g < full; g++) {
-    const uint2 c = group(g);
-    bond(4 * g, (int)(c.x & 0xffffu));
-    bond(4 * g + 1, (int)(c.x >> 16));
-    bond(4 * g + 2, (int)(c.y & 0xffffu));
-    bond(4 * g + 3, (int)(c.y >> 16));
-  }
-  if (len & 3) {
-    const uint2 c = group(full);
-    const int jl[3] = {(int)(c.x & 0xffffu), (int)(c.x >> 16), (int)(c.y & 0xffffu)};
-    for (int q = 0; q < (len & 3); q++) bond(4 * full + q, jl[q]);
-  }
+  if (any_bits)
+    run(std::true_type{});
+  else
+    run(std::false_type{});
   integrate_node32<DIM, SCHEME>(P, Q, D, T, A, i, fl, uih, uil, fi);
 }
 

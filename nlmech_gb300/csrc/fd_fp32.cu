@@ -404,14 +404,18 @@ __global__ void __launch_bounds__(kTileNodes, 3)
 // Returns s0 (the linearised bond's F = s0 d), ex = exp(-beta r S^2) (the
 // unbroken bond's F = s0 ex d), bs2 = S^2 r (|S| > S_c <=> bs2 > Ksc) and r.
 // A padding bond (d = e = 0) gives s0 = bs2 = 0.
-template <int OPT, bool KV>
+// UV: one volume for the model, K1 V min(1, cu_ih - r inv_h) formed as
+// min(K1 V, K1 V cu_ih - r K1 V inv_h) with the products precomputed.
+template <int OPT, bool KV, bool UV = false>
 __device__ __forceinline__ void tile_bond_core(const Params32 &Q, float2 d, float2 e, float vj,
                                                float &s0, float &ex, float &bs2, float &r) {
   const float r2 = fmaxf(__fmaf_rn(d.y, d.y, __fmul_rn(d.x, d.x)), 1e-30f);
   const float de = __fmaf_rn(d.y, e.y, __fmul_rn(d.x, e.x));
   const float rinv = rsqrt_approx(r2);
   r = __fmul_rn(r2, rinv);
-  float kw = __fmul_rn(KV ? vj : __fmul_rn(Q.K1, vj), fminf(1.f, __fmaf_rn(-r, Q.inv_h, Q.cu_ih)));
+  float kw = UV ? fminf(Q.kv_uniform, __fmaf_rn(-r, Q.kv_ih, Q.kv_cuih))
+                : __fmul_rn(KV ? vj : __fmul_rn(Q.K1, vj),
+                            fminf(1.f, __fmaf_rn(-r, Q.inv_h, Q.cu_ih)));
   if (!(OPT & OPT_CONSTJ) && Q.infl_type != 0) {  // type 0: J folded into K1
     const float rr = __fmul_rn(r, Q.inv_delta);
     kw = __fmul_rn(kw, Q.infl_type == 1
@@ -487,6 +491,7 @@ __device__ __forceinline__ void tilel_node(const StepParams &P, const Params32 &
   if (FAST && !full) {
     float mx = 0.f;  // largest S^2 r of the row
     uint2 nxt = ng > 0 ? sb[0] : make_uint2(0u, 0u);  // ids one group ahead
+#pragma unroll 2
     for (int g = 0; g < ng; g++) {
       const uint2 cur = nxt;
       if (g + 1 < ng) nxt = sb[32 * (g + 1)];
@@ -499,7 +504,7 @@ __device__ __forceinline__ void tilel_node(const StepParams &P, const Params32 &
 #pragma unroll
       for (int q = 0; q < 4; q++) {
         float s0, ex, bs2, r;
-        tile_bond_core<OPT, KV>(Qn, d[q], e[q], vj[q], s0, ex, bs2, r);
+        tile_bond_core<OPT, KV, UV>(Qn, d[q], e[q], vj[q], s0, ex, bs2, r);
         const float s1 = __fmul_rn(s0, ex);
         mx = fmaxf(mx, bs2);
         fi[0] = fmaf(s1, d[q].x, fi[0]);
@@ -531,7 +536,7 @@ __device__ __forceinline__ void tilel_node(const StepParams &P, const Params32 &
         float vj;
         tile_bond_data<UV, EXACT>(S, o[q], xi_x, xi_u, uli, kvu, d, e, vj);
         float s0, ex, bs2, r;
-        tile_bond_core<OPT, KV>(Qn, d, e, vj, s0, ex, bs2, r);
+        tile_bond_core<OPT, KV, UV>(Qn, d, e, vj, s0, ex, bs2, r);
         bool fs = (w4 >> q) & 1u;
         bool breakable = true;
         if (OPT & OPT_NOFAIL) breakable = brk_i && !(S.fl[o[q] >> 4] & FLAG_NOFAIL);

@@ -18,6 +18,8 @@
 // integrateVerlet.  K_0 (first = true) does the step-0 force evaluation of
 // integrate() (:319-333) and the drift of step 1.
 
+#include <array>
+
 #include "fd_handle.h"
 #include "tile_store.h"
 
@@ -189,21 +191,23 @@ int rnp_constants(const nlm_material &m, int dim, double delta, StepParams &P) {
   return NLM_OK;
 }
 
-// Lattice renumbering of an FP32C 2-D RNPBond model (after the neighbour
-// build, which orders nodes by the Morton code of their search cell, edge
-// >= horizon).  Nodes are renumbered by the Morton code of their cell on the
-// mesh lattice (edge h, g = floor((x - lo) / h + 1/2)): consecutive nodes then
-// form 4 x 2, 8 x 4, 16 x 16 ... patches of a grid-like mesh, and a 256-node
-// tile is a 16 x 16 patch.  Each row is ordered by the lattice offset of its
-// neighbour (|offset|^2, then angle; ties by node): in the interior the k-th
-// neighbours of eight consecutive nodes are then the same offset from each of
-// them, a shifted 4 x 2 patch whose Morton residues (g_x mod 4, g_y mod 2) are
-// all different, which is what the tile kernel's shared-memory layout needs
-// to read the eight records of a quarter warp in one pass.  Any node set
-// works (the order is only a layout); only results' rounding changes.
-// lres receives each node's residue (new order) for the tile store.
-int lattice_relabel(nlm_fd *h, NeighborBuild &nb, int S, double mesh_h, cudaStream_t s,
-                    std::vector<uint8_t> &lres) {
+// Lattice renumbering of an FP32C model on a tile decomposition (after the
+// neighbour build, which orders nodes by the Morton code of their search
+// cell, edge >= horizon).  Nodes are renumbered by the Morton code of their
+// cell on the mesh lattice (edge h, g = floor((x - lo) / h + 1/2)):
+// consecutive nodes then form 4 x 2, 8 x 4, ... 16 x 16 patches of a
+// grid-like 2-D mesh (2 x 2 x 2, ... 8 x 8 x 4 blocks in 3-D), and a 256-node
+// tile is one such patch.  Each row is ordered by the lattice offset of its
+// neighbour (|offset|^2, then the offset's components; ties by node): in the
+// interior the k-th neighbours of eight consecutive nodes are then the same
+// offset from each of them, a shifted 4 x 2 patch (2 x 2 x 2 block) whose
+// lattice residues are all different, which is what the tile kernels'
+// shared-memory layout needs to read the eight records of a quarter warp in
+// one pass.  Any node set works (the order is only a layout); only the
+// results' rounding changes.  lres receives each node's residue (new order):
+// (g_x mod 4, g_y mod 2) as a Morton code in 2-D, (g_x, g_y, g_z mod 2) in 3-D.
+int lattice_relabel(nlm_fd *h, NeighborBuild &nb, int dim, int S, double mesh_h,
+                    cudaStream_t s, std::vector<uint8_t> &lres) {
   const int64_t n = nb.n, nnz = nb.nnz;
   if (n == 0) return NLM_OK;
   std::vector<int> perm(n), cols(nnz);
@@ -214,22 +218,27 @@ int lattice_relabel(nlm_fd *h, NeighborBuild &nb, int S, double mesh_h, cudaStre
   NLM_CUDA(cudaMemcpyAsync(rp.data(), nb.rowptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, s));
   if (nnz) NLM_CUDA(cudaMemcpyAsync(cols.data(), nb.cols, sizeof(int) * nnz, cudaMemcpyDeviceToHost, s));
   NLM_CUDA(cudaStreamSynchronize(s));
-  double lo[2] = {1e300, 1e300};
+  const int D3 = dim == 3 ? 3 : 2;
+  double lo[3] = {1e300, 1e300, 1e300};
   for (int64_t i = 0; i < n; i++)
-    for (int d = 0; d < 2; d++) lo[d] = std::min(lo[d], pos[(size_t)S * i + d]);
-  std::vector<int64_t> gx(n), gy(n);
+    for (int d = 0; d < D3; d++) lo[d] = std::min(lo[d], pos[(size_t)S * i + d]);
+  std::vector<int64_t> gc((size_t)3 * n, 0);
   std::vector<std::pair<uint64_t, int64_t>> key(n);
-  auto spread = [](uint64_t v) {
+  const int bits = D3 == 3 ? 21 : 32;
+  auto spread = [&](uint64_t v) {
     uint64_t r = 0;
-    for (int b = 0; b < 32; b++) r |= ((v >> b) & 1ull) << (2 * b);
+    for (int b = 0; b < bits; b++) r |= ((v >> b) & 1ull) << (D3 * b);
     return r;
   };
+  const int64_t cmax = (1ll << bits) - 1;
   for (int64_t i = 0; i < n; i++) {
-    gx[i] = (int64_t)std::floor((pos[(size_t)S * i] - lo[0]) / mesh_h + 0.5);
-    gy[i] = (int64_t)std::floor((pos[(size_t)S * i + 1] - lo[1]) / mesh_h + 0.5);
-    const uint64_t cx = (uint64_t)std::max<int64_t>(0, std::min<int64_t>(gx[i], 0xffffffffll));
-    const uint64_t cy = (uint64_t)std::max<int64_t>(0, std::min<int64_t>(gy[i], 0xffffffffll));
-    key[i] = {spread(cx) | (spread(cy) << 1), i};
+    uint64_t k = 0;
+    for (int d = 0; d < D3; d++) {
+      const int64_t g = (int64_t)std::floor((pos[(size_t)S * i + d] - lo[d]) / mesh_h + 0.5);
+      gc[3 * i + d] = g;
+      k |= spread((uint64_t)std::max<int64_t>(0, std::min<int64_t>(g, cmax))) << d;
+    }
+    key[i] = {k, i};
   }
   std::sort(key.begin(), key.end());  // ties keep the search-cell order
   std::vector<int64_t> order(n), inv(n);
@@ -237,14 +246,16 @@ int lattice_relabel(nlm_fd *h, NeighborBuild &nb, int S, double mesh_h, cudaStre
     order[k] = key[k].second;
     inv[key[k].second] = k;
   }
-  // rank of a lattice offset: |o|^2, then angle
-  const int R = (int)std::ceil(h->P.delta / mesh_h) + 2, W = 2 * R + 1;
-  std::vector<std::pair<std::pair<int, double>, int>> offs;
-  for (int oy = -R; oy <= R; oy++)
-    for (int ox = -R; ox <= R; ox++)
-      offs.push_back({{ox * ox + oy * oy, std::atan2((double)oy, (double)ox)}, (oy + R) * W + ox + R});
+  // rank of a lattice offset: |o|^2, then its components
+  const int R = (int)std::ceil(h->P.delta / mesh_h) + 2, W = 2 * R + 1, Wz = D3 == 3 ? W : 1;
+  std::vector<std::pair<std::array<int, 4>, int>> offs;
+  for (int oz = (D3 == 3 ? -R : 0); oz <= (D3 == 3 ? R : 0); oz++)
+    for (int oy = -R; oy <= R; oy++)
+      for (int ox = -R; ox <= R; ox++)
+        offs.push_back({{ox * ox + oy * oy + oz * oz, oz, oy, ox},
+                        ((oz + (D3 == 3 ? R : 0)) * W + oy + R) * W + ox + R});
   std::sort(offs.begin(), offs.end());
-  std::vector<int> orank(W * W);
+  std::vector<int> orank((size_t)W * W * Wz);
   for (size_t k = 0; k < offs.size(); k++) orank[offs[k].second] = (int)k;
   std::vector<int> perm2(n), cols2(nnz);
   std::vector<double> pos2((size_t)S * n);
@@ -255,7 +266,9 @@ int lattice_relabel(nlm_fd *h, NeighborBuild &nb, int S, double mesh_h, cudaStre
     perm2[k] = perm[o];
     for (int d = 0; d < S; d++) pos2[(size_t)S * k + d] = pos[(size_t)S * o + d];
     rp2[k + 1] = rp2[k] + (rp[o + 1] - rp[o]);
-    lres[k] = (uint8_t)((gx[o] & 1) | ((gy[o] & 1) << 1) | ((gx[o] & 2) << 1));
+    const int64_t *g = &gc[3 * o];
+    lres[k] = D3 == 3 ? (uint8_t)((g[0] & 1) | ((g[1] & 1) << 1) | ((g[2] & 1) << 2))
+                      : (uint8_t)((g[0] & 1) | ((g[1] & 1) << 1) | ((g[0] & 2) << 1));
   }
   unsigned nthr = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
   auto work = [&](unsigned w) {
@@ -265,10 +278,15 @@ int lattice_relabel(nlm_fd *h, NeighborBuild &nb, int S, double mesh_h, cudaStre
       row.clear();
       for (int64_t q = rp[o]; q < rp[o + 1]; q++) {
         const int64_t jo = cols[q];
-        const int64_t ox = gx[jo] - gx[o], oy = gy[jo] - gy[o];
-        const int64_t rk = (ox >= -R && ox <= R && oy >= -R && oy <= R)
-                               ? orank[(oy + R) * W + ox + R]
-                               : (int64_t)W * W + ox * ox + oy * oy;
+        int64_t d[3] = {0, 0, 0};
+        bool in = true;
+        for (int c = 0; c < D3; c++) {
+          d[c] = gc[3 * jo + c] - gc[3 * o + c];
+          in = in && d[c] >= -R && d[c] <= R;
+        }
+        const int64_t rk =
+            in ? orank[((d[2] + (D3 == 3 ? R : 0)) * W + d[1] + R) * W + d[0] + R]
+               : (int64_t)W * W * Wz + d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         row.push_back({rk * (int64_t)n + inv[jo], (int)inv[jo]});
       }
       std::sort(row.begin(), row.end());
@@ -727,8 +745,8 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
     return bail(why.empty() ? cuda_fail(e, "neighbour build") : fail(NLM_ERR_INVALID, why));
   h->nnz = nb.nnz;
   if (h->nnz > INT32_MAX) return bail(fail(NLM_ERR_INVALID, "too many bonds for one handle"));
-  if (tile_able && !es_model && d->mesh_size > 0.) {
-    int rc_l = lattice_relabel(h, nb, S, d->mesh_size, s, h->lattice_res);
+  if (tile_able && d->mesh_size > 0.) {
+    int rc_l = lattice_relabel(h, nb, d->dim, S, d->mesh_size, s, h->lattice_res);
     if (rc_l) return bail(rc_l);
   }
   SellStore st;

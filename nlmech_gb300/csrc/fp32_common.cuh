@@ -36,6 +36,7 @@ struct Params32 {
   // (hi, lo) pairs
   float span_max;
   float kv_uniform;  // K1 V when every node has the same volume V, else 0
+  float kv_ih, kv_cuih;  // K1 V / h and K1 V (delta + h/2) / h (uniform V)
 };
 
 inline void split_const(double v, float &hi, float &lo) {
@@ -77,6 +78,8 @@ inline Params32 make_p32(const StepParams &P) {
                    ? (float)P.tile_span_max
                    : (float)(16.0 * P.h * P.fsc * P.rbar / std::sqrt(P.delta));
   q.kv_uniform = P.vol_uniform > 0. ? (float)(k1 * P.vol_uniform) : 0.f;
+  q.kv_ih = (float)(k1 * P.vol_uniform / P.h);
+  q.kv_cuih = (float)(k1 * P.vol_uniform * P.check_up / P.h);
   return q;
 }
 

@@ -695,8 +695,9 @@ __device__ double coop_sum(const double *part, int nb) {
   return t;
 }
 
-// out[0] = iterations done, out[1] = r.r at the end (as double bits in the
-// double array res)
+constexpr int kCoopThreads = 256;
+
+// res[0] = iterations done, res[1] = r.r at the end
 template <int DIM>
 __global__ void __launch_bounds__(256) k_cg32_coop(
     int64_t n, const uint8_t *flags, const int64_t *rowptr, const int *cols, const float *blk,
@@ -1025,10 +1026,10 @@ static cudaError_t qs_cg32(const StepParams &P, const DevPtrs &D, const QSWork &
     void *args[] = {&n, &flags, &rowptr, &cols, &blk, &dblk, &p0, &p1, &ap, &x, &r, &z,
                     &part, &rz0, &tgt, &mi, &coop, &expect, &wait_ns, &res};
     // p_{-1} = 0 lives in pbuf[1] (zeroed by the seed), p_0 goes to pbuf[0]
-    e = dim == 2 ? cudaLaunchCooperativeKernel((const void *)k_cg32_coop<2>, W.coop_blocks, 256,
-                                               args, 0, s)
-                 : cudaLaunchCooperativeKernel((const void *)k_cg32_coop<3>, W.coop_blocks, 256,
-                                               args, 0, s);
+    e = dim == 2 ? cudaLaunchCooperativeKernel((const void *)k_cg32_coop<2>, W.coop_blocks,
+                                               kCoopThreads, args, 0, s)
+                 : cudaLaunchCooperativeKernel((const void *)k_cg32_coop<3>, W.coop_blocks,
+                                               kCoopThreads, args, 0, s);
     if (e != cudaSuccess) return e;
     double hres[2] = {0., 0.};
     int status = 0;
@@ -1074,22 +1075,24 @@ static cudaError_t qs_cg32(const StepParams &P, const DevPtrs &D, const QSWork &
   return cudaGetLastError();
 }
 
-// Blocks of the cooperative solve: up to four per SM that can be resident
-// together, at most one per 256 (node, lane) items; 0 if the device cannot
-// launch it cooperatively.
+// Blocks of the cooperative solve: up to four blocks of kCoopThreads per SM
+// that can be resident together, at most one per kCoopThreads (node, lane)
+// items; 0 if the device cannot launch it cooperatively.  (One block of 1024
+// threads per SM, fewer arrivals per barrier, measured slower.)
 int qs_coop_blocks(int64_t n, int dim) {
   int dev = 0, sms = 0, coop = 0, per = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
   if (!coop || sms <= 0) return 0;
-  cudaError_t e = dim == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cg32_coop<2>, 256, 0)
-                           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cg32_coop<3>, 256, 0);
+  cudaError_t e =
+      dim == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cg32_coop<2>, kCoopThreads, 0)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cg32_coop<3>, kCoopThreads, 0);
   if (e != cudaSuccess || per <= 0) {
     cudaGetLastError();
     return 0;
   }
-  const int64_t need = std::max<int64_t>(1, (int64_t)grp_blocks(n));
+  const int64_t need = std::max<int64_t>(1, (n * kG + kCoopThreads - 1) / kCoopThreads);
   return (int)std::min<int64_t>((int64_t)sms * std::min(per, 4), need);
 }
 

@@ -145,7 +145,7 @@ int nlm_qs_create(const nlm_fd_desc *desc, const nlm_qs_params *prm, nlm_qs **ou
   q->W.nnz = nnz;
   if (e == cudaSuccess) e = q->alloc(&q->W.ticket, 4);
   if (e == cudaSuccess) e = cudaMemset(q->W.ticket, 0, 4 * sizeof(unsigned));
-  if (e == cudaSuccess && prm->krylov_launch == 0) {
+  if (e == cudaSuccess && prm->krylov_launch == 1) {
     q->W.coop_blocks = qs_coop_blocks(n, h->dim);
     if (q->W.coop_blocks > 0) {
       e = q->alloc(&q->W.coop, 4);

@@ -17,8 +17,9 @@ namespace nlm {
 // model) the halo is laid out by residue: halo node j takes staged slot
 // 256 + 8 m + res(j) (m counting the tile's halo nodes of that residue), so
 // that eight neighbours of one lattice offset from a quarter warp's 4 x 2
-// patch land in eight different 16-byte bank groups; the slots left empty
-// hold -1 in the halo list and are skipped by the staging.
+// patch (2 x 2 x 2 block in 3-D) land in eight different 16-byte bank
+// groups; the slots left empty hold -1 in the halo list and are skipped by
+// the staging.
 // What a tile store is built from (one model or a batch's combined layout).
 struct TileInputs {
   int64_t n, nnz, nslices, sell_entries;
@@ -68,7 +69,7 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
       // staged slot (from kTileNodes) of each halo node, in hl's order
       std::vector<int> hslot(hl.size());
       for (size_t k = 0; k < hl.size(); k++) hslot[k] = (int)k;
-      if (in.lres && boff_too) {
+      if (in.lres) {
         int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (size_t k = 0; k < hl.size(); k++) {
           const int r = (*in.lres)[hl[k]] & 7;
@@ -82,8 +83,7 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
         // slot-ordered one after the rows are written
         halo_slots[t] = std::move(bys);
       }
-      const int64_t nstaged = in.lres && boff_too ? (int64_t)halo_slots[t].size()
-                                                   : (int64_t)hl.size();
+      const int64_t nstaged = in.lres ? (int64_t)halo_slots[t].size() : (int64_t)hl.size();
       if (kTileNodes + nstaged > max_local) {
         too_big[0] = 1;
         continue;
@@ -117,7 +117,7 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
     ids_max = std::max(ids_max, 2 * (sptr[s1] - sptr[s0]));
   }
   if (boff_too && ids_max > kTileIdsMaxBytes) return NLM_OK;
-  if (in.lres && boff_too)
+  if (in.lres)
     for (int64_t t = 0; t < nt; t++) halo[t] = std::move(halo_slots[t]);
   std::vector<int> hptr(nt + 1, 0);
   size_t nmax = 0;

@@ -89,8 +89,8 @@ def test_qs_single_launch_krylov_matches_two_launch(gpu):
     converges to the 1e-8 relative residual in both, with equal broken bonds
     and displacements equal to the Newton tolerance."""
     p = configs.qs_plate(48, h=5e-4, du=1e-6)
-    qa = gpu.QSModel(p, gpu.qs_params(lin_tol=1e-6, max_newton=60, krylov_launch=0))
-    qb = gpu.QSModel(p, gpu.qs_params(lin_tol=1e-6, max_newton=60, krylov_launch=1))
+    qa = gpu.QSModel(p, gpu.qs_params(lin_tol=1e-6, max_newton=60, krylov_launch=1))
+    qb = gpu.QSModel(p, gpu.qs_params(lin_tol=1e-6, max_newton=60, krylov_launch=0))
     for k in range(4):
         sa, sb = qa.load_step(), qb.load_step()
         assert sa["res_final"] <= 1e-8 * sa["res_plain"], (k, sa)
@@ -107,7 +107,7 @@ def test_qs_barrier_wait_runs_out_with_status(gpu):
     runs out after 50 ms, the launch ends and the load step fails with
     NLM_ERR_TIMEOUT; the device stays usable for the next model."""
     p = configs.qs_plate(40, h=5e-4, du=1e-6)
-    bad = gpu.QSModel(p, gpu.qs_params(wait_limit_s=0.05, barrier_extra=1))
+    bad = gpu.QSModel(p, gpu.qs_params(krylov_launch=1, wait_limit_s=0.05, barrier_extra=1))
     with pytest.raises(gpu.NLMError) as e:
         bad.load_step()
     assert e.value.code == 4  # NLM_ERR_TIMEOUT

@@ -97,25 +97,70 @@ __device__ __forceinline__ void es_ext32(const float X[3], const float et[3], fl
 // es_ext32 for the tile kernels: the same quantities with the division by
 // |Y| + |X| done by the hardware reciprocal (relative error ~1 ulp) and 1/|Y|
 // returned from the square-root step, so no bond takes an IEEE division.
+// Every operation is written out with its rounding, in the order of
+// es_ext32_pair, so that the scalar and the pair forms give one bond the same
+// e and |X| (and so the same break decision).  The squared lengths carry
+// 1e-30 added to the first square: below half an ulp of any bond's squared
+// length, it only keeps a zero-length bond (a row's padding entry) away from
+// rsqrt(0).
 template <int DIM>
 __device__ __forceinline__ void es_ext32_fast(const float X[3], const float et[3], float Y[3],
                                               float &Xl, float &iY, float &e) {
-  float x2 = X[0] * X[0] + X[1] * X[1];
-  float xe = X[0] * et[0] + X[1] * et[1];
-  float ee = et[0] * et[0] + et[1] * et[1];
+  float x2 = __fmaf_rn(X[1], X[1], __fmaf_rn(X[0], X[0], 1e-30f));
+  float xe = __fmaf_rn(X[1], et[1], __fmul_rn(X[0], et[0]));
+  float ee = __fmaf_rn(et[1], et[1], __fmul_rn(et[0], et[0]));
   if (DIM == 3) {
-    x2 = fmaf(X[2], X[2], x2);
-    xe = fmaf(X[2], et[2], xe);
-    ee = fmaf(et[2], et[2], ee);
+    x2 = __fmaf_rn(X[2], X[2], x2);
+    xe = __fmaf_rn(X[2], et[2], xe);
+    ee = __fmaf_rn(et[2], et[2], ee);
   }
-  for (int c = 0; c < 3; c++) Y[c] = X[c] + et[c];
-  float y2 = Y[0] * Y[0] + Y[1] * Y[1];
-  if (DIM == 3) y2 = fmaf(Y[2], Y[2], y2);
-  x2 = fmaxf(x2, 1e-30f);
-  y2 = fmaxf(y2, 1e-30f);
+  for (int c = 0; c < 3; c++) Y[c] = __fadd_rn(X[c], et[c]);
+  float y2 = __fmaf_rn(Y[1], Y[1], __fmaf_rn(Y[0], Y[0], 1e-30f));
+  if (DIM == 3) y2 = __fmaf_rn(Y[2], Y[2], y2);
   iY = rsqrt_approx(y2);
-  Xl = x2 * rsqrt_approx(x2);
-  e = fmaf(2.f, xe, ee) * rcp_approx(fmaf(y2, iY, Xl));
+  Xl = __fmul_rn(x2, rsqrt_approx(x2));
+  e = __fmul_rn(__fmaf_rn(2.f, xe, ee), rcp_approx(__fmaf_rn(y2, iY, Xl)));
+}
+
+// es_ext32_fast for two bonds at once (lane x, lane y) by packed FP32 pair
+// operations; each lane equals es_ext32_fast of its bond.
+template <int DIM>
+__device__ __forceinline__ void es_ext32_pair(const float2 X[3], const float2 et[3], float2 Y[3],
+                                              float2 &Xl, float2 &iY, float2 &e) {
+  const float2 eps = make_float2(1e-30f, 1e-30f);
+  float2 x2 = __ffma2_rn(X[1], X[1], __ffma2_rn(X[0], X[0], eps));
+  float2 xe = __ffma2_rn(X[1], et[1], __fmul2_rn(X[0], et[0]));
+  float2 ee = __ffma2_rn(et[1], et[1], __fmul2_rn(et[0], et[0]));
+  if (DIM == 3) {
+    x2 = __ffma2_rn(X[2], X[2], x2);
+    xe = __ffma2_rn(X[2], et[2], xe);
+    ee = __ffma2_rn(et[2], et[2], ee);
+  }
+  for (int c = 0; c < DIM; c++) Y[c] = __fadd2_rn(X[c], et[c]);
+  float2 y2 = __ffma2_rn(Y[1], Y[1], __ffma2_rn(Y[0], Y[0], eps));
+  if (DIM == 3) y2 = __ffma2_rn(Y[2], Y[2], y2);
+  iY = make_float2(rsqrt_approx(y2.x), rsqrt_approx(y2.y));
+  Xl = __fmul2_rn(x2, make_float2(rsqrt_approx(x2.x), rsqrt_approx(x2.y)));
+  const float2 den = __ffma2_rn(y2, iY, Xl);
+  e = __fmul2_rn(__ffma2_rn(make_float2(2.f, 2.f), xe, ee),
+                 make_float2(rcp_approx(den.x), rcp_approx(den.y)));
+}
+
+// The staged bond vectors of bonds a (lane x) and b (lane y) of node i.
+template <int DIM>
+__device__ __forceinline__ void es_pair_vec(const float4 &xi, const float4 &ui, const float4 &xa,
+                                            const float4 &ua, const float4 &xb,
+                                            const float4 &ub, float2 X[3], float2 et[3]) {
+  X[0] = make_float2(__fsub_rn(xa.x, xi.x), __fsub_rn(xb.x, xi.x));
+  X[1] = make_float2(__fsub_rn(xa.y, xi.y), __fsub_rn(xb.y, xi.y));
+  et[0] = make_float2(__fsub_rn(ua.x, ui.x), __fsub_rn(ub.x, ui.x));
+  et[1] = make_float2(__fsub_rn(ua.y, ui.y), __fsub_rn(ub.y, ui.y));
+  if (DIM == 3) {
+    X[2] = make_float2(__fsub_rn(xa.z, xi.z), __fsub_rn(xb.z, xi.z));
+    et[2] = make_float2(__fsub_rn(ua.z, ui.z), __fsub_rn(ub.z, ui.z));
+  } else {
+    X[2] = et[2] = make_float2(0.f, 0.f);
+  }
 }
 
 template <int DIM>
@@ -153,7 +198,7 @@ __global__ void __launch_bounds__(128)
     th += fs ? 0.f : Xl * e * om * nj.vol;
   }
   if (nw) D.bits[(int64_t)((len - 1) >> 5) * P.npad + i] = word | nw;
-  const float minv = (float)(1.0 / D.mw64[i]);
+  const float minv = D.minv32[i];
   const float theta = E.cfac * minv * th;
   D.es_ab[i] = make_float2(E.ka * theta * minv, E.kb * minv);
 }
@@ -274,33 +319,40 @@ __global__ void __launch_bounds__(kTileNodes)
   uint32_t any_bits = 0;
   for (int w = 0; w * 32 < len; w++) any_bits |= D.bits[(int64_t)w * P.npad + i];
   if (any_bits == 0u) {
-    float thf = 0.f, mx = -1.f;
-    auto fbond = [&](int jl) {
-      const float4 xj = s_x[jl], uj = s_u[jl];
-      float X[3] = {xj.x - xi.x, xj.y - xi.y, xj.z - xi.z};
-      float et[3] = {uj.x - ui.x, uj.y - ui.y, uj.z - ui.z};
-      float Y[3], Xl, iY, e;
-      es_ext32_fast<DIM>(X, et, Y, Xl, iY, e);
-      mx = fmaxf(mx, e - __fmul_rn(E.sc_eff, Xl));
-      const float om = fminf(1.f, (E.check_up - Xl) * E.inv_h);
-      thf += Xl * e * om * xj.w;
+    // bonds in pairs (lane x, lane y), each lane summing its share of theta;
+    // a row's padding entries (its own node) are masked in the last group
+    float mx = -1.f;
+    float2 th2 = make_float2(0.f, 0.f);
+    const float2 nsc = make_float2(-E.sc_eff, -E.sc_eff);
+    const float2 cu2 = make_float2(E.check_up, E.check_up), ih2 = make_float2(E.inv_h, E.inv_h);
+    auto fpair = [&](int ja, int jb, bool va, bool vb) {
+      const float4 xa = s_x[ja], xb = s_x[jb], ua = s_u[ja], ub = s_u[jb];
+      float2 X[3], et[3], Y[3], Xl, iY, e;
+      es_pair_vec<DIM>(xi, ui, xa, ua, xb, ub, X, et);
+      es_ext32_pair<DIM>(X, et, Y, Xl, iY, e);
+      const float2 z = __fadd2_rn(e, __fmul2_rn(nsc, Xl));  // e - s_c |X|
+      const float2 t = __fmul2_rn(__fadd2_rn(cu2, make_float2(-Xl.x, -Xl.y)), ih2);
+      const float2 om = make_float2(fminf(1.f, t.x), fminf(1.f, t.y));
+      float2 w = __fmul2_rn(__fmul2_rn(Xl, e), om);
+      w = make_float2(va ? w.x : 0.f, vb ? w.y : 0.f);
+      mx = fmax3(mx, va ? z.x : -1.f, vb ? z.y : -1.f);
+      th2 = __ffma2_rn(w, make_float2(xa.w, xb.w), th2);
     };
     uint2 c = ng > 0 ? __ldg(lp) : make_uint2(0u, 0u);
     const int full = len >> 2;
     for (int g = 0; g < full; g++) {
       const uint2 cur = c;
       if (g + 1 < ng) c = __ldg(lp + 32 * (g + 1));
-      fbond((int)(cur.x & 0xffffu));
-      fbond((int)(cur.x >> 16));
-      fbond((int)(cur.y & 0xffffu));
-      fbond((int)(cur.y >> 16));
+      fpair((int)(cur.x & 0xffffu), (int)(cur.x >> 16), true, true);
+      fpair((int)(cur.y & 0xffffu), (int)(cur.y >> 16), true, true);
     }
-    if (len & 3) {
-      const int jl[3] = {(int)(c.x & 0xffffu), (int)(c.x >> 16), (int)(c.y & 0xffffu)};
-      for (int q = 0; q < (len & 3); q++) fbond(jl[q]);
+    if (const int rem = len & 3) {
+      fpair((int)(c.x & 0xffffu), (int)(c.x >> 16), true, rem > 1);
+      if (rem > 2) fpair((int)(c.y & 0xffffu), (int)(c.y >> 16), true, false);
     }
+    const float thf = __fadd_rn(th2.x, th2.y);
     if (!(mx > 0.f)) {
-      const float minv = (float)(1.0 / D.mw64[i]);
+      const float minv = D.minv32[i];
       const float theta = E.cfac * minv * thf;
       D.es_ab[i] = make_float2(E.ka * theta * minv, E.kb * minv);
       return;
@@ -349,13 +401,13 @@ __global__ void __launch_bounds__(kTileNodes)
     for (int q = 0; q < (len & 3); q++) bond(4 * full + q, jl[q]);
   }
   if (nw) D.bits[(int64_t)((len - 1) >> 5) * P.npad + i] = word | nw;
-  const float minv = (float)(1.0 / D.mw64[i]);
+  const float minv = D.minv32[i];
   const float theta = E.cfac * minv * th;
   D.es_ab[i] = make_float2(E.ka * theta * minv, E.kb * minv);
 }
 
 template <int DIM, int SCHEME>
-__global__ void __launch_bounds__(kTileNodes)
+__global__ void __launch_bounds__(kTileNodes, 4)
     k_es_force32_tile(const StepParams P, const Params32 Q, const ESConst32 E, const DevPtrs D,
                       const BCTable T, const StepArgs A) {
   extern __shared__ float4 es_sm[];
@@ -383,22 +435,32 @@ __global__ void __launch_bounds__(kTileNodes)
   // a row without broken bonds skips the per-bond state test
   uint32_t any_bits = 0;
   for (int w = 0; w * 32 < len; w++) any_bits |= D.bits[(int64_t)w * P.npad + i];
+  // bonds in pairs (lane x: bond k, lane y: bond k + 1), each lane summing
+  // its share of the force; padding entries are masked in the last group
+  const float2 ai2 = make_float2(ai, ai), bi2 = make_float2(bi, bi);
+  const float2 cu2 = make_float2(E.check_up, E.check_up), ih2 = make_float2(E.inv_h, E.inv_h);
+  float2 fx = make_float2(0.f, 0.f), fy = fx, fz = fx;
   auto run = [&](auto has_bits) {
     constexpr bool HB = decltype(has_bits)::value;
-    auto bond = [&](int k, int jl) {
-      const float4 xj = s_x[jl], uj = s_u[jl];
-      float X[3] = {xj.x - xi.x, xj.y - xi.y, xj.z - xi.z};
-      float et[3] = {uj.x - ui.x, uj.y - ui.y, uj.z - ui.z};
-      float Y[3], Xl, iY, e;
-      es_ext32_fast<DIM>(X, et, Y, Xl, iY, e);
-      const float tsum = (ai + uj.w) * Xl + (bi + s_b[jl]) * e;
-      const float om = fminf(1.f, (E.check_up - Xl) * E.inv_h);
+    auto bond = [&](int k, int ja, int jb, bool va, bool vb) {
+      const float4 xa = s_x[ja], xb = s_x[jb], ua = s_u[ja], ub = s_u[jb];
+      float2 X[3], et[3], Y[3], Xl, iY, e;
+      es_pair_vec<DIM>(xi, ui, xa, ua, xb, ub, X, et);
+      es_ext32_pair<DIM>(X, et, Y, Xl, iY, e);
+      const float2 tsum = __ffma2_rn(__fadd2_rn(bi2, make_float2(s_b[ja], s_b[jb])), e,
+                                     __fmul2_rn(__fadd2_rn(ai2, make_float2(ua.w, ub.w)), Xl));
+      const float2 t = __fmul2_rn(__fadd2_rn(cu2, make_float2(-Xl.x, -Xl.y)), ih2);
+      const float2 om = make_float2(fminf(1.f, t.x), fminf(1.f, t.y));
+      float2 s = __fmul2_rn(__fmul2_rn(__fmul2_rn(tsum, om), make_float2(xa.w, xb.w)), iY);
       // a broken bond carries no force
-      const float s =
-          (HB && ((word >> (k & 31)) & 1u)) ? 0.f : tsum * om * xj.w * iY;
-      fi[0] = fmaf(s, Y[0], fi[0]);
-      fi[1] = fmaf(s, Y[1], fi[1]);
-      if (DIM == 3) fi[2] = fmaf(s, Y[2], fi[2]);
+      if (HB) {
+        va = va && !((word >> (k & 31)) & 1u);
+        vb = vb && !((word >> ((k + 1) & 31)) & 1u);
+      }
+      s = make_float2(va ? s.x : 0.f, vb ? s.y : 0.f);
+      fx = __ffma2_rn(s, Y[0], fx);
+      fy = __ffma2_rn(s, Y[1], fy);
+      if (DIM == 3) fz = __ffma2_rn(s, Y[2], fz);
     };
     uint2 nxt = ng > 0 ? __ldg(lp) : make_uint2(0u, 0u);
     uint32_t wnext = (HB && ng > 0) ? D.bits[i] : 0u;
@@ -414,21 +476,22 @@ __global__ void __launch_bounds__(kTileNodes)
     const int full = len >> 2;
     for (int g = 0; g < full; g++) {
       const uint2 c = group(g);
-      bond(4 * g, (int)(c.x & 0xffffu));
-      bond(4 * g + 1, (int)(c.x >> 16));
-      bond(4 * g + 2, (int)(c.y & 0xffffu));
-      bond(4 * g + 3, (int)(c.y >> 16));
+      bond(4 * g, (int)(c.x & 0xffffu), (int)(c.x >> 16), true, true);
+      bond(4 * g + 2, (int)(c.y & 0xffffu), (int)(c.y >> 16), true, true);
     }
-    if (len & 3) {
+    if (const int rem = len & 3) {
       const uint2 c = group(full);
-      const int jl[3] = {(int)(c.x & 0xffffu), (int)(c.x >> 16), (int)(c.y & 0xffffu)};
-      for (int q = 0; q < (len & 3); q++) bond(4 * full + q, jl[q]);
+      bond(4 * full, (int)(c.x & 0xffffu), (int)(c.x >> 16), true, rem > 1);
+      if (rem > 2) bond(4 * full + 2, (int)(c.y & 0xffffu), (int)(c.y >> 16), true, false);
     }
   };
   if (any_bits)
     run(std::true_type{});
   else
     run(std::false_type{});
+  fi[0] = __fadd_rn(fx.x, fx.y);
+  fi[1] = __fadd_rn(fy.x, fy.y);
+  if (DIM == 3) fi[2] = __fadd_rn(fz.x, fz.y);
   integrate_node32<DIM, SCHEME>(P, Q, D, T, A, i, fl, uih, uil, fi);
 }
 
@@ -479,6 +542,19 @@ static cudaError_t es32(const StepParams &P, const DevPtrs &D, const BCTable &T,
     k_es_force32<DIM, NLM_VELOCITY_VERLET><<<g, 128, 0, s>>>(P, Q, E, D, T, a);
   else
     k_es_force32<DIM, NLM_CENTRAL_DIFFERENCE><<<g, 128, 0, s>>>(P, Q, E, D, T, a);
+  return cudaGetLastError();
+}
+
+// 1 / m_i for the FP32C passes, formed once in FP64 (m_i stays at its
+// initial value), so no step takes a per-node FP64 division.
+__global__ void k_es_minv32(const double *mw, float *minv, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) minv[i] = (float)(1.0 / mw[i]);
+}
+
+cudaError_t launch_es_minv32(const double *mw, float *minv, int64_t n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_es_minv32<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(mw, minv, n);
   return cudaGetLastError();
 }
 

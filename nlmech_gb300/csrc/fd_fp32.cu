@@ -403,13 +403,15 @@ __global__ void __launch_bounds__(kTileNodes, 3)
 // One bond in the tile frame: d = xi, e = eta, vj = K1 V_j (KV) or V_j.
 // Returns s0 (the linearised bond's F = s0 d), ex = exp(-beta r S^2) (the
 // unbroken bond's F = s0 ex d), bs2 = S^2 r (|S| > S_c <=> bs2 > Ksc) and r.
-// A padding bond (d = e = 0) gives s0 = bs2 = 0.
+// A padding bond (d = e = 0) gives s0 = bs2 = 0: r^2 carries 1e-30 added to
+// the first square (below half an ulp of any bond's squared length, so it
+// only keeps a zero-length bond away from rsqrt(0)).
 // UV: one volume for the model, K1 V min(1, cu_ih - r inv_h) formed as
 // min(K1 V, K1 V cu_ih - r K1 V inv_h) with the products precomputed.
 template <int OPT, bool KV, bool UV = false>
 __device__ __forceinline__ void tile_bond_core(const Params32 &Q, float2 d, float2 e, float vj,
                                                float &s0, float &ex, float &bs2, float &r) {
-  const float r2 = fmaxf(__fmaf_rn(d.y, d.y, __fmul_rn(d.x, d.x)), 1e-30f);
+  const float r2 = __fmaf_rn(d.y, d.y, __fmaf_rn(d.x, d.x, 1e-30f));
   const float de = __fmaf_rn(d.y, e.y, __fmul_rn(d.x, e.x));
   const float rinv = rsqrt_approx(r2);
   r = __fmul_rn(r2, rinv);
@@ -428,6 +430,48 @@ __device__ __forceinline__ void tile_bond_core(const Params32 &Q, float2 d, floa
   bs2 = __fmul_rn(a, S);
   s0 = __fmul_rn(kw, __fmul_rn(S, rinv));
   ex = ex2_approx(__fmul_rn(Q.nbl2e, bs2));
+}
+
+// Two bonds a, b at once, lane x = a, lane y = b, by packed FP32 pair
+// operations: every lane value equals what tile_bond_core gives that bond
+// (the same separately rounded operations; rsqrt and exp2 per lane).
+// Returns s1 = s0 ex (the unbroken bond's force per unit xi) and bs2.
+template <int OPT, bool KV, bool UV>
+__device__ __forceinline__ void tile_bond_pair(const Params32 &Q, float2 dx, float2 dy, float2 ex,
+                                               float2 ey, float2 vj, float2 &s1, float2 &bs2) {
+  const float2 r2 = __ffma2_rn(dy, dy, __ffma2_rn(dx, dx, make_float2(1e-30f, 1e-30f)));
+  const float2 de = __ffma2_rn(dy, ey, __fmul2_rn(dx, ex));
+  const float2 rinv = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+  const float2 r = __fmul2_rn(r2, rinv);
+  float2 kw;
+  if (UV) {
+    const float2 t = __ffma2_rn(make_float2(-r.x, -r.y), make_float2(Q.kv_ih, Q.kv_ih),
+                                make_float2(Q.kv_cuih, Q.kv_cuih));
+    kw = make_float2(fminf(Q.kv_uniform, t.x), fminf(Q.kv_uniform, t.y));
+  } else {
+    const float2 t = __ffma2_rn(make_float2(-r.x, -r.y), make_float2(Q.inv_h, Q.inv_h),
+                                make_float2(Q.cu_ih, Q.cu_ih));
+    const float2 kv = KV ? vj : __fmul2_rn(make_float2(Q.K1, Q.K1), vj);
+    kw = __fmul2_rn(kv, make_float2(fminf(1.f, t.x), fminf(1.f, t.y)));
+  }
+  if (!(OPT & OPT_CONSTJ) && Q.infl_type != 0) {
+    const float2 rr = __fmul2_rn(r, make_float2(Q.inv_delta, Q.inv_delta));
+    float2 j;
+    if (Q.infl_type == 1) {
+      j = __ffma2_rn(make_float2(Q.a1, Q.a1), rr, make_float2(Q.a0, Q.a0));
+    } else {
+      const float c = Q.ibeta * 1.4426950408889634f;
+      const float2 z = __fmul2_rn(__fmul2_rn(make_float2(-rr.x, -rr.y), rr), make_float2(c, c));
+      j = __fmul2_rn(make_float2(Q.alpha, Q.alpha), make_float2(ex2_approx(z.x), ex2_approx(z.y)));
+    }
+    kw = __fmul2_rn(kw, j);
+  }
+  const float2 a = __fmul2_rn(de, rinv);  // S r
+  const float2 S = __fmul2_rn(a, rinv);
+  bs2 = __fmul2_rn(a, S);
+  const float2 s0 = __fmul2_rn(kw, __fmul2_rn(S, rinv));
+  const float2 z = __fmul2_rn(make_float2(Q.nbl2e, Q.nbl2e), bs2);
+  s1 = __fmul2_rn(s0, make_float2(ex2_approx(z.x), ex2_approx(z.y)));
 }
 
 __device__ __forceinline__ float4 lds_f4(const char *base, uint32_t off) {
@@ -470,7 +514,8 @@ template <int SCHEME, bool NW1, int OPT, bool BATCH, bool UV, bool EXACT>
 __device__ __forceinline__ void tilel_node(const StepParams &P, const Params32 &Qn,
                                            const DevPtrs &D, const BCTable &T, const StepArgs &A,
                                            const TileShared &S, const uint2 *sb, int64_t i, int il,
-                                           uint8_t fl, int len, uint32_t word, float4 ui4) {
+                                           uint8_t fl, int len, uint32_t word, float4 ui4,
+                                           const float4 *vpre, const float2 *fpre) {
   constexpr bool KV = !(OPT & OPT_CONTACT) && !BATCH;
   constexpr bool FAST = !(OPT & (OPT_NOFAIL | OPT_CONTACT));
   const int ng = (len + 3) >> 2;
@@ -488,7 +533,43 @@ __device__ __forceinline__ void tilel_node(const StepParams &P, const Params32 &
       for (int w = 0; w * 32 < len; w++) word |= D.bits[(int64_t)w * P.npad + i];
     full = word != 0u;
   }
-  if (FAST && !full) {
+  if (FAST && !full && !EXACT) {
+    // bonds in pairs (lane x: bonds 0, 2 of a group; lane y: bonds 1, 3),
+    // each lane summing its own share of the force
+    float mx = 0.f;  // largest S^2 r of the row
+    float2 fx = make_float2(0.f, 0.f), fy = make_float2(0.f, 0.f);
+    uint2 nxt = ng > 0 ? sb[0] : make_uint2(0u, 0u);  // ids one group ahead
+#pragma unroll 2
+    for (int g = 0; g < ng; g++) {
+      const uint2 cur = nxt;
+      if (g + 1 < ng) nxt = sb[32 * (g + 1)];
+      const uint32_t o[4] = {cur.x & 0xffffu, cur.x >> 16, cur.y & 0xffffu, cur.y >> 16};
+      float4 xj[4];
+      float vj[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        xj[q] = lds_f4(S.xu, o[q]);
+        vj[q] = UV ? kvu : lds_f(S.vol, o[q] >> 2);
+      }
+#pragma unroll
+      for (int p = 0; p < 2; p++) {
+        const float4 A = xj[2 * p], B = xj[2 * p + 1];
+        const float2 dx = make_float2(__fsub_rn(A.x, xi.x), __fsub_rn(B.x, xi.x));
+        const float2 dy = make_float2(__fsub_rn(A.y, xi.y), __fsub_rn(B.y, xi.y));
+        const float2 ex = make_float2(__fsub_rn(A.z, xi.z), __fsub_rn(B.z, xi.z));
+        const float2 ey = make_float2(__fsub_rn(A.w, xi.w), __fsub_rn(B.w, xi.w));
+        float2 s1, bs2;
+        tile_bond_pair<OPT, KV, UV>(Qn, dx, dy, ex, ey, make_float2(vj[2 * p], vj[2 * p + 1]),
+                                    s1, bs2);
+        mx = fmax3(mx, bs2.x, bs2.y);
+        fx = __ffma2_rn(s1, dx, fx);
+        fy = __ffma2_rn(s1, dy, fy);
+      }
+    }
+    fi[0] = __fadd_rn(fx.x, fx.y);
+    fi[1] = __fadd_rn(fy.x, fy.y);
+    full = mx > Qn.ksc_on;
+  } else if (FAST && !full) {
     float mx = 0.f;  // largest S^2 r of the row
     uint2 nxt = ng > 0 ? sb[0] : make_uint2(0u, 0u);  // ids one group ahead
 #pragma unroll 2
@@ -567,7 +648,7 @@ __device__ __forceinline__ void tilel_node(const StepParams &P, const Params32 &
     if (len & 31) nw &= (1u << (len & 31)) - 1u;
     if (nw) D.bits[NW1 ? i : (int64_t)((len - 1) >> 5) * P.npad + i] = word | nw;
   }
-  integrate_node32<2, SCHEME>(P, Qn, D, T, A, i, fl, uih, uil, fi);
+  integrate_node32<2, SCHEME>(P, Qn, D, T, A, i, fl, uih, uil, fi, vpre, fpre);
 }
 
 template <int SCHEME, bool NW1, int OPT, bool BATCH, bool UV>
@@ -581,6 +662,9 @@ __global__ void __launch_bounds__(kTileNodes, 4)
   __shared__ float2 s_ul[kTileMaxLocal];
   constexpr bool KV = !(OPT & OPT_CONTACT) && !BATCH;
   __shared__ uint8_t s_fl[(OPT & OPT_NOFAIL) ? kTileMaxLocal : 1];
+  // the tile's own velocity pairs and previous forces, for the epilogue
+  __shared__ __align__(16) float4 s_vown[kTileNodes];
+  __shared__ __align__(16) float2 s_fown[kTileNodes];
   __shared__ __align__(8) uint64_t s_bar;
   __shared__ float s_wspan[kTileNodes / 32];
   extern __shared__ __align__(128) unsigned char s_ids[];  // the tile's id block
@@ -589,18 +673,26 @@ __global__ void __launch_bounds__(kTileNodes, 4)
   const int64_t t0 = (int64_t)tb * kTileNodes;
   const int64_t sl0 = 8 * (int64_t)tb;
   const int64_t ib0 = D.sell_ptr[sl0];
+  const int nt = (int)min((int64_t)kTileNodes, P.n - t0);
+  // A whole tile's own v (and f of the previous step) arrive by bulk copies
+  // on the same barrier as its id block (contiguous, 16-byte aligned: tiles
+  // start at multiples of 256 nodes); a partial last tile reads them directly.
+  const bool vpre = nt == kTileNodes;
+  const bool fpre = vpre && SCHEME == NLM_VELOCITY_VERLET && !A.first;
   if (threadIdx.x == 0) {
     mbar_init(&s_bar, 1);
     const int64_t sl1 = min(sl0 + 8, (P.n + 31) >> 5);
     const uint32_t bytes = (uint32_t)(2 * (D.sell_ptr[sl1] - ib0));
-    if (bytes > 0)
-      bulk_copy_g2s(s_ids, D.tile_boff + ib0, bytes, &s_bar);
-    else
-      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&s_bar)) : "memory");
+    const uint32_t vb = vpre ? kTileNodes * sizeof(float4) : 0u;
+    const uint32_t fb = fpre ? kTileNodes * sizeof(float2) : 0u;
+    mbar_arrive_expect(&s_bar, bytes + vb + fb);
+    if (bytes > 0) bulk_copy_g2s(s_ids, D.tile_boff + ib0, bytes, &s_bar);
+    if (vb > 0)
+      bulk_copy_g2s(s_vown, D.v32[SCHEME == NLM_VELOCITY_VERLET ? 0 : A.cur] + t0, vb, &s_bar);
+    if (fb > 0) bulk_copy_g2s(s_fown, reinterpret_cast<const float2 *>(D.f32) + t0, fb, &s_bar);
   }
   const int h0 = D.tile_hptr[tb];
   const int nh = D.tile_hptr[tb + 1] - h0;
-  const int nt = (int)min((int64_t)kTileNodes, P.n - t0);
   const float4 *ucur = D.u32[A.cur];
   const float4 po = __ldg(D.pos32 + t0);
   const float2 plo = __half22float2(*reinterpret_cast<const __half2 *>(&po.w));
@@ -619,13 +711,6 @@ __global__ void __launch_bounds__(kTileNodes, 4)
   const float4 ui4 = il < nt ? __ldg(ucur + i) : make_float4(0.f, 0.f, 0.f, 0.f);
   const float4 pown = il < nt ? __ldg(D.pos32 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
   const uint8_t fown = ((OPT & OPT_NOFAIL) && il < nt) ? D.flags[i] : 0;
-  if (own) {
-    // the integrator's velocity and force reads, brought into L1 early
-    const float4 *vp = D.v32[SCHEME == NLM_VELOCITY_VERLET ? 0 : A.cur] + i;
-    const float2 *fp = reinterpret_cast<const float2 *>(D.f32) + i;
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(vp));
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(fp));
-  }
   // Staging: the thread's own tile node was loaded with the early loads
   // above; halo entries come two per thread per round, their ids loaded
   // together and then their nodes together, so a thread waits for memory
@@ -692,14 +777,16 @@ __global__ void __launch_bounds__(kTileNodes, 4)
   if (!own) return;
   const Params32 &Qn = BATCH ? static_cast<const Params32 *>(D.qtab)[D.slice_spec[i >> 5]] : Q;
   const uint2 *sb = reinterpret_cast<const uint2 *>(s_ids) + ((rbase - ib0) >> 2) + (i & 31);
+  const float4 *vp = vpre ? &s_vown[il] : nullptr;
+  const float2 *fp = fpre ? &s_fown[il] : nullptr;
   const TileShared S{reinterpret_cast<const char *>(s_xu), reinterpret_cast<const char *>(s_vol),
                      reinterpret_cast<const char *>(s_ul), s_fl};
   if (exact)
     tilel_node<SCHEME, NW1, OPT, BATCH, UV, true>(P, Qn, D, T, A, S, sb, i, il, fl, len, word,
-                                                  ui4);
+                                                  ui4, vp, fp);
   else
     tilel_node<SCHEME, NW1, OPT, BATCH, UV, false>(P, Qn, D, T, A, S, sb, i, il, fl, len, word,
-                                                   ui4);
+                                                   ui4, vp, fp);
 }
 
 // Dynamic shared memory above the default 48 KB for the tile-frame kernel's

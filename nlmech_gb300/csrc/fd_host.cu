@@ -966,6 +966,10 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
     } else {
       TRY(h->alloc(&D.es_ab, n));
       TRY(cudaMemsetAsync(D.es_ab, 0, sizeof(float2) * n, s));
+      float *minv;
+      TRY(h->alloc(&minv, n));
+      TRY(launch_es_minv32(mw, minv, n, s));
+      D.minv32 = minv;
     }
   }
   TRY(h->alloc(&D.err, 1));

@@ -37,6 +37,7 @@ struct DevPtrs {
   float *f32;      // FP32C force density, S per node
   // ElasticState
   const double *mw64;     // weighted volume m_i
+  const float *minv32;    // FP32C: 1 / m_i formed in FP64, rounded once
   double *theta64;        // FP64: dilatation theta_i
   float2 *es_ab;          // FP32C: t = a |X| + b e coefficients per node
   int *err;               // device error flag
@@ -115,6 +116,7 @@ cudaError_t launch_pipe_commit32(int64_t n, int64_t nbits, const int *bad, const
                                  float4 *u_now, float4 *u_next, float4 *v, float2 *f,
                                  uint32_t *bits, const uint32_t *bits_saved, cudaStream_t s);
 cudaError_t launch_es_setup(const StepParams &P, const DevPtrs &D, double *mw, cudaStream_t s);
+cudaError_t launch_es_minv32(const double *mw, float *minv, int64_t n, cudaStream_t s);
 cudaError_t launch_damage(const StepParams &P, const DevPtrs &D, int cur, bool fp32,
                           bool es, float *phi, float *Z, cudaStream_t s);
 cudaError_t launch_reaction(const StepParams &P, const DevPtrs &D, int cur, bool fp32,

@@ -100,6 +100,14 @@ __device__ __forceinline__ float ex2_approx(float x) {
   return y;
 }
 
+// largest of three (sm_100 and later: one instruction); NaN inputs are
+// ignored as by fmaxf
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+  float m;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(m) : "f"(a), "f"(b), "f"(c));
+  return m;
+}
+
 // ---- packed FP32 pairs (sm_100 and later: one instruction for both lanes) --
 __device__ __forceinline__ float2 sub_f32x2(float2 a, float2 b) {
   unsigned long long ra, rb, rd;
@@ -121,13 +129,17 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
   // make the initialised barrier visible to the copy engine (async proxy)
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
-// One arrival that also announces `bytes` of copies, then the copy of
-// `bytes` (16-byte aligned addresses, a multiple of 16 bytes) completing on it.
-__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes,
-                                              uint64_t *bar) {
+// One arrival that also announces `bytes` of copies to complete on the
+// barrier (the sum of the copies issued after it).
+__device__ __forceinline__ void mbar_arrive_expect(uint64_t *bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
                "r"(bytes)
                : "memory");
+}
+// The copy of `bytes` (16-byte aligned addresses, a multiple of 16 bytes)
+// completing on the barrier.
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes,
+                                              uint64_t *bar) {
   asm volatile(
       "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
           "r"(smem_u32(dst)),
@@ -248,18 +260,37 @@ static __device__ __noinline__ void bc_df(const DevPtrs &D, const BCTable &T, in
   v = df_from_double(dv);
 }
 
+// Internal force plus the external force of a Force_BC node, summed in FP64
+// and rounded once.  Out of line for the same reason as bc_df: inlined, its
+// conversions and FP64 additions were if-converted into every node's path,
+// where each FP64 warp instruction holds the SM's FP64 pipe for many cycles
+// (GB300: 2 FP64 operations per SM and cycle).
+struct F3 {
+  float c[3];
+};
+template <int DIM>
+static __device__ __noinline__ F3 fext_add32(const DevPtrs &D, int64_t i, F3 f) {
+  double fe[3];
+  ld_node<DIM>(D.fext, i, fe);
+  for (int c = 0; c < DIM; c++) f.c[c] = (float)(fe[c] + (double)f.c[c]);
+  return f;
+}
+
 // FP32C integrator epilogue (same phase structure as integrate_node64).
 template <int DIM, int SCHEME>
 __device__ __forceinline__ void integrate_node32(const StepParams &P, const Params32 &Q,
                                                  const DevPtrs &D, const BCTable &T,
                                                  const StepArgs &A, int64_t i, uint8_t fl,
                                                  const float uih[3], const float uil[3],
-                                                 const float fint[3]) {
+                                                 const float fint[3],
+                                                 const float4 *vpre = nullptr,
+                                                 const float2 *fpre = nullptr) {
+  // vpre, fpre (2-D): the node's velocity pair and previous force, already
+  // staged in shared memory by the caller
   float f[3] = {fint[0], fint[1], fint[2]};
   if (fl & FLAG_FBC) {
-    double fe[3];
-    ld_node<DIM>(D.fext, i, fe);
-    for (int c = 0; c < DIM; c++) f[c] = (float)(fe[c] + (double)fint[c]);
+    const F3 r = fext_add32<DIM>(D, i, F3{{fint[0], fint[1], fint[2]}});
+    for (int c = 0; c < 3; c++) f[c] = r.c[c];
   }
   const int ref = (fl & 7) ? D.bcref[i] : -1;
   double t_now = 0., t_next = 0.;
@@ -270,12 +301,15 @@ __device__ __forceinline__ void integrate_node32(const StepParams &P, const Para
   df un[3], vn[3];
   if (SCHEME == NLM_VELOCITY_VERLET) {
     float vh_[3], vl_[3];
-    ld_pair<DIM>(D.v32[0], i, vh_, vl_);
+    if (DIM == 2 && vpre)
+      ld_pair<DIM>(vpre, 0, vh_, vl_);
+    else
+      ld_pair<DIM>(D.v32[0], i, vh_, vl_);
     const bool FIRST = A.first;
     float fp[3] = {0.f, 0.f, 0.f};
     if (!FIRST) {
       if (DIM == 2) {
-        const float2 a = reinterpret_cast<const float2 *>(D.f32)[i];
+        const float2 a = fpre ? *fpre : reinterpret_cast<const float2 *>(D.f32)[i];
         fp[0] = a.x;
         fp[1] = a.y;
       } else {
@@ -310,7 +344,10 @@ __device__ __forceinline__ void integrate_node32(const StepParams &P, const Para
     st_pair<DIM>(D.v32[0], i, vn);
   } else {
     float vh_[3], vl_[3];
-    ld_pair<DIM>(D.v32[A.cur], i, vh_, vl_);
+    if (DIM == 2 && vpre)
+      ld_pair<DIM>(vpre, 0, vh_, vl_);
+    else
+      ld_pair<DIM>(D.v32[A.cur], i, vh_, vl_);
 #pragma unroll
     for (int c = 0; c < DIM; c++) {
       if (!(fl >> c & 1)) {

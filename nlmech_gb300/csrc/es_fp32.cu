@@ -269,8 +269,8 @@ template <int DIM, bool FORCE>
 __device__ __forceinline__ int es_stage_tile(const Params32 &Q, const DevPtrs &D,
                                              const float4 *ucur, int64_t t0, int nt, float4 *s_x,
                                              float4 *s_u, float *s_b, int tb) {
-  const int h0 = D.tile_hptr[tb];
-  const int nh = D.tile_hptr[tb + 1] - h0;
+  const int nh = D.tile_hstride;  // halo lists padded to one stride
+  const int64_t h0 = (int64_t)tb * nh;
   Node32<DIM> no;
   ld_pos<DIM>(D, t0, no);
   float uoh[3], uol[3];
@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(kTileNodes)
       es_pair_vec<DIM>(xi, ui, xa, ua, xb, ub, X, et);
       es_ext32_pair<DIM>(X, et, Y, Xl, iY, e);
       const float2 z = __fadd2_rn(e, __fmul2_rn(nsc, Xl));  // e - s_c |X|
-      const float2 t = __fmul2_rn(__fadd2_rn(cu2, make_float2(-Xl.x, -Xl.y)), ih2);
+      const float2 t = __fmul2_rn(__ffma2_rn(Xl, make_float2(-1.f, -1.f), cu2), ih2);  // (cu - |X|) / h
       const float2 om = make_float2(fminf(1.f, t.x), fminf(1.f, t.y));
       float2 w = __fmul2_rn(__fmul2_rn(Xl, e), om);
       w = make_float2(va ? w.x : 0.f, vb ? w.y : 0.f);
@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(kTileNodes, 4)
       es_ext32_pair<DIM>(X, et, Y, Xl, iY, e);
       const float2 tsum = __ffma2_rn(__fadd2_rn(bi2, make_float2(s_b[ja], s_b[jb])), e,
                                      __fmul2_rn(__fadd2_rn(ai2, make_float2(ua.w, ub.w)), Xl));
-      const float2 t = __fmul2_rn(__fadd2_rn(cu2, make_float2(-Xl.x, -Xl.y)), ih2);
+      const float2 t = __fmul2_rn(__ffma2_rn(Xl, make_float2(-1.f, -1.f), cu2), ih2);  // (cu - |X|) / h
       const float2 om = make_float2(fminf(1.f, t.x), fminf(1.f, t.y));
       float2 s = __fmul2_rn(__fmul2_rn(__fmul2_rn(tsum, om), make_float2(xa.w, xb.w)), iY);
       // a broken bond carries no force

@@ -293,8 +293,8 @@ __global__ void __launch_bounds__(kTileNodes, 3)
   __shared__ uint8_t s_fl[(OPT & OPT_NOFAIL) ? kTileMaxLocal : 1];
   const int tb = A.tiles ? A.tiles[blockIdx.x] : (int)blockIdx.x;
   const int64_t t0 = (int64_t)tb * kTileNodes;
-  const int h0 = D.tile_hptr[tb];
-  const int nh = D.tile_hptr[tb + 1] - h0;
+  const int nh = D.tile_hstride;  // halo lists padded to one stride
+  const int64_t h0 = (int64_t)tb * nh;
   const int nt = (int)min((int64_t)kTileNodes, P.n - t0);
   const float4 *ucur = D.u32[A.cur];
   for (int e = threadIdx.x; e < kTileNodes + nh; e += blockDim.x) {
@@ -443,13 +443,13 @@ __device__ __forceinline__ void tile_bond_pair(const Params32 &Q, float2 dx, flo
   const float2 de = __ffma2_rn(dy, ey, __fmul2_rn(dx, ex));
   const float2 rinv = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
   const float2 r = __fmul2_rn(r2, rinv);
-  float2 kw;
+  float2 kw;  // fma(-r, a, b) formed as fma(r, -a, b): the same value
   if (UV) {
-    const float2 t = __ffma2_rn(make_float2(-r.x, -r.y), make_float2(Q.kv_ih, Q.kv_ih),
+    const float2 t = __ffma2_rn(r, make_float2(-Q.kv_ih, -Q.kv_ih),
                                 make_float2(Q.kv_cuih, Q.kv_cuih));
     kw = make_float2(fminf(Q.kv_uniform, t.x), fminf(Q.kv_uniform, t.y));
   } else {
-    const float2 t = __ffma2_rn(make_float2(-r.x, -r.y), make_float2(Q.inv_h, Q.inv_h),
+    const float2 t = __ffma2_rn(r, make_float2(-Q.inv_h, -Q.inv_h),
                                 make_float2(Q.cu_ih, Q.cu_ih));
     const float2 kv = KV ? vj : __fmul2_rn(make_float2(Q.K1, Q.K1), vj);
     kw = __fmul2_rn(kv, make_float2(fminf(1.f, t.x), fminf(1.f, t.y)));
@@ -460,8 +460,8 @@ __device__ __forceinline__ void tile_bond_pair(const Params32 &Q, float2 dx, flo
     if (Q.infl_type == 1) {
       j = __ffma2_rn(make_float2(Q.a1, Q.a1), rr, make_float2(Q.a0, Q.a0));
     } else {
-      const float c = Q.ibeta * 1.4426950408889634f;
-      const float2 z = __fmul2_rn(__fmul2_rn(make_float2(-rr.x, -rr.y), rr), make_float2(c, c));
+      const float c = Q.ibeta * 1.4426950408889634f;  // (-rr rr) c = (rr rr) (-c)
+      const float2 z = __fmul2_rn(__fmul2_rn(rr, rr), make_float2(-c, -c));
       j = __fmul2_rn(make_float2(Q.alpha, Q.alpha), make_float2(ex2_approx(z.x), ex2_approx(z.y)));
     }
     kw = __fmul2_rn(kw, j);
@@ -539,7 +539,7 @@ __device__ __forceinline__ void tilel_node(const StepParams &P, const Params32 &
     float mx = 0.f;  // largest S^2 r of the row
     float2 fx = make_float2(0.f, 0.f), fy = make_float2(0.f, 0.f);
     uint2 nxt = ng > 0 ? sb[0] : make_uint2(0u, 0u);  // ids one group ahead
-#pragma unroll 2
+#pragma unroll 1
     for (int g = 0; g < ng; g++) {
       const uint2 cur = nxt;
       if (g + 1 < ng) nxt = sb[32 * (g + 1)];
@@ -691,8 +691,8 @@ __global__ void __launch_bounds__(kTileNodes, 4)
       bulk_copy_g2s(s_vown, D.v32[SCHEME == NLM_VELOCITY_VERLET ? 0 : A.cur] + t0, vb, &s_bar);
     if (fb > 0) bulk_copy_g2s(s_fown, reinterpret_cast<const float2 *>(D.f32) + t0, fb, &s_bar);
   }
-  const int h0 = D.tile_hptr[tb];
-  const int nh = D.tile_hptr[tb + 1] - h0;
+  const int nh = D.tile_hstride;
+  const int64_t h0 = (int64_t)tb * nh;
   const float4 *ucur = D.u32[A.cur];
   const float4 po = __ldg(D.pos32 + t0);
   const float2 plo = __half22float2(*reinterpret_cast<const __half2 *>(&po.w));
@@ -719,7 +719,7 @@ __global__ void __launch_bounds__(kTileNodes, 4)
   auto stage = [&](int e, const float4 a, const float4 u, uint8_t f) {
     const float2 lo = __half22float2(*reinterpret_cast<const __half2 *>(&a.w));
     const float dux = (u.x - uo.x) + (u.z - uo.z), duy = (u.y - uo.y) + (u.w - uo.w);
-    span = fmaxf(span, fmaxf(fabsf(dux), fabsf(duy)));
+    span = fmax3(span, fabsf(dux), fabsf(duy));
     s_xu[e] = make_float4(fmaf(lo.x - plo.x, Q.inv_lo, a.x - po.x),
                           fmaf(lo.y - plo.y, Q.inv_lo, a.y - po.y), dux, duy);
     if (!UV) s_vol[e] = KV ? Q.K1 * a.z : a.z;

@@ -55,9 +55,9 @@ struct DevPtrs {
   // (16 x index; 2-D RNPBond tile-frame kernel)
   const uint16_t *tile_boff;
   int tile_ids_bytes;    // largest id block of a tile (8 slices of tile_boff), bytes
-  const int *tile_hptr;  // tiles + 1
-  const int *tile_halo;
+  const int *tile_halo;  // halo lists, tile_hstride slots per tile (-1: empty)
   int tile_nmax;         // largest staged node list of any tile
+  int tile_hstride;      // halo slots per tile: tile t's list is tile_halo[t * stride ...]
 };
 
 // Tile decomposition: kTileNodes consecutive (Morton-ordered) nodes per

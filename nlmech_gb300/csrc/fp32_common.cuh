@@ -325,7 +325,9 @@ __device__ __forceinline__ void integrate_node32(const StepParams &P, const Para
       if (!(fl >> c & 1)) {
         const df cf = df_cmul(Q.c_hi, Q.c_lo, f[c]);
         df vm = v;
-        if (!FIRST) vm = df_add(df_add(v, df_cmul(Q.c_hi, Q.c_lo, fp[c])), cf);
+        // v^m = v^{m-1} + fact (f^{m-1} + f^m): the two FP32 forces summed
+        // once in FP32 (one rounding, at the level of their own FP32 error)
+        if (!FIRST) vm = df_add(v, df_cmul(Q.c_hi, Q.c_lo, __fadd_rn(fp[c], f[c])));
         vn[c] = vm;
         const df vh2 = df_add(vm, cf);
         un[c] = df_add({uih[c], uil[c]}, df_mul_c(vh2, Q.dt_hi, Q.dt_lo));

@@ -119,21 +119,20 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
   if (boff_too && ids_max > kTileIdsMaxBytes) return NLM_OK;
   if (in.lres)
     for (int64_t t = 0; t < nt; t++) halo[t] = std::move(halo_slots[t]);
-  std::vector<int> hptr(nt + 1, 0);
+  // Every tile's halo list is padded with empty slots (-1) to the longest,
+  // so tile t's list starts at t x stride: a kernel finds it without a
+  // dependent load of per-tile offsets.
   size_t nmax = 0;
-  for (int64_t t = 0; t < nt; t++) {
-    hptr[t + 1] = hptr[t] + (int)halo[t].size();
-    nmax = std::max(nmax, halo[t].size());
-  }
-  std::vector<int> hall(std::max(1, hptr[nt]));
-  for (int64_t t = 0; t < nt; t++) std::copy(halo[t].begin(), halo[t].end(), hall.begin() + hptr[t]);
+  for (int64_t t = 0; t < nt; t++) nmax = std::max(nmax, halo[t].size());
+  if ((int64_t)nmax * nt > (int64_t)INT32_MAX) return NLM_OK;
+  std::vector<int> hall(std::max<int64_t>(1, (int64_t)nmax * nt), -1);
+  for (int64_t t = 0; t < nt; t++)
+    std::copy(halo[t].begin(), halo[t].end(), hall.begin() + t * (int64_t)nmax);
   uint16_t *d_l = nullptr;
-  int *d_hp = nullptr, *d_h = nullptr;
+  int *d_h = nullptr;
   NLM_CUDA(h->alloc(&d_l, lidx.size()));
-  NLM_CUDA(h->alloc(&d_hp, hptr.size()));
   NLM_CUDA(h->alloc(&d_h, hall.size()));
   NLM_CUDA(cudaMemcpyAsync(d_l, lidx.data(), sizeof(uint16_t) * lidx.size(), cudaMemcpyHostToDevice, h->stream));
-  NLM_CUDA(cudaMemcpyAsync(d_hp, hptr.data(), sizeof(int) * hptr.size(), cudaMemcpyHostToDevice, h->stream));
   NLM_CUDA(cudaMemcpyAsync(d_h, hall.data(), sizeof(int) * hall.size(), cudaMemcpyHostToDevice, h->stream));
   uint16_t *d_b = nullptr;
   if (boff_too) {
@@ -145,9 +144,9 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
   h->D.tile_lidx = d_l;
   h->D.tile_boff = d_b;
   h->D.tile_ids_bytes = (int)ids_max;
-  h->D.tile_hptr = d_hp;
   h->D.tile_halo = d_h;
   h->D.tile_nmax = kTileNodes + (int)nmax;
+  h->D.tile_hstride = (int)nmax;
   ok = true;
   if (need_out) *need_out = std::move(need);
   return NLM_OK;

@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <type_traits>
 
 #include "fp32_common.cuh"
 
@@ -436,35 +437,44 @@ __device__ __forceinline__ void tile_bond_core(const Params32 &Q, float2 d, floa
 // operations: every lane value equals what tile_bond_core gives that bond
 // (the same separately rounded operations; rsqrt and exp2 per lane).
 // Returns s1 = s0 ex (the unbroken bond's force per unit xi) and bs2.
-template <int OPT, bool KV, bool UV>
+// INTERIOR: both bonds lie where the volume factor is 1 (a row's interior
+// prefix, with a constant influence function): kw is K1 V (or V_j's term)
+// itself, the value the general form gives there, without forming r.
+template <int OPT, bool KV, bool UV, bool INTERIOR = false>
 __device__ __forceinline__ void tile_bond_pair(const Params32 &Q, float2 dx, float2 dy, float2 ex,
                                                float2 ey, float2 vj, float2 &s1, float2 &bs2) {
   const float2 r2 = __ffma2_rn(dy, dy, __ffma2_rn(dx, dx, make_float2(1e-30f, 1e-30f)));
   const float2 de = __ffma2_rn(dy, ey, __fmul2_rn(dx, ex));
   const float2 rinv = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
-  const float2 r = __fmul2_rn(r2, rinv);
-  float2 kw;  // fma(-r, a, b) formed as fma(r, -a, b): the same value
-  if (UV) {
-    const float2 t = __ffma2_rn(r, make_float2(-Q.kv_ih, -Q.kv_ih),
-                                make_float2(Q.kv_cuih, Q.kv_cuih));
-    kw = make_float2(fminf(Q.kv_uniform, t.x), fminf(Q.kv_uniform, t.y));
+  float2 kw;
+  if (INTERIOR) {
+    kw = UV ? make_float2(Q.kv_uniform, Q.kv_uniform)
+            : (KV ? vj : __fmul2_rn(make_float2(Q.K1, Q.K1), vj));
   } else {
-    const float2 t = __ffma2_rn(r, make_float2(-Q.inv_h, -Q.inv_h),
-                                make_float2(Q.cu_ih, Q.cu_ih));
-    const float2 kv = KV ? vj : __fmul2_rn(make_float2(Q.K1, Q.K1), vj);
-    kw = __fmul2_rn(kv, make_float2(fminf(1.f, t.x), fminf(1.f, t.y)));
-  }
-  if (!(OPT & OPT_CONSTJ) && Q.infl_type != 0) {
-    const float2 rr = __fmul2_rn(r, make_float2(Q.inv_delta, Q.inv_delta));
-    float2 j;
-    if (Q.infl_type == 1) {
-      j = __ffma2_rn(make_float2(Q.a1, Q.a1), rr, make_float2(Q.a0, Q.a0));
+    const float2 r = __fmul2_rn(r2, rinv);
+    // fma(-r, a, b) formed as fma(r, -a, b): the same value
+    if (UV) {
+      const float2 t = __ffma2_rn(r, make_float2(-Q.kv_ih, -Q.kv_ih),
+                                  make_float2(Q.kv_cuih, Q.kv_cuih));
+      kw = make_float2(fminf(Q.kv_uniform, t.x), fminf(Q.kv_uniform, t.y));
     } else {
-      const float c = Q.ibeta * 1.4426950408889634f;  // (-rr rr) c = (rr rr) (-c)
-      const float2 z = __fmul2_rn(__fmul2_rn(rr, rr), make_float2(-c, -c));
-      j = __fmul2_rn(make_float2(Q.alpha, Q.alpha), make_float2(ex2_approx(z.x), ex2_approx(z.y)));
+      const float2 t = __ffma2_rn(r, make_float2(-Q.inv_h, -Q.inv_h),
+                                  make_float2(Q.cu_ih, Q.cu_ih));
+      const float2 kv = KV ? vj : __fmul2_rn(make_float2(Q.K1, Q.K1), vj);
+      kw = __fmul2_rn(kv, make_float2(fminf(1.f, t.x), fminf(1.f, t.y)));
     }
-    kw = __fmul2_rn(kw, j);
+    if (!(OPT & OPT_CONSTJ) && Q.infl_type != 0) {
+      const float2 rr = __fmul2_rn(r, make_float2(Q.inv_delta, Q.inv_delta));
+      float2 j;
+      if (Q.infl_type == 1) {
+        j = __ffma2_rn(make_float2(Q.a1, Q.a1), rr, make_float2(Q.a0, Q.a0));
+      } else {
+        const float c = Q.ibeta * 1.4426950408889634f;  // (-rr rr) c = (rr rr) (-c)
+        const float2 z = __fmul2_rn(__fmul2_rn(rr, rr), make_float2(-c, -c));
+        j = __fmul2_rn(make_float2(Q.alpha, Q.alpha), make_float2(ex2_approx(z.x), ex2_approx(z.y)));
+      }
+      kw = __fmul2_rn(kw, j);
+    }
   }
   const float2 a = __fmul2_rn(de, rinv);  // S r
   const float2 S = __fmul2_rn(a, rinv);
@@ -514,8 +524,8 @@ template <int SCHEME, bool NW1, int OPT, bool BATCH, bool UV, bool EXACT>
 __device__ __forceinline__ void tilel_node(const StepParams &P, const Params32 &Qn,
                                            const DevPtrs &D, const BCTable &T, const StepArgs &A,
                                            const TileShared &S, const uint2 *sb, int64_t i, int il,
-                                           uint8_t fl, int len, uint32_t word, float4 ui4,
-                                           const float4 *vpre, const float2 *fpre) {
+                                           uint8_t fl, int len, int nint, uint32_t word,
+                                           float4 ui4, const float4 *vpre, const float2 *fpre) {
   constexpr bool KV = !(OPT & OPT_CONTACT) && !BATCH;
   constexpr bool FAST = !(OPT & (OPT_NOFAIL | OPT_CONTACT));
   const int ng = (len + 3) >> 2;
@@ -535,14 +545,12 @@ __device__ __forceinline__ void tilel_node(const StepParams &P, const Params32 &
   }
   if (FAST && !full && !EXACT) {
     // bonds in pairs (lane x: bonds 0, 2 of a group; lane y: bonds 1, 3),
-    // each lane summing its own share of the force
+    // each lane summing its own share of the force; the row's interior
+    // prefix (nint bonds, whole groups) skips the volume factor
     float mx = 0.f;  // largest S^2 r of the row
     float2 fx = make_float2(0.f, 0.f), fy = make_float2(0.f, 0.f);
-    uint2 nxt = ng > 0 ? sb[0] : make_uint2(0u, 0u);  // ids one group ahead
-#pragma unroll 1
-    for (int g = 0; g < ng; g++) {
-      const uint2 cur = nxt;
-      if (g + 1 < ng) nxt = sb[32 * (g + 1)];
+    auto group = [&](const uint2 cur, auto interior) {
+      constexpr bool IN = decltype(interior)::value;
       const uint32_t o[4] = {cur.x & 0xffffu, cur.x >> 16, cur.y & 0xffffu, cur.y >> 16};
       float4 xj[4];
       float vj[4];
@@ -559,12 +567,26 @@ __device__ __forceinline__ void tilel_node(const StepParams &P, const Params32 &
         const float2 ex = make_float2(__fsub_rn(A.z, xi.z), __fsub_rn(B.z, xi.z));
         const float2 ey = make_float2(__fsub_rn(A.w, xi.w), __fsub_rn(B.w, xi.w));
         float2 s1, bs2;
-        tile_bond_pair<OPT, KV, UV>(Qn, dx, dy, ex, ey, make_float2(vj[2 * p], vj[2 * p + 1]),
-                                    s1, bs2);
+        tile_bond_pair<OPT, KV, UV, IN>(Qn, dx, dy, ex, ey,
+                                        make_float2(vj[2 * p], vj[2 * p + 1]), s1, bs2);
         mx = fmax3(mx, bs2.x, bs2.y);
         fx = __ffma2_rn(s1, dx, fx);
         fy = __ffma2_rn(s1, dy, fy);
       }
+    };
+    const int gi = min(nint >> 2, ng);
+    uint2 nxt = ng > 0 ? sb[0] : make_uint2(0u, 0u);  // ids one group ahead
+#pragma unroll 1
+    for (int g = 0; g < gi; g++) {
+      const uint2 cur = nxt;
+      if (g + 1 < ng) nxt = sb[32 * (g + 1)];
+      group(cur, std::true_type{});
+    }
+#pragma unroll 1
+    for (int g = gi; g < ng; g++) {
+      const uint2 cur = nxt;
+      if (g + 1 < ng) nxt = sb[32 * (g + 1)];
+      group(cur, std::false_type{});
     }
     fi[0] = __fadd_rn(fx.x, fx.y);
     fi[1] = __fadd_rn(fy.x, fy.y);
@@ -706,6 +728,7 @@ __global__ void __launch_bounds__(kTileNodes, 4)
   const uint8_t fl = own ? D.flags[i] : 0;
   if (BATCH && (fl & FLAG_GHOST)) own = false;
   const int len = own ? D.rowlen[i] : 0;
+  const int nint = (own && D.row_int) ? D.row_int[i] : 0;
   const int64_t rbase = own ? D.sell_ptr[i >> 5] : ib0;
   const uint32_t word = (NW1 && own) ? D.bits[i] : 0u;
   const float4 ui4 = il < nt ? __ldg(ucur + i) : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -782,11 +805,11 @@ __global__ void __launch_bounds__(kTileNodes, 4)
   const TileShared S{reinterpret_cast<const char *>(s_xu), reinterpret_cast<const char *>(s_vol),
                      reinterpret_cast<const char *>(s_ul), s_fl};
   if (exact)
-    tilel_node<SCHEME, NW1, OPT, BATCH, UV, true>(P, Qn, D, T, A, S, sb, i, il, fl, len, word,
-                                                  ui4, vp, fp);
+    tilel_node<SCHEME, NW1, OPT, BATCH, UV, true>(P, Qn, D, T, A, S, sb, i, il, fl, len, nint,
+                                                  word, ui4, vp, fp);
   else
-    tilel_node<SCHEME, NW1, OPT, BATCH, UV, false>(P, Qn, D, T, A, S, sb, i, il, fl, len, word,
-                                                   ui4, vp, fp);
+    tilel_node<SCHEME, NW1, OPT, BATCH, UV, false>(P, Qn, D, T, A, S, sb, i, il, fl, len, nint,
+                                                   word, ui4, vp, fp);
 }
 
 // Dynamic shared memory above the default 48 KB for the tile-frame kernel's

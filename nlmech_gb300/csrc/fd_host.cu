@@ -334,10 +334,20 @@ int launch_step(nlm_fd *h, const StepArgs &a0) {
   return NLM_OK;
 }
 
-int build_tiles(nlm_fd *h, const int64_t *sell_ptr_dev, int max_local) {
+int build_tiles(nlm_fd *h, const int64_t *sell_ptr_dev, int max_local, const double *x) {
   TileInputs in{h->n, h->nnz, h->nslices, h->sell_entries, h->D.cols, sell_ptr_dev,
                 &h->rowptr, &h->perm, max_local,
                 h->lattice_res.empty() ? nullptr : &h->lattice_res};
+  // Interior prefixes of the rows, for RNPBond with a constant influence
+  // function: a bond with r <= check_low - 1e-3 h has volume factor 1 in
+  // FP32 too, as long as the tile frame's rounding (2^-24 of the tile's
+  // extent per coordinate) and the FP32 forming of r stay far below the
+  // 1e-3 h margin: tiles up to 1000 h across.
+  if (h->material == NLM_MAT_RNP_BOND && h->P.infl_type == 0 && h->P.h > 0.) {
+    in.xc = x;
+    in.r_int = h->P.check_low - 1e-3 * h->P.h;
+    in.ext_max = 1000. * h->P.h;
+  }
   return build_tile_store(h, in, h->tile_ok, &h->tile_need);
 }
 
@@ -781,7 +791,7 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
   D.bits = bits;
   if (tile_able &&
       (h->decomp == NLM_DECOMP_TILE || h->decomp == NLM_DECOMP_TILE_LOCAL || want_tune)) {
-    int rc_t = build_tiles(h, st.ptr, es_model ? kTileMaxLocalES : kTileMaxLocal);
+    int rc_t = build_tiles(h, st.ptr, es_model ? kTileMaxLocalES : kTileMaxLocal, d->x);
     if (rc_t) return bail(rc_t);
     if ((h->decomp == NLM_DECOMP_TILE || h->decomp == NLM_DECOMP_TILE_LOCAL) && !h->tile_ok)
       return bail(fail(NLM_ERR_UNSUPPORTED, "a tile's halo exceeds the tile store limit"));

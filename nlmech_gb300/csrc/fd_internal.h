@@ -58,6 +58,9 @@ struct DevPtrs {
   const int *tile_halo;  // halo lists, tile_hstride slots per tile (-1: empty)
   int tile_nmax;         // largest staged node list of any tile
   int tile_hstride;      // halo slots per tile: tile t's list is tile_halo[t * stride ...]
+  // 2-D RNPBond tile-frame kernel: per node the number of leading bonds of
+  // its row (a multiple of 4) whose volume factor is certainly 1, or null
+  const uint8_t *row_int;
 };
 
 // Tile decomposition: kTileNodes consecutive (Morton-ordered) nodes per

@@ -29,6 +29,12 @@ struct TileInputs {
   const std::vector<int> *perm;        // internal -> caller id (for tile_need), or null
   int max_local;                       // largest staged list allowed
   const std::vector<uint8_t> *lres = nullptr;  // lattice residues per node, or null
+  // interior prefixes (2-D RNPBond store): caller-order positions (3 per
+  // node, with perm), the radius below which a bond is certainly outside
+  // the volume-correction band, and the largest tile extent for which the
+  // tile frame's rounding stays far below the margin in that radius
+  const double *xc = nullptr;
+  double r_int = 0., ext_max = 0.;
 };
 
 template <class H>
@@ -49,6 +55,10 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
   std::vector<uint16_t> lidx(in.sell_entries + 4, 0);
   std::vector<uint16_t> boff(boff_too ? in.sell_entries + 4 : 0, 0);
   std::vector<int> too_big(1, 0);
+  // per node: how many leading bonds of its row (whole groups of four) lie
+  // within r_int, where the volume factor min(1, (check_up - r) / h) is 1
+  const bool rint_too = boff_too && in.xc && in.perm && in.r_int > 0.;
+  std::vector<uint8_t> rint(rint_too ? n : 0, 0);
   std::vector<int> need(nt, -1);
   std::vector<std::vector<int>> halo_slots(nt);  // lattice layout: halo by slot, -1 = empty
   unsigned nthr = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
@@ -87,6 +97,33 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
       if (kTileNodes + nstaged > max_local) {
         too_big[0] = 1;
         continue;
+      }
+      if (rint_too) {
+        const std::vector<int> &pm = *in.perm;
+        auto X = [&](int64_t k) { return in.xc + 3 * (int64_t)pm[k]; };
+        const double *xo = X(a);
+        double ext = 0.;
+        for (int64_t i = a; i < b; i++) {
+          const double *xi = X(i);
+          ext = std::max(ext, std::max(std::fabs(xi[0] - xo[0]), std::fabs(xi[1] - xo[1])));
+          for (int64_t q = rp[i]; q < rp[i + 1]; q++) {
+            const double *xj = X(cols[q]);
+            ext = std::max(ext, std::max(std::fabs(xj[0] - xo[0]), std::fabs(xj[1] - xo[1])));
+          }
+        }
+        // the split (hi, lo) positions carry ~2^-35 of |x|: keep that far
+        // below the margin too
+        const bool near = std::max(std::fabs(xo[0]), std::fabs(xo[1])) <= 1000. * in.ext_max;
+        if (ext <= in.ext_max && near)
+          for (int64_t i = a; i < b; i++) {
+            const double *xi = X(i);
+            int64_t k = 0;
+            for (int64_t q = rp[i]; q < rp[i + 1] && k < 252; q++, k++) {
+              const double *xj = X(cols[q]);
+              if (!(std::hypot(xj[0] - xi[0], xj[1] - xi[1]) <= in.r_int)) break;
+            }
+            rint[i] = (uint8_t)(k & ~int64_t(3));
+          }
       }
       for (int64_t i = a; i < b; i++) {
         const int64_t base = sptr[i >> 5] + 4 * (i & 31);
@@ -134,6 +171,11 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
   NLM_CUDA(h->alloc(&d_h, hall.size()));
   NLM_CUDA(cudaMemcpyAsync(d_l, lidx.data(), sizeof(uint16_t) * lidx.size(), cudaMemcpyHostToDevice, h->stream));
   NLM_CUDA(cudaMemcpyAsync(d_h, hall.data(), sizeof(int) * hall.size(), cudaMemcpyHostToDevice, h->stream));
+  uint8_t *d_r = nullptr;
+  if (rint_too) {
+    NLM_CUDA(h->alloc(&d_r, rint.size()));
+    NLM_CUDA(cudaMemcpyAsync(d_r, rint.data(), rint.size(), cudaMemcpyHostToDevice, h->stream));
+  }
   uint16_t *d_b = nullptr;
   if (boff_too) {
     NLM_CUDA(h->alloc(&d_b, boff.size()));
@@ -143,6 +185,7 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
   NLM_CUDA(cudaStreamSynchronize(h->stream));
   h->D.tile_lidx = d_l;
   h->D.tile_boff = d_b;
+  h->D.row_int = d_r;
   h->D.tile_ids_bytes = (int)ids_max;
   h->D.tile_halo = d_h;
   h->D.tile_nmax = kTileNodes + (int)nmax;

@@ -567,3 +567,30 @@ def test_step_host_banded_rejects_nonfinite(gpu):
     pin[1].numpy()[n - 5, 0] = st0[1][n - 5, 0]
     m.step_host_ptr(*ptrs, nsteps=1)
     assert m.time() > t0
+
+
+def test_tile_frame_interior_prefix_is_exact(gpu):
+    """The tile-frame kernel evaluates the leading bonds of a row that lie
+    certainly inside the horizon's interior (r <= check_low - 1e-3 h, where
+    the volume factor min(1, (check_up - r) / h) is 1) without forming the
+    factor (rnpBond.cpp:242-256); it does so for a constant influence
+    function only.  The linear influence function J = 1 + 0 r / delta has
+    the same constants and multiplies every bond by exactly 1, but takes the
+    general path for every bond.  Both runs of the 100 x 100 plate (crack
+    growing, 600 steps) agree bit for bit."""
+    import dataclasses
+    p0 = configs.config0()
+    p1 = dataclasses.replace(p0, material=dataclasses.replace(
+        p0.material, influence_type=1, influence_params=[1.0, 0.0]))
+    out = []
+    for p in (p0, p1):
+        m = gpu.FDModel(p, precision=abi.FP32C, decomposition=abi.DECOMP_TILE_LOCAL)
+        pre = np.count_nonzero(m.bond_state())
+        m.run(600)
+        out.append((m.state(), m.bond_state(), pre))
+        m.close()
+    (s0, b0, pre0), (s1, b1, _) = out
+    for a, b in zip(s0, s1):
+        assert np.array_equal(a, b)
+    assert np.array_equal(b0, b1)
+    assert np.count_nonzero(b0) > pre0  # the crack grew

@@ -424,16 +424,22 @@ typedef struct nlm_qs_params {
                           at most guess_accept times that of the plain
                           start (<= 0: 0.1)                                  */
   int krylov_launch;   /* 0: the FP32 Krylov solve runs two launches per
-                          iteration (default; 30 us per iteration on the
-                          200 x 200 plate); 1: one cooperative launch per
-                          solve with grid barriers between its phases where
-                          the device allows it (37 us per iteration there)  */
+                          iteration (default; 46.6 us per iteration with the
+                          Newton work around it on the 200 x 200 plate);
+                          1: one cooperative launch per solve with grid
+                          barriers between its phases where the device
+                          allows it (50.2 us per iteration there)          */
   double wait_limit_s; /* bound of each grid-barrier wait of that launch
                           (<= 0: 1 s); a wait that runs out ends the solve
                           with NLM_ERR_TIMEOUT and the handle stays usable   */
   int barrier_extra;   /* testing the bound only: arrivals each barrier waits
                           for beyond the launched blocks (0 in use; > 0 makes
                           every wait run out)                                */
+  double lin_tol_gamma; /* > 0: a Newton iteration whose residual is already
+                          near the target solves to the looser relative
+                          tolerance min(0.1, gamma * target / ||r||), never
+                          tighter than lin_tol (a forcing term after
+                          Eisenstat and Walker); 0: lin_tol throughout      */
 } nlm_qs_params;
 
 typedef struct nlm_qs_stats {

@@ -160,6 +160,7 @@ class QSParams(C.Structure):
         ("krylov_launch", C.c_int),
         ("wait_limit_s", C.c_double),
         ("barrier_extra", C.c_int),
+        ("lin_tol_gamma", C.c_double),
     ]
 
 

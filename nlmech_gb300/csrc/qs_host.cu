@@ -72,9 +72,14 @@ int qs_newton(nlm_qs *q, double target, nlm_qs_stats *st) {
     if (c) st->break_rounds++;
     st->res_final = std::sqrt(rr);
     if (!(st->res_final > target) || it >= q->prm.max_newton) return NLM_OK;
+    // the linear tolerance: lin_tol, or looser when the residual is already
+    // near the target (a correction accurate to gamma * target / ||r|| of
+    // ||r|| leaves a linear residual of gamma * target)
+    double eta = q->prm.lin_tol;
+    if (q->prm.lin_tol_gamma > 0. && st->res_final > 0.)
+      eta = std::max(eta, std::min(0.1, q->prm.lin_tol_gamma * target / st->res_final));
     int li = 0;
-    e = qs_cg(h->P, h->D, q->W, q->W.res, q->W.dx, q->prm.lin_tol, q->prm.lin_max_iters, 8, &li,
-              &q->cg64,
+    e = qs_cg(h->P, h->D, q->W, q->W.res, q->W.dx, eta, q->prm.lin_max_iters, 8, &li, &q->cg64,
               h->stream);
     if (e == cudaSuccess) e = qs_add(h->P, q->W.dx, u, h->stream);
     if (e != cudaSuccess) return cuda_fail(e, "qs linear solve");

@@ -332,13 +332,15 @@ class Batch:
 
 def qs_params(max_newton=30, tol=1e-8, lin_max_iters=20000, lin_tol=1e-4, break_bonds=True,
               max_break_rounds=50, guess_accept=0.1, krylov_launch=0, wait_limit_s=1.0,
-              barrier_extra=0):
+              barrier_extra=0, lin_tol_gamma=0.0):
     """nlm_qs_params; krylov_launch 0: the FP32 Krylov solve in two launches
     per iteration, 1: in one cooperative launch per solve; barrier_extra > 0
-    only to test the bounded barrier wait (wait_limit_s) of the latter."""
+    only to test the bounded barrier wait (wait_limit_s) of the latter;
+    lin_tol_gamma > 0 loosens the Krylov tolerance of a Newton iteration
+    whose residual is already near the target."""
     return abi.QSParams(max_newton, tol, lin_max_iters, lin_tol, int(break_bonds),
                         max_break_rounds, guess_accept, int(krylov_launch),
-                        float(wait_limit_s), int(barrier_extra))
+                        float(wait_limit_s), int(barrier_extra), float(lin_tol_gamma))
 
 
 class QSModel:

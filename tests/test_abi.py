@@ -56,6 +56,8 @@ int main(void) {
          offsetof(nlm_fd_desc, dt), offsetof(nlm_fd_desc, u0), offsetof(nlm_material, es_sc));
   printf("%zu %zu %zu\n", sizeof(nlm_esqs_params), offsetof(nlm_esqs_params, lin_tol),
          offsetof(nlm_esqs_params, dt));
+  printf("%zu %zu %zu\n", sizeof(nlm_qs_params), offsetof(nlm_qs_params, wait_limit_s),
+         offsetof(nlm_qs_params, lin_tol_gamma));
   return 0;
 }
 """
@@ -69,7 +71,9 @@ int main(void) {
     offs = [abi.FDDesc.material.offset, abi.FDDesc.ubc.offset, abi.FDDesc.dt.offset,
             abi.FDDesc.u0.offset, abi.Material.es_sc.offset]
     esqs = [C.sizeof(abi.ESQSParams), abi.ESQSParams.lin_tol.offset, abi.ESQSParams.dt.offset]
-    assert [int(v) for v in out] == sizes + offs + esqs
+    qs = [C.sizeof(abi.QSParams), abi.QSParams.wait_limit_s.offset,
+          abi.QSParams.lin_tol_gamma.offset]
+    assert [int(v) for v in out] == sizes + offs + esqs + qs
 
 
 def test_invalid_arguments_are_status_codes(lib):

@@ -515,6 +515,9 @@ def qs_warm_start(steps, heldout=()):
     res = ws.evaluate(model, [p], steps, log=lambda *_: None)[p.name]
     res.update({"workload": "qs_rnp2d_200x200_d3h_precrack0.2W", "load_steps": steps,
                 "tolerance": "||r|| <= 1e-8 ||r0|| every load step",
+                "krylov": "PCG to 1e-4, loosened to min(0.1, %g target/||r||) for Newton "
+                          "iterations already near the target; the same in every arm"
+                          % ws.LIN_TOL_GAMMA,
                 "mlp": "10 -> 128 x 3 -> 2, bf16 GEMMs with fp32 accumulation",
                 "trained_on": "%d load steps of %d seeded pre-crack geometries (held out here)"
                               % (int(z["steps"]) * len(z["seeds"]), len(z["seeds"]))})

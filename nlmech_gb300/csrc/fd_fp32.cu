@@ -701,6 +701,11 @@ __global__ void __launch_bounds__(kTileNodes, 4)
   // start at multiples of 256 nodes); a partial last tile reads them directly.
   const bool vpre = nt == kTileNodes;
   const bool fpre = vpre && SCHEME == NLM_VELOCITY_VERLET && !A.first;
+  // Launched with programmatic stream serialization: everything up to
+  // griddepcontrol.wait reads only what no step writes (ids, positions,
+  // flags, row layout), so it overlaps the previous step's last blocks; the
+  // state (u, v, f, bond bits) is read after the wait, which returns once
+  // the previous step's writes are visible.
   if (threadIdx.x == 0) {
     mbar_init(&s_bar, 1);
     const int64_t sl1 = min(sl0 + 8, (P.n + 31) >> 5);
@@ -709,18 +714,12 @@ __global__ void __launch_bounds__(kTileNodes, 4)
     const uint32_t fb = fpre ? kTileNodes * sizeof(float2) : 0u;
     mbar_arrive_expect(&s_bar, bytes + vb + fb);
     if (bytes > 0) bulk_copy_g2s(s_ids, D.tile_boff + ib0, bytes, &s_bar);
-    if (vb > 0)
-      bulk_copy_g2s(s_vown, D.v32[SCHEME == NLM_VELOCITY_VERLET ? 0 : A.cur] + t0, vb, &s_bar);
-    if (fb > 0) bulk_copy_g2s(s_fown, reinterpret_cast<const float2 *>(D.f32) + t0, fb, &s_bar);
   }
   const int nh = D.tile_hstride;
   const int64_t h0 = (int64_t)tb * nh;
   const float4 *ucur = D.u32[A.cur];
   const float4 po = __ldg(D.pos32 + t0);
   const float2 plo = __half22float2(*reinterpret_cast<const __half2 *>(&po.w));
-  const float4 uo = ucur[t0];
-  // the node's own loads go out before the staging loop, so their latency
-  // overlaps it
   const int il = threadIdx.x;
   const int64_t i = t0 + il;
   bool own = il < nt;
@@ -730,14 +729,39 @@ __global__ void __launch_bounds__(kTileNodes, 4)
   const int len = own ? D.rowlen[i] : 0;
   const int nint = (own && D.row_int) ? D.row_int[i] : 0;
   const int64_t rbase = own ? D.sell_ptr[i >> 5] : ib0;
-  const uint32_t word = (NW1 && own) ? D.bits[i] : 0u;
-  const float4 ui4 = il < nt ? __ldg(ucur + i) : make_float4(0.f, 0.f, 0.f, 0.f);
   const float4 pown = il < nt ? __ldg(D.pos32 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
   const uint8_t fown = ((OPT & OPT_NOFAIL) && il < nt) ? D.flags[i] : 0;
-  // Staging: the thread's own tile node was loaded with the early loads
-  // above; halo entries come two per thread per round, their ids loaded
-  // together and then their nodes together, so a thread waits for memory
-  // twice per round rather than twice per staged node.
+  // the first round of halo entries (two per thread): ids and positions
+  int g0[2];
+  float4 a0[2];
+  uint8_t f0[2] = {0, 0};
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const int e = il + q * kTileNodes;
+    g0[q] = e < nh ? __ldg(D.tile_halo + h0 + e) : -1;
+  }
+#pragma unroll
+  for (int q = 0; q < 2; q++)
+    if (g0[q] >= 0) {
+      a0[q] = __ldg(D.pos32 + g0[q]);
+      if (OPT & OPT_NOFAIL) f0[q] = D.flags[g0[q]];
+    }
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  if (threadIdx.x == 0) {
+    if (vpre)
+      bulk_copy_g2s(s_vown, D.v32[SCHEME == NLM_VELOCITY_VERLET ? 0 : A.cur] + t0,
+                    kTileNodes * sizeof(float4), &s_bar);
+    if (fpre)
+      bulk_copy_g2s(s_fown, reinterpret_cast<const float2 *>(D.f32) + t0,
+                    kTileNodes * sizeof(float2), &s_bar);
+  }
+  const float4 uo = ucur[t0];
+  const uint32_t word = (NW1 && own) ? D.bits[i] : 0u;
+  const float4 ui4 = il < nt ? __ldg(ucur + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+  // Staging: two halo entries per thread per round, the first round's ids
+  // and positions already loaded above; then the displacements together,
+  // so a thread waits for memory once per round.
   float span = 0.f;  // largest |u - u_o| staged by this thread
   auto stage = [&](int e, const float4 a, const float4 u, uint8_t f) {
     const float2 lo = __half22float2(*reinterpret_cast<const __half2 *>(&a.w));
@@ -749,21 +773,25 @@ __global__ void __launch_bounds__(kTileNodes, 4)
     if (OPT & OPT_NOFAIL) s_fl[e] = f;
   };
   for (int base = 0; base < nh; base += 2 * kTileNodes) {
-    int g[2];
+    int g[2] = {g0[0], g0[1]};
+    float4 a[2] = {a0[0], a0[1]}, u[2];
+    uint8_t f[2] = {f0[0], f0[1]};
+    if (base > 0) {
 #pragma unroll
-    for (int q = 0; q < 2; q++) {
-      const int e = base + il + q * kTileNodes;
-      g[q] = e < nh ? __ldg(D.tile_halo + h0 + e) : -1;
+      for (int q = 0; q < 2; q++) {
+        const int e = base + il + q * kTileNodes;
+        g[q] = e < nh ? __ldg(D.tile_halo + h0 + e) : -1;
+      }
+#pragma unroll
+      for (int q = 0; q < 2; q++)
+        if (g[q] >= 0) {
+          a[q] = __ldg(D.pos32 + g[q]);
+          if (OPT & OPT_NOFAIL) f[q] = D.flags[g[q]];
+        }
     }
-    float4 a[2], u[2];
-    uint8_t f[2] = {0, 0};
 #pragma unroll
     for (int q = 0; q < 2; q++)
-      if (g[q] >= 0) {
-        a[q] = __ldg(D.pos32 + g[q]);
-        u[q] = __ldg(ucur + g[q]);
-        if (OPT & OPT_NOFAIL) f[q] = D.flags[g[q]];
-      }
+      if (g[q] >= 0) u[q] = __ldg(ucur + g[q]);
 #pragma unroll
     for (int q = 0; q < 2; q++)
       if (g[q] >= 0) stage(kTileNodes + base + il + q * kTileNodes, a[q], u[q], f[q]);
@@ -825,6 +853,30 @@ static void tile_ids_smem(K kernel, std::atomic<uint64_t> &done) {
     done.fetch_or(bit);
 }
 
+// One launch of the tile-frame kernel; with a.pdl set, with programmatic
+// stream serialization (the kernel's griddepcontrol.wait orders its state
+// reads after the previous step).
+template <class K>
+static void tilel_go(K kernel, const StepParams &P, const Params32 &Q, const DevPtrs &D,
+                     const BCTable &T, const StepArgs &a, unsigned grid, size_t dyn,
+                     cudaStream_t s) {
+  if (!a.pdl) {
+    kernel<<<grid, kTileNodes, dyn, s>>>(P, Q, D, T, a);
+    return;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kTileNodes);
+  cfg.dynamicSmemBytes = dyn;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, P, Q, D, T, a);
+}
+
 template <int SCHEME, int OPT, bool BATCH, bool UV>
 static void tilel_launch(const StepParams &P, const Params32 &Q, const DevPtrs &D,
                          const BCTable &T, const StepArgs &a, unsigned grid, size_t dyn,
@@ -832,11 +884,11 @@ static void tilel_launch(const StepParams &P, const Params32 &Q, const DevPtrs &
   if (P.nw1) {
     static std::atomic<uint64_t> opt{0};
     tile_ids_smem(k_rnp32_tilel<SCHEME, true, OPT, BATCH, UV>, opt);
-    k_rnp32_tilel<SCHEME, true, OPT, BATCH, UV><<<grid, kTileNodes, dyn, s>>>(P, Q, D, T, a);
+    tilel_go(k_rnp32_tilel<SCHEME, true, OPT, BATCH, UV>, P, Q, D, T, a, grid, dyn, s);
   } else {
     static std::atomic<uint64_t> opt{0};
     tile_ids_smem(k_rnp32_tilel<SCHEME, false, OPT, BATCH, UV>, opt);
-    k_rnp32_tilel<SCHEME, false, OPT, BATCH, UV><<<grid, kTileNodes, dyn, s>>>(P, Q, D, T, a);
+    tilel_go(k_rnp32_tilel<SCHEME, false, OPT, BATCH, UV>, P, Q, D, T, a, grid, dyn, s);
   }
 }
 

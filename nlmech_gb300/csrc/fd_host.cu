@@ -307,6 +307,9 @@ int lattice_relabel(nlm_fd *h, NeighborBuild &nb, int dim, int S, double mesh_h,
 int launch_step(nlm_fd *h, const StepArgs &a0) {
   StepArgs a = a0;
   if (a.i1 == 0) a.i1 = h->n;
+  // after the step-0 evaluation every step launch follows another step or a
+  // between-steps kernel that writes only state (u, v, f, bits, loads)
+  a.pdl = !a.first;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (h->timing && !h->capturing) {
     while (h->ev_used + 2 > h->ev_pool.size()) {

@@ -87,6 +87,11 @@ struct StepArgs {
   // (device array) instead of every tile
   const int *tiles;
   int64_t ntiles;
+  // the launch directly follows the model's previous step on its stream (no
+  // set-up kernel in between): the tile-frame kernel is then launched with
+  // programmatic stream serialization, its prologue overlapping that step's
+  // last blocks
+  bool pdl;
 };
 
 // Launchers (return cudaError_t of the launch).

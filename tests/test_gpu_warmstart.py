@@ -44,12 +44,14 @@ def test_trained_network_cuts_newton_work(gpu):
     0.2 W pre-crack, a geometry outside its training seeds, 100 load steps:
     every step of both runs converges to the same 1e-8 relative residual,
     the learned start needs at least 1.5x fewer Newton iterations and Krylov
-    iterations and less wall time than the plain previous-step start, and it
-    ends in the plain run's state (QuasiStaticModel.cpp:526-594)."""
+    iterations and at most half the wall time of the plain previous-step
+    start, and it ends in the plain run's state (QuasiStaticModel.cpp:526-594).
+    Both runs use the same Newton-Krylov settings (the evaluation's forcing
+    term)."""
     from nlmech_gb300 import warmstart as ws
     model = ws.load_model()
     p = configs.config4()
-    params = gpu.qs_params(max_newton=500)
+    params = gpu.qs_params(max_newton=500, lin_tol_gamma=ws.LIN_TOL_GAMMA)
     ra = ws.run_steps(p, 100, params)
     rb = ws.run_steps(p, 100, params, model=model)
     a, b = ws.summary(ra), ws.summary(rb)
@@ -57,7 +59,7 @@ def test_trained_network_cuts_newton_work(gpu):
     assert a["all_steps_converged"] and b["all_steps_converged"]
     assert a["newton_iters"] >= 1.5 * b["newton_iters"]
     assert a["cg_iters"] >= 1.5 * b["cg_iters"]
-    assert rb["wall_s"] < ra["wall_s"]
+    assert 2.0 * rb["wall_s"] <= ra["wall_s"], (ra["wall_s"], rb["wall_s"])
     du = np.linalg.norm(rb["u"] - ra["u"]) / np.linalg.norm(ra["u"])
     assert du <= 1e-6, du
     for st in rb["stats"]:

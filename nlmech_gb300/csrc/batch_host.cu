@@ -70,6 +70,9 @@ struct nlm_batch {
 namespace {
 
 int batch_launch(nlm_batch *b, StepArgs a) {
+  // after the step-0 evaluation a step follows another step or a kernel that
+  // writes only state: the tile-frame kernel may overlap it
+  a.pdl = !a.first;
   // every bucket on the tile-frame kernel: one launch over all of them (its
   // tiles take each node's own specimen constants, and a tile that straddles
   // two buckets is staged once instead of once per bucket)

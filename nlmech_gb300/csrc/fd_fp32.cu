@@ -746,8 +746,7 @@ __global__ void __launch_bounds__(kTileNodes, 4)
       a0[q] = __ldg(D.pos32 + g0[q]);
       if (OPT & OPT_NOFAIL) f0[q] = D.flags[g0[q]];
     }
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  asm volatile("griddepcontrol.wait;" ::: "memory");
+  pdl_trigger_and_wait();
   if (threadIdx.x == 0) {
     if (vpre)
       bulk_copy_g2s(s_vown, D.v32[SCHEME == NLM_VELOCITY_VERLET ? 0 : A.cur] + t0,
@@ -860,21 +859,7 @@ template <class K>
 static void tilel_go(K kernel, const StepParams &P, const Params32 &Q, const DevPtrs &D,
                      const BCTable &T, const StepArgs &a, unsigned grid, size_t dyn,
                      cudaStream_t s) {
-  if (!a.pdl) {
-    kernel<<<grid, kTileNodes, dyn, s>>>(P, Q, D, T, a);
-    return;
-  }
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(kTileNodes);
-  cfg.dynamicSmemBytes = dyn;
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, kernel, P, Q, D, T, a);
+  launch_pdl(kernel, grid, kTileNodes, dyn, s, a.pdl, P, Q, D, T, a);
 }
 
 template <int SCHEME, int OPT, bool BATCH, bool UV>

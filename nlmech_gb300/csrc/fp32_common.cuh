@@ -159,6 +159,30 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32
   return false;
 }
 
+// ---- launches with programmatic stream serialization ------------------------
+// With pdl set the kernel may start while the previous kernel on the stream
+// finishes its last blocks; it must read nothing that kernel writes before
+// its griddepcontrol.wait, which returns once those writes are visible.
+template <class K, class... Args>
+static cudaError_t launch_pdl(K kernel, unsigned grid, unsigned block, size_t dyn,
+                              cudaStream_t s, bool pdl, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = dyn;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+__device__ __forceinline__ void pdl_trigger_and_wait() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // ---- double-float arithmetic (error-free transformations) ------------------
 struct df {
   float hi, lo;

@@ -250,12 +250,22 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
                    [&](int a, int c) { return descs[a].n_nodes < descs[c].n_nodes; });
   b->off.assign(nspec, 0);
   b->n.assign(nspec, 0);
+  // the decomposition (explicit when every specimen names the same one)
+  int fixed = descs[0].decomposition;
+  for (int s = 1; s < nspec; s++)
+    if (descs[s].decomposition != fixed) fixed = NLM_DECOMP_AUTO;
+  const bool tiles_possible =
+      d0.dim == 2 && (fixed == NLM_DECOMP_AUTO || fixed == NLM_DECOMP_TILE_LOCAL);
+  // Specimens start at slice boundaries (32 nodes), or at tile boundaries
+  // (256) when the tile-frame kernel may run, so that a specimen's lattice
+  // patches are whole tiles.
+  const int64_t align = tiles_possible ? kTileNodes : 32;
   int64_t cursor = 0;
   for (int k = 0; k < nspec; k++) {
     const int s = b->order[k];
     b->off[s] = cursor;
     b->n[s] = descs[s].n_nodes;
-    cursor += ((descs[s].n_nodes + 31) / 32) * 32;
+    cursor += ((descs[s].n_nodes + align - 1) / align) * align;
   }
   const int64_t N = cursor;
   b->ntot = N;
@@ -268,11 +278,14 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
   BTRY(b->alloc(&rowptr, N + 1));
   std::vector<int64_t> hrow(N + 1, 0);
   std::vector<NeighborBuild> nbs(nspec);
+  std::vector<uint8_t> lres;  // lattice residues (combined layout), if relabelled
   b->perm.resize(nspec);
   b->bond_off.assign(nspec, 0);
   b->nbond.assign(nspec, 0);
   double xmax = 0.;
   int64_t nnz = 0;
+  std::vector<double> posh, rint;
+  double hmin = 1e300;
   for (int k = 0; k < nspec; k++) {
     const int s = b->order[k];
     const nlm_fd_desc &d = descs[s];
@@ -287,6 +300,14 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
       if (q) b->allocs.push_back(q);
     if (e != cudaSuccess)
       return bail(why.empty() ? cuda_fail(e, "neighbour build") : fail(NLM_ERR_INVALID, why));
+    if (tiles_possible && d.mesh_size > 0.) {
+      // each specimen on its own mesh lattice, as a single model's tiles
+      std::vector<uint8_t> lr;
+      if (int rc_l = lattice_relabel(nbs[s], d.dim, S, d.mesh_size, d.horizon, st, lr))
+        return bail(rc_l);
+      if (lres.empty()) lres.assign(N, 0);
+      std::copy(lr.begin(), lr.end(), lres.begin() + b->off[s]);
+    }
     b->perm[s].resize(d.n_nodes);
     std::vector<int64_t> rp(d.n_nodes + 1);
     BTRY(cudaMemcpyAsync(b->perm[s].data(), nbs[s].perm, sizeof(int) * d.n_nodes, cudaMemcpyDeviceToHost, st));
@@ -300,6 +321,21 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
     nnz += nbs[s].nnz;
     BTRY(cudaMemcpyAsync(pos64 + (size_t)S * b->off[s], nbs[s].pos, sizeof(double) * S * d.n_nodes,
                          cudaMemcpyDeviceToDevice, st));
+    if (tiles_possible) {
+      // internal-order positions and the interior radius per node (constant
+      // influence functions only), for the rows' interior prefixes
+      if (posh.empty()) {
+        posh.assign((size_t)S * N, 0.);
+        rint.assign(N, 0.);
+      }
+      BTRY(cudaMemcpyAsync(posh.data() + (size_t)S * b->off[s], nbs[s].pos,
+                           sizeof(double) * S * d.n_nodes, cudaMemcpyDeviceToHost, st));
+      if (d.material.influence_type == 0 && d.mesh_size > 0.) {
+        const double r = d.horizon - 0.5 * d.mesh_size - 1e-3 * d.mesh_size;
+        std::fill(rint.begin() + b->off[s], rint.begin() + b->off[s] + d.n_nodes, r);
+        hmin = std::min(hmin, d.mesh_size);
+      }
+    }
     for (int64_t q = 0; q < 3 * d.n_nodes; q++) xmax = std::max(xmax, std::fabs(d.x[q]));
   }
   hrow[N] = nnz;
@@ -353,9 +389,6 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
   D.sell_cols = ss.cols;
   // explicit decomposition: every specimen names the same one, used for all
   // buckets; NLM_DECOMP_AUTO (any specimen) autotunes per bucket
-  int fixed = descs[0].decomposition;
-  for (int s = 1; s < nspec; s++)
-    if (descs[s].decomposition != fixed) fixed = NLM_DECOMP_AUTO;
   if (fixed == NLM_DECOMP_TILE)
     return bail(fail(NLM_ERR_UNSUPPORTED, "a batch takes NLM_DECOMP_TILE_LOCAL, not TILE"));
   if (fixed != NLM_DECOMP_AUTO && fixed != NLM_DECOMP_THREAD && fixed != NLM_DECOMP_THREAD1 &&
@@ -363,7 +396,14 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
     return bail(fail(NLM_ERR_INVALID, "unknown decomposition"));
   if (b->dim == 2 && (fixed == NLM_DECOMP_AUTO || fixed == NLM_DECOMP_TILE_LOCAL)) {
     TileInputs tin{N, nnz, ss.nslices, ss.entries, cols, ss.ptr, &b->rowptr, nullptr,
-                   kTileMaxLocal};
+                   kTileMaxLocal, lres.empty() ? nullptr : &lres};
+    BTRY(cudaStreamSynchronize(st));  // posh
+    if (hmin < 1e300) {
+      tin.xin = posh.data();
+      tin.xs = S;
+      tin.r_int_node = rint.data();
+      tin.ext_max = 1000. * hmin;
+    }
     if (int rc_t = build_tile_store(b, tin, b->tile_ok, nullptr)) return bail(rc_t);
   }
   if (fixed == NLM_DECOMP_TILE_LOCAL && !b->tile_ok)
@@ -383,6 +423,7 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
   std::vector<double> volp(N, 0.);
   std::vector<uint16_t> rl(N, 0);
   bool any_nofail = false;
+  bool all_uniform = true;
   double span_min = 1e300;
   for (int s = 0; s < nspec; s++) {
     const nlm_fd_desc &d = descs[s];
@@ -400,6 +441,11 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
     int rc = rnp_constants(d.material, d.dim, d.horizon, Ps);
     if (rc) return bail(rc);
     if (Ps.contact) return bail(fail(NLM_ERR_UNSUPPORTED, "contact forces are not batched"));
+    // one volume for the specimen: its K1 V as a constant in its table
+    Ps.vol_uniform = d.n_nodes > 0 ? d.volume[0] : 0.;
+    for (int64_t i = 1; i < d.n_nodes && Ps.vol_uniform > 0.; i++)
+      if (d.volume[i] != d.volume[0]) Ps.vol_uniform = 0.;
+    all_uniform = all_uniform && Ps.vol_uniform > 0.;
     qtab[s] = make_p32(Ps);
     // the tile kernel decides per tile (specimens may share one): the
     // smallest span limit of all specimens
@@ -461,6 +507,7 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
   }
   (void)total_sets;
   P.nofail = any_nofail ? 1 : 0;
+  P.uv_specimens = all_uniform ? 1 : 0;
   Params32 *dq;
   BCTime *dbct;
   int *dss;

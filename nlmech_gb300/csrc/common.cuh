@@ -72,6 +72,7 @@ struct StepParams {
   double lo_scale;    // FP32C position lo parts are stored as half(lo * lo_scale)
   int nw1;            // 1 when every row fits one 32-bit bond-bit word
   double vol_uniform; // the common nodal volume when every node has the same one, else 0
+  int uv_specimens;   // batch: every specimen has one nodal volume (K1 V per specimen)
   double tile_span_max;  // > 0: tile-frame displacement span limit (batches: the
                          // smallest of the specimens'); 0: from this model's constants
   // integration

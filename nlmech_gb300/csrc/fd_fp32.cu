@@ -902,10 +902,11 @@ static void launch_opt(const StepParams &P, const Params32 &Q, const DevPtrs &D,
                 : (unsigned)((P.n + kTileNodes - 1) / kTileNodes);
     if (grid == 0) return;
     const size_t dyn = (size_t)D.tile_ids_bytes;
-    // one nodal volume for the whole model: K1 V as a constant
-    constexpr bool KV = !(OPT & OPT_CONTACT) && !BATCH;
-    if (KV && Q.kv_uniform > 0.f) {
-      tilel_launch<SCHEME, OPT, BATCH, KV>(P, Q, D, T, a, grid, dyn, s);
+    // one nodal volume for the whole model (for a batch: per specimen, the
+    // constants in each specimen's table): K1 V as a constant
+    constexpr bool UVOK = !(OPT & OPT_CONTACT);
+    if (UVOK && (BATCH ? P.uv_specimens != 0 : Q.kv_uniform > 0.f)) {
+      tilel_launch<SCHEME, OPT, BATCH, UVOK>(P, Q, D, T, a, grid, dyn, s);
     } else {
       tilel_launch<SCHEME, OPT, BATCH, false>(P, Q, D, T, a, grid, dyn, s);
     }

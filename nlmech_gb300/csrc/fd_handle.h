@@ -246,6 +246,8 @@ void nofail_flags(const double *x, int64_t n, double tol, int nreg, const nlm_no
                   std::vector<uint8_t> &interior);
 int check_nofail_regions(const nlm_fd_desc &d);
 int rnp_constants(const nlm_material &m, int dim, double delta, StepParams &P);
+int lattice_relabel(NeighborBuild &nb, int dim, int S, double mesh_h, double delta,
+                    cudaStream_t s, std::vector<uint8_t> &lres);
 int launch_step(nlm_fd *h, const StepArgs &a0);
 int apply_fbc(nlm_fd *h, double t);
 int apply_bc(nlm_fd *h, double t);

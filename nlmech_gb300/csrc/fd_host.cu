@@ -206,7 +206,7 @@ int rnp_constants(const nlm_material &m, int dim, double delta, StepParams &P) {
 // one pass.  Any node set works (the order is only a layout); only the
 // results' rounding changes.  lres receives each node's residue (new order):
 // (g_x mod 4, g_y mod 2) as a Morton code in 2-D, (g_x, g_y, g_z mod 2) in 3-D.
-int lattice_relabel(nlm_fd *h, NeighborBuild &nb, int dim, int S, double mesh_h,
+int lattice_relabel(NeighborBuild &nb, int dim, int S, double mesh_h, double delta,
                     cudaStream_t s, std::vector<uint8_t> &lres) {
   const int64_t n = nb.n, nnz = nb.nnz;
   if (n == 0) return NLM_OK;
@@ -247,7 +247,7 @@ int lattice_relabel(nlm_fd *h, NeighborBuild &nb, int dim, int S, double mesh_h,
     inv[key[k].second] = k;
   }
   // rank of a lattice offset: |o|^2, then its components
-  const int R = (int)std::ceil(h->P.delta / mesh_h) + 2, W = 2 * R + 1, Wz = D3 == 3 ? W : 1;
+  const int R = (int)std::ceil(delta / mesh_h) + 2, W = 2 * R + 1, Wz = D3 == 3 ? W : 1;
   std::vector<std::pair<std::array<int, 4>, int>> offs;
   for (int oz = (D3 == 3 ? -R : 0); oz <= (D3 == 3 ? R : 0); oz++)
     for (int oy = -R; oy <= R; oy++)
@@ -759,7 +759,7 @@ int nlm_fd_create(const nlm_fd_desc *d, nlm_fd **out) {
   h->nnz = nb.nnz;
   if (h->nnz > INT32_MAX) return bail(fail(NLM_ERR_INVALID, "too many bonds for one handle"));
   if (tile_able && d->mesh_size > 0.) {
-    int rc_l = lattice_relabel(h, nb, d->dim, S, d->mesh_size, s, h->lattice_res);
+    int rc_l = lattice_relabel(nb, d->dim, S, d->mesh_size, d->horizon, s, h->lattice_res);
     if (rc_l) return bail(rc_l);
   }
   SellStore st;

@@ -35,6 +35,11 @@ struct TileInputs {
   // tile frame's rounding stays far below the margin in that radius
   const double *xc = nullptr;
   double r_int = 0., ext_max = 0.;
+  // or: positions in the internal order (xs doubles per node) and a radius
+  // per node (a batch of specimens with their own mesh sizes)
+  const double *xin = nullptr;
+  int xs = 3;
+  const double *r_int_node = nullptr;
 };
 
 template <class H>
@@ -57,7 +62,8 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
   std::vector<int> too_big(1, 0);
   // per node: how many leading bonds of its row (whole groups of four) lie
   // within r_int, where the volume factor min(1, (check_up - r) / h) is 1
-  const bool rint_too = boff_too && in.xc && in.perm && in.r_int > 0.;
+  const bool rint_too =
+      boff_too && ((in.xc && in.perm && in.r_int > 0.) || (in.xin && in.r_int_node));
   std::vector<uint8_t> rint(rint_too ? n : 0, 0);
   std::vector<int> need(nt, -1);
   std::vector<std::vector<int>> halo_slots(nt);  // lattice layout: halo by slot, -1 = empty
@@ -99,8 +105,9 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
         continue;
       }
       if (rint_too) {
-        const std::vector<int> &pm = *in.perm;
-        auto X = [&](int64_t k) { return in.xc + 3 * (int64_t)pm[k]; };
+        auto X = [&](int64_t k) {
+          return in.xin ? in.xin + (int64_t)in.xs * k : in.xc + 3 * (int64_t)(*in.perm)[k];
+        };
         const double *xo = X(a);
         double ext = 0.;
         for (int64_t i = a; i < b; i++) {
@@ -117,10 +124,11 @@ int build_tile_store(H *h, const TileInputs &in, bool &ok, std::vector<int> *nee
         if (ext <= in.ext_max && near)
           for (int64_t i = a; i < b; i++) {
             const double *xi = X(i);
+            const double ri = in.r_int_node ? in.r_int_node[i] : in.r_int;
             int64_t k = 0;
             for (int64_t q = rp[i]; q < rp[i + 1] && k < 252; q++, k++) {
               const double *xj = X(cols[q]);
-              if (!(std::hypot(xj[0] - xi[0], xj[1] - xi[1]) <= in.r_int)) break;
+              if (!(std::hypot(xj[0] - xi[0], xj[1] - xi[1]) <= ri)) break;
             }
             rint[i] = (uint8_t)(k & ~int64_t(3));
           }

@@ -294,6 +294,17 @@ __device__ __forceinline__ int es_stage_tile(const Params32 &Q, const DevPtrs &D
   return nh;
 }
 
+// The ids of a warp's 32 rows (one slice of tile_lidx: 256 bytes per group
+// of four bonds, contiguous) brought into L2 before the staging, two 128-byte
+// lines per group, spread over the lanes; the bond loops then find them in
+// L2 instead of waiting on DRAM group by group.
+__device__ __forceinline__ void es_prefetch_ids(const DevPtrs &D, int64_t i, int len) {
+  const int gmax = __reduce_max_sync(0xffffffffu, (len + 3) >> 2);
+  const char *base = reinterpret_cast<const char *>(D.tile_lidx + D.sell_ptr[i >> 5]);
+  for (int k = threadIdx.x & 31; k < 2 * gmax; k += 32)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(base + 128 * k));
+}
+
 template <int DIM>
 __global__ void __launch_bounds__(kTileNodes)
     k_es_dil32_tile(const StepParams P, const Params32 Q, const ESConst32 E, const DevPtrs D,
@@ -303,6 +314,7 @@ __global__ void __launch_bounds__(kTileNodes)
   const int tb = blockIdx.x;
   const int64_t t0 = (int64_t)tb * kTileNodes;
   const int nt = (int)min((int64_t)kTileNodes, P.n - t0);
+  es_prefetch_ids(D, t0 + threadIdx.x, threadIdx.x < nt ? D.rowlen[t0 + threadIdx.x] : 0);
   es_stage_tile<DIM, false>(Q, D, D.u32[A.cur], t0, nt, s_x, s_u, nullptr, tb);
   __syncthreads();
   const int il = threadIdx.x;
@@ -417,6 +429,7 @@ __global__ void __launch_bounds__(kTileNodes, 4)
   const int64_t t0 = (int64_t)tb * kTileNodes;
   const int nt = (int)min((int64_t)kTileNodes, P.n - t0);
   const float4 *ucur = D.u32[A.cur];
+  es_prefetch_ids(D, t0 + threadIdx.x, threadIdx.x < nt ? D.rowlen[t0 + threadIdx.x] : 0);
   es_stage_tile<DIM, true>(Q, D, ucur, t0, nt, s_x, s_u, s_b, tb);
   __syncthreads();
   const int il = threadIdx.x;

@@ -688,7 +688,7 @@ __global__ void __launch_bounds__(kTileNodes, 4)
   __shared__ __align__(16) float4 s_vown[kTileNodes];
   __shared__ __align__(16) float2 s_fown[kTileNodes];
   __shared__ __align__(8) uint64_t s_bar;
-  __shared__ float s_wspan[kTileNodes / 32];
+  __shared__ __align__(16) float s_wspan[kTileNodes / 32];
   extern __shared__ __align__(128) unsigned char s_ids[];  // the tile's id block
   const int tb = A.tiles ? A.tiles[blockIdx.x]
                          : (int)blockIdx.x + (BATCH ? (int)(A.i0 / kTileNodes) : 0);
@@ -796,13 +796,16 @@ __global__ void __launch_bounds__(kTileNodes, 4)
       if (g[q] >= 0) stage(kTileNodes + base + il + q * kTileNodes, a[q], u[q], f[q]);
   }
   if (il < nt) stage(il, pown, ui4, fown);
-  // the tile's displacement span (NaN counts as too large)
-  for (int o = 16; o > 0; o >>= 1) span = fmaxf(span, __shfl_xor_sync(0xffffffffu, span, o));
-  if ((threadIdx.x & 31) == 0) s_wspan[threadIdx.x >> 5] = span != span ? 3e38f : span;
+  // the tile's displacement span (NaN counts as too large): non-negative
+  // floats order as their bit patterns, so one warp reduction takes the max
+  const float wspan = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(span)));
+  if ((threadIdx.x & 31) == 0) s_wspan[threadIdx.x >> 5] = wspan != wspan ? 3e38f : wspan;
   __syncthreads();
-  float bspan = 0.f;
-#pragma unroll
-  for (int w = 0; w < kTileNodes / 32; w++) bspan = fmaxf(bspan, s_wspan[w]);
+  static_assert(kTileNodes / 32 == 8, "eight warp spans");
+  const float4 w0 = reinterpret_cast<const float4 *>(s_wspan)[0];
+  const float4 w1 = reinterpret_cast<const float4 *>(s_wspan)[1];
+  const float bspan =
+      fmax3(fmax3(w0.x, w0.y, w0.z), fmax3(w0.w, w1.x, w1.y), fmaxf(w1.z, w1.w));
   const bool exact = bspan > Q.span_max;
   if (exact) {
     // block-uniform: restage eta's inputs as (hi, lo) pairs

@@ -314,7 +314,7 @@ DECOMP_NAMES = {1: "thread-per-node, 4-bond groups", 2: "warp-per-node",
                 5: "256-node tiles staged in shared memory, tile-frame FP32 bond data"}
 
 
-def survey_bytes(nnz, n):
+def hot_path_bytes(nnz, n):
     """Compulsory bytes of one FP32C 2-D RNPBond step in the hot-path byte
     model: 4 B neighbour id + 0.25 B bond bit read and write per directed
     bond; x (8 B FP32 offset) + V 4 + flags 1 + rowptr 4 + u read/write 32 +
@@ -450,7 +450,7 @@ def run_ours(a):
     # one step-kernel launch per step: the kernel's mean duration is the timed
     # region's device time over its steps (CUDA events on the handle's stream)
     kms = ms / a.steps
-    alg = survey_bytes(nnz, n)
+    alg = hot_path_bytes(nnz, n)
     achieved = alg / (kms * 1e-3) / 1e9
     traffic = profiled_traffic(dcode)
     out = {

@@ -988,8 +988,7 @@ __device__ __forceinline__ void drift_node32(const StepParams &P, const Params32
     if (!(fl >> c & 1)) {
       const df u{uh[c], ul[c]}, v{vh[c], vl[c]};
       if (P.scheme == NLM_VELOCITY_VERLET) {
-        const df vh2 = df_add(v, df_cmul(Q.c_hi, Q.c_lo, f[c]));
-        un[c] = df_add(u, df_mul_c(vh2, Q.dt_hi, Q.dt_lo));
+        un[c] = vv_drift(Q, u, v, f[c]);
         vn[c] = v;
       } else {
         const df inc = df_add(df_cmul(Q.c_hi, Q.c_lo, f[c]), df_mul_c(v, Q.dt_hi, Q.dt_lo));

@@ -214,6 +214,20 @@ __device__ __forceinline__ df df_mul_c(df x, float c_hi, float c_lo) {
   e = fmaf(x.lo, c_hi, fmaf(x.hi, c_lo, e));
   return fast_two_sum(p, e);
 }
+// x + y for a pair x and a float y
+__device__ __forceinline__ df df_add_f(df x, float y) {
+  const df s = two_sum(x.hi, y);
+  return fast_two_sum(s.hi, s.lo + x.lo);
+}
+// Velocity-Verlet drift of one dof, u + dt (v + fact f): the increments fact f
+// and dt v^{m+1/2} are formed in FP32 -- f is itself an FP32 sum, so their
+// rounding is at the level of its own error -- and added to the (hi, lo)
+// pairs without loss.  The fused step and the drift of a host-supplied state
+// both use it, so they agree bit for bit.
+__device__ __forceinline__ df vv_drift(const Params32 &Q, df u, df v, float f) {
+  const df vh2 = df_add_f(v, __fmul_rn(Q.c_hi, f));
+  return df_add_f(u, __fmul_rn(Q.dt_hi, vh2.hi));
+}
 __device__ __forceinline__ df df_from_double(double v) {
   const float h = __double2float_rn(v);
   return {h, __double2float_rn(v - (double)h)};
@@ -347,14 +361,12 @@ __device__ __forceinline__ void integrate_node32(const StepParams &P, const Para
     for (int c = 0; c < DIM; c++) {
       const df v{vh_[c], vl_[c]};
       if (!(fl >> c & 1)) {
-        const df cf = df_cmul(Q.c_hi, Q.c_lo, f[c]);
+        // v^m = v^{m-1} + fact (f^{m-1} + f^m), the increment in FP32 (the
+        // two forces summed once); then the drift to u^{m+1}
         df vm = v;
-        // v^m = v^{m-1} + fact (f^{m-1} + f^m): the two FP32 forces summed
-        // once in FP32 (one rounding, at the level of their own FP32 error)
-        if (!FIRST) vm = df_add(v, df_cmul(Q.c_hi, Q.c_lo, __fadd_rn(fp[c], f[c])));
+        if (!FIRST) vm = df_add_f(v, __fmul_rn(Q.c_hi, __fadd_rn(fp[c], f[c])));
         vn[c] = vm;
-        const df vh2 = df_add(vm, cf);
-        un[c] = df_add({uih[c], uil[c]}, df_mul_c(vh2, Q.dt_hi, Q.dt_lo));
+        un[c] = vv_drift(Q, {uih[c], uil[c]}, vm, f[c]);
       } else {
         df du, dv;
         if (!FIRST) {

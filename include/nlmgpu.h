@@ -385,8 +385,9 @@ int nlm_fd_set_graph(nlm_fd *h, int steps_per_graph);
  * node-count bucket over all specimens, each bucket with the decomposition
  * the autotuner picked for it (THREAD, THREAD1, WARP or, in 2-D,
  * TILE_LOCAL), or with the one every desc names when all name the same
- * (NLM_DECOMP_TILE is refused).  Per-specimen constants live in a table in
- * device memory.  Specimen ids below are positions in the descs array. */
+ * (NLM_DECOMP_TILE is refused); when every bucket takes TILE_LOCAL a step
+ * is a single launch.  Per-specimen constants live in a table in device
+ * memory.  Specimen ids below are positions in the descs array. */
 typedef struct nlm_batch nlm_batch;
 
 int nlm_batch_create(const nlm_fd_desc *descs, int n_specimens, nlm_batch **out);

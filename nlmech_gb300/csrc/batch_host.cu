@@ -279,6 +279,7 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
   std::vector<int64_t> hrow(N + 1, 0);
   std::vector<NeighborBuild> nbs(nspec);
   std::vector<uint8_t> lres;  // lattice residues (combined layout), if relabelled
+  bool relabel_all = true;    // the residue layout of the halo needs every specimen's
   b->perm.resize(nspec);
   b->bond_off.assign(nspec, 0);
   b->nbond.assign(nspec, 0);
@@ -300,6 +301,7 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
       if (q) b->allocs.push_back(q);
     if (e != cudaSuccess)
       return bail(why.empty() ? cuda_fail(e, "neighbour build") : fail(NLM_ERR_INVALID, why));
+    if (tiles_possible && !(d.mesh_size > 0.)) relabel_all = false;
     if (tiles_possible && d.mesh_size > 0.) {
       // each specimen on its own mesh lattice, as a single model's tiles
       std::vector<uint8_t> lr;
@@ -396,7 +398,7 @@ int nlm_batch_create(const nlm_fd_desc *descs, int nspec, nlm_batch **out) {
     return bail(fail(NLM_ERR_INVALID, "unknown decomposition"));
   if (b->dim == 2 && (fixed == NLM_DECOMP_AUTO || fixed == NLM_DECOMP_TILE_LOCAL)) {
     TileInputs tin{N, nnz, ss.nslices, ss.entries, cols, ss.ptr, &b->rowptr, nullptr,
-                   kTileMaxLocal, lres.empty() ? nullptr : &lres};
+                   kTileMaxLocal, (lres.empty() || !relabel_all) ? nullptr : &lres};
     BTRY(cudaStreamSynchronize(st));  // posh
     if (hmin < 1e300) {
       tin.xin = posh.data();
